@@ -1,0 +1,362 @@
+"""Numpy restatement of seistorch's 2D acoustic / elastic time stepping.
+
+TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``).
+
+Every function cites the reference file:line it restates (paths inside the
+seistorch project).  Arrays are (Nz, Nx) for models and (B, Nz, Nx) for
+wavefields; ``dtype`` selects the arithmetic (float64 for the oracle, float32
+for the CPU baseline).
+"""
+import numpy as np
+
+# ---------------------------------------------------------------- setup ---
+
+
+def fd_coefficients(order):
+    """Second-derivative Taylor weights c_1..c_M, M = order/2.
+
+    Restates ``even_intergrid`` (equations2d/acoustic.py:5-30): solve
+    sum_j c_j j^(2i) = [i == 0] for i < M (the weights of
+    u(x+j)+u(x-j)), then divide by j^2.  Order 2 -> [1], order 4 ->
+    [4/3, -1/12].
+    """
+    if order < 2 or order % 2:
+        raise ValueError(f"spatial order must be an even integer >= 2, got {order}")
+    m = order // 2
+    a = np.array([[float(j + 1) ** (2 * i) for j in range(m)] for i in range(m)])
+    rhs = np.zeros(m)
+    rhs[0] = 1.0
+    c = np.linalg.solve(a, rhs)
+    return c / np.array([(j + 1) ** 2 for j in range(m)], dtype=np.float64)
+
+
+def laplacian_kernel(order):
+    """(order+1)^2 cross stencil; centre = -4 sum(c)  (acoustic.py:32-53)."""
+    c = fd_coefficients(order)
+    r = order // 2
+    k = np.zeros((order + 1, order + 1))
+    k[r, r + 1:] = c
+    k[r, :r] = c[::-1]
+    k[r + 1:, r] = c
+    k[:r, r] = c[::-1]
+    k[r, r] = -4.0 * c.sum()
+    return k
+
+
+def pml_profile_2d(shape, N=50, multiple=False, dtype=np.float64):
+    """Damping profile d(z, x) (pml.py:29-59).
+
+    d0 = 1.5*1500/N*log10(1e4); per side a quadratic ramp over N+1 cells
+    (d0 at the outer edge, 0 at cell N); corners combine as
+    sqrt(dz^2 + dx^2); the top side is absent when ``multiple``.  The
+    reference computes this in torch's default dtype; ``dtype`` plays
+    that role here.
+    """
+    nz, nx = shape
+    d0 = (1.5 * 1500.0 / N) * np.log10(1e4) if N > 0 else 0.0
+    ramp = (d0 * np.linspace(0.0, 1.0, N + 1, dtype=dtype) ** 2)[::-1].astype(dtype)
+    dz = np.zeros((nz, nx), dtype)
+    dx = np.zeros((nz, nx), dtype)
+    if N > 0:
+        # pml.py:36-54 unpacks (nz, nx) as "Nx, Ny" and transposes at the
+        # end: its first array ramps along x at both sides, its second along
+        # z, whose top ramp is the one dropped for ``multiple``.
+        dx[:, 0:N + 1] = ramp[None, :]
+        dx[:, nx - N - 1:nx] = ramp[::-1][None, :]
+        if not multiple:
+            dz[0:N + 1, :] = ramp[:, None]
+        dz[nz - N - 1:nz, :] = ramp[::-1][:, None]
+    return np.sqrt(dz ** 2 + dx ** 2).astype(dtype)
+
+
+def habc_masks(nz, nx, w=50, multiple=False):
+    """Boolean strip masks (top, bottom, left, right) (habc.py:4-40).
+
+    top[r, x]  (r < w):  r <= x <= nx-1-r      (None when ``multiple``)
+    bottom: top mirrored in z; left[z, c] (c < w): c <= z and c <= nz-1-z,
+    with rows z < w all set when ``multiple``; right: left mirrored in x.
+    """
+    r = np.arange(w)[:, None]
+    x = np.arange(nx)[None, :]
+    top = (x >= r) & (x <= nx - 1 - r)
+    bottom = top[::-1].copy()
+    z = np.arange(nz)[:, None]
+    c = np.arange(w)[None, :]
+    first = ~((z < w) & (c > z))
+    zf = nz - 1 - z
+    second = ~((zf < w) & (c > zf))
+    left = first & second
+    right = left[:, ::-1].copy()
+    if multiple:
+        left[:w] = True
+        right[:w] = True
+        top = None
+    return top, bottom, left, right
+
+
+def habc_coefficients_2d(shape, N=50, multiple=False, dtype=np.float64):
+    """HABC blend weight b(z, x) (habc.py:42-81).
+
+    Along each side the weight falls linearly from 1 at the outer cell to 0
+    at cell N-1: d_vals[k] = (N-1-k)/(N-1) (torch.linspace(0,N,N)/N
+    flipped, in torch's default dtype -- ``dtype`` here).  Written side by
+    side in the order top, bottom, left, right through the masks of
+    ``habc_masks`` (later sides win).
+    """
+    nz, nx = shape
+    d = np.zeros((nz, nx), dtype)
+    if N <= 0:
+        return d
+    dv = (np.linspace(0.0, N, N, dtype=dtype) / dtype(N))[::-1].astype(dtype)
+    tm, bm, lm, rm = habc_masks(nz, nx, N, multiple)
+    if not multiple:
+        blk = np.repeat(dv[:, None], nx, 1)
+        d[:N][tm] = blk[tm]
+    blk = np.repeat(dv[::-1][:, None], nx, 1)
+    d[-N:][bm] = blk[bm]
+    blk = np.repeat(dv[None, :], nz, 0)
+    d[:, :N][lm] = blk[lm]
+    blk = np.repeat(dv[::-1][None, :], nz, 0)
+    d[:, -N:][rm] = blk[rm]
+    return d
+
+
+def ricker(fm, dt, T, delay=80, inverse=False):
+    """Ricker wavelet, rounded to float32 (utils.py:235-249)."""
+    i = np.arange(T, dtype=np.float64)
+    c = np.pi * fm * (i * dt - delay * dt)
+    p = -1.0 if inverse else 1.0
+    return (p * (1 - 2 * c ** 2) * np.exp(-c ** 2)).astype(np.float32)
+
+
+def pad_model(m, width, multiple=False):
+    """Edge padding by the boundary width, top unpadded with ``multiple``
+    (geom.py:213-240)."""
+    top = 0 if multiple else width
+    return np.pad(m, ((top, width), (width, width)), mode="edge")
+
+
+# ------------------------------------------------------------ stencils ---
+
+
+def laplacian(u, order, h, dtype=np.float64):
+    """Zero-padded cross-stencil Laplacian / h^2 of (B, Nz, Nx) fields
+    (acoustic.py:60-71, conv2d with padding=order/2)."""
+    u = np.asarray(u, dtype)
+    c = fd_coefficients(order).astype(dtype)
+    r = order // 2
+    nz, nx = u.shape[-2:]
+    up = np.pad(u, ((0, 0), (r, r), (r, r)))
+    out = dtype(-4.0 * fd_coefficients(order).sum()) * u
+    for j in range(1, r + 1):
+        out = out + c[j - 1] * (up[:, r + j:r + j + nz, r:r + nx] + up[:, r - j:r - j + nz, r:r + nx]
+                                + up[:, r:r + nz, r + j:r + j + nx] + up[:, r:r + nz, r - j:r - j + nx])
+    return out * dtype(1.0 / (h * h))
+
+
+def acoustic_step(vp, h1, h2, dt, h, d, order, dtype=np.float64):
+    """One 2nd-order acoustic PML step (acoustic.py:73-86).
+
+    y = (dt^-2 + d/dt)^-1 (2/dt^2 h1 - (dt^-2 - d/dt) h2 + vp^2 lap(h1));
+    returns (y, h1).
+    """
+    vp = np.asarray(vp, dtype)
+    d = np.asarray(d, dtype)
+    dt = dtype(dt)
+    lap = laplacian(h1, order, h, dtype)
+    y = (dt ** -2 + d / dt) ** -1 * (2 / dt ** 2 * h1 - (dt ** -2 - d / dt) * h2 + vp ** 2 * lap)
+    return y.astype(dtype), np.asarray(h1, dtype)
+
+
+def _one_way(u_now, u_pre, y, c, b, dt, h, depth_axis, from_end, w=50):
+    """HABC one-way extrapolation + blend for one side, over the 50-cell
+    strip (acoustic_habc.py:79-101).
+
+    Depth k counts cells from the outer edge.  With U(k) = u_now at depth k:
+      u_one = (2-lam-mu) U(k) + (lam+2mu) U(k+1) - mu U(k+2)
+              + (lam-1) P(k) - lam P(k+1),    lam = 2c dt/h, mu = c^2 dt^2/h^2
+    and the result is b*u_one + (1-b)*y.  The reference builds a 51-deep
+    slab and uses torch.roll, so U(k+2) at k = 49 wraps to depth 0
+    (acoustic_habc.py:93-96); that wrap is kept.
+    Returns an array of the strip's shape (w along depth_axis).
+    """
+    n = u_now.shape[depth_axis]
+
+    def take(a, k):
+        idx = (n - 1 - k) if from_end else k
+        return np.take(a, idx, axis=depth_axis)
+
+    out = []
+    for k in range(w):
+        k2 = (k + 2) if (k + 2) <= w else (k + 2) - (w + 1)
+        cc = take(c, k)
+        bb = take(b, k)
+        lam = 2 * cc * dt / h
+        mu = cc ** 2 * dt ** 2 / h ** 2
+        uo = ((2 - lam - mu) * take(u_now, k) + (lam + 2 * mu) * take(u_now, k + 1)
+              - mu * take(u_now, k2) + (lam - 1) * take(u_pre, k) - lam * take(u_pre, k + 1))
+        out.append(uo * bb + (1 - bb) * take(y, k))
+    st = np.stack(out, axis=depth_axis)
+    if from_end:
+        st = np.flip(st, axis=depth_axis)
+    return st
+
+
+def habc_apply(y, h1, h2, vp, b, dt, h, w=50, multiple=False, dtype=np.float64):
+    """Hybrid ABC on the four strips (acoustic_habc.py:147-204).
+
+    Strip results are scattered through the masks in the order top,
+    bottom, left, right (later sides win), then four 50-cell diagonals are
+    replaced by 0.5/0.5 averages: (i, i) top/left, (i, nx-w+i) top/right,
+    (nz-w+i, i) bottom/left, (nz-w+i, nx-w+i) bottom/right (the top ones
+    are skipped with ``multiple``).
+    """
+    y = np.array(y, dtype)
+    h1 = np.asarray(h1, dtype)
+    h2 = np.asarray(h2, dtype)
+    vp = np.asarray(vp, dtype)[None]
+    b = np.asarray(b, dtype)[None]
+    dt = dtype(dt)
+    h = dtype(h)
+    nz, nx = y.shape[-2:]
+    tm, bm, lm, rm = habc_masks(nz, nx, w, multiple)
+    yt = _one_way(h1, h2, y, vp, b, dt, h, 1, False, w)       # (B, w, nx) rows 0..w-1
+    yb = _one_way(h1, h2, y, vp, b, dt, h, 1, True, w)        # rows nz-w..nz-1
+    yl = _one_way(h1, h2, y, vp, b, dt, h, 2, False, w)       # cols 0..w-1
+    yr = _one_way(h1, h2, y, vp, b, dt, h, 2, True, w)        # cols nx-w..nx-1
+    out = y.copy()
+    if not multiple:
+        out[:, :w, :][:, tm] = yt[:, tm]
+    out[:, -w:, :][:, bm] = yb[:, bm]
+    out[:, :, :w][:, lm] = yl[:, lm]
+    out[:, :, -w:][:, rm] = yr[:, rm]
+    i = np.arange(w)
+    half = dtype(0.5)
+    if not multiple:
+        out[:, i, i] = half * yt[:, i, i] + half * yl[:, i, i]
+        out[:, i, nx - w + i] = half * yt[:, i, nx - w + i] + half * yr[:, i, i]
+    out[:, nz - w + i, i] = half * yb[:, i, i] + half * yl[:, nz - w + i, i]
+    out[:, nz - w + i, nx - w + i] = half * yb[:, i, nx - w + i] + half * yr[:, nz - w + i, i]
+    return out
+
+
+def acoustic_habc_step(vp, h1, h2, dt, h, b, order, multiple=False, dtype=np.float64):
+    """Undamped interior step then HABC (acoustic_habc.py:206-221)."""
+    vp = np.asarray(vp, dtype)
+    dt_ = dtype(dt)
+    lap = laplacian(h1, order, h, dtype)
+    y = (dt_ ** -2) ** -1 * (2 / dt_ ** 2 * np.asarray(h1, dtype) - dt_ ** -2 * np.asarray(h2, dtype)
+                             + vp ** 2 * lap)
+    y = habc_apply(y, h1, h2, vp, b, dt, h, 50, multiple, dtype)
+    return y, np.asarray(h1, dtype)
+
+
+def dfwd(a, axis):
+    """a[i] - a[i-1], zero at index 0 (equations2d/utils.py:3-25, forward)."""
+    out = a - np.roll(a, 1, axis=axis)
+    idx = [slice(None)] * a.ndim
+    idx[axis] = 0
+    out[tuple(idx)] = 0
+    return out
+
+
+def dbwd(a, axis):
+    """a[i+1] - a[i], zero at the last index (equations2d/utils.py:27-43)."""
+    out = np.roll(a, -1, axis=axis) - a
+    idx = [slice(None)] * a.ndim
+    idx[axis] = -1
+    out[tuple(idx)] = 0
+    return out
+
+
+def elastic_step(vp, vs, rho, vx, vz, txx, tzz, txz, dt, h, d, dtype=np.float64):
+    """Velocity-stress staggered step (elastic.py:7-37): stresses first
+    (A-8..A-10), then velocities from the new stresses; c = 0.5 dt d."""
+    vp, vs, rho, d = (np.asarray(a, dtype) for a in (vp, vs, rho, d))
+    vx, vz, txx, tzz, txz = (np.asarray(a, dtype) for a in (vx, vz, txx, tzz, txz))
+    dt = dtype(dt)
+    h = dtype(h)
+    lam = rho * (vp ** 2 - 2 * vs ** 2)
+    mu = rho * vs ** 2
+    c = dtype(0.5) * dt * d
+    vx_x = dfwd(vx, 2)
+    vz_z = dbwd(vz, 1)
+    vx_z = dfwd(vx, 1)
+    vz_x = dbwd(vz, 2)
+    ytxx = (1 + c) ** -1 * (dt / h * ((lam + 2 * mu) * vx_x + lam * vz_z) + (1 - c) * txx)
+    ytzz = (1 + c) ** -1 * (dt / h * ((lam + 2 * mu) * vz_z + lam * vx_x) + (1 - c) * tzz)
+    ytxz = (1 + c) ** -1 * (dt * mu / h * (vz_x + vx_z) + (1 - c) * txz)
+    txx_x = dbwd(ytxx, 2)
+    txz_z = dbwd(ytxz, 1)
+    tzz_z = dfwd(ytzz, 1)
+    txz_x = dfwd(ytxz, 2)
+    yvx = (1 + c) ** -1 * (dt / rho / h * (txx_x + txz_z) + (1 - c) * vx)
+    yvz = (1 + c) ** -1 * (dt / rho / h * (txz_x + tzz_z) + (1 - c) * vz)
+    return yvx, yvz, ytxx, ytzz, ytxz
+
+
+# ----------------------------------------------------------- time loop ---
+
+WAVEFIELDS = {"acoustic": ["h1", "h2"], "acoustic_habc": ["h1", "h2"],
+              "elastic": ["vx", "vz", "txx", "tzz", "txz"]}
+MODEL_PARAMS = {"acoustic": ["vp"], "acoustic_habc": ["vp"],
+                "elastic": ["vp", "vs", "rho"]}
+
+
+def forward(equation, models, d, dt, h, wavelet, sources, receivers, *,
+            order=2, multiple=False, source_type=None, receiver_type=None,
+            illumination=False, dtype=np.float64, nt=None, return_fields=False):
+    """Time loop of ``WaveRNN.forward`` (rnn.py:100-217).
+
+    sources:   per shot, a list of (z, x) padded-grid points (the mask
+               ``smask[b, z, x] = 1`` of rnn.py:158-166, so repeated points
+               inject once);
+    receivers: per shot, (zs, xs) index lists (probe.py:42-44).
+    Per step: equation step; ``field[b, z, x] += w[i]`` at the shot's source
+    points for every source_type (source.py:47-57, one shared wavelet
+    value); records read every receiver_type after injection; the
+    illumination adds sum_b src_field^2 (rnn.py:204-205).
+    Returns dict(records=[(nt, nrec_b, nch)], fields=..., illum=...).
+    """
+    wavelet = np.asarray(wavelet, np.float64)
+    nt = len(wavelet) if nt is None else nt
+    names = WAVEFIELDS[equation]
+    source_type = source_type or (["h1"] if equation != "elastic" else ["txx", "tzz"])
+    receiver_type = receiver_type or (["h1"] if equation != "elastic" else ["vx", "vz"])
+    B = len(sources)
+    m0 = np.asarray(models[MODEL_PARAMS[equation][0]])
+    nz, nx = m0.shape
+    fields = {n: np.zeros((B, nz, nx), dtype) for n in names}
+    smask = np.zeros((B, nz, nx), dtype)
+    for b, pts in enumerate(sources):
+        for (z, x) in pts:
+            smask[b, z, x] = 1
+    recs = [[] for _ in range(B)]
+    illum = np.zeros((nz, nx), dtype) if illumination else None
+    for i in range(nt):
+        if equation == "acoustic":
+            y, h1 = acoustic_step(models["vp"], fields["h1"], fields["h2"], dt, h, d, order, dtype)
+            fields["h1"], fields["h2"] = y, h1
+        elif equation == "acoustic_habc":
+            y, h1 = acoustic_habc_step(models["vp"], fields["h1"], fields["h2"], dt, h, d, order,
+                                       multiple, dtype)
+            fields["h1"], fields["h2"] = y, h1
+        elif equation == "elastic":
+            out = elastic_step(models["vp"], models["vs"], models["rho"],
+                               *[fields[n] for n in names], dt, h, d, dtype)
+            fields = dict(zip(names, out))
+        else:
+            raise ValueError(equation)
+        wv = dtype(wavelet[i])
+        for st in source_type:
+            fields[st] = fields[st] + smask * wv
+        for b, (zs, xs) in enumerate(receivers):
+            zs = np.asarray(zs, int)
+            xs = np.asarray(xs, int)
+            recs[b].append(np.stack([fields[k][b, zs, xs] for k in receiver_type], axis=-1))
+        if illumination:
+            illum = illum + np.sum(fields[source_type[-1]] ** 2, axis=0)
+    out = {"records": [np.asarray(r) for r in recs], "illum": illum}
+    if return_fields:
+        out["fields"] = fields
+    return out
