@@ -1,0 +1,160 @@
+/*
+ * seistorch_gb300 -- C ABI of the GB300 (sm_103a) wave-propagation hot path.
+ *
+ * Drop-in native layer for seistorch's 2D time stepping (the equation modules
+ * seistorch/equations2d/{acoustic,acoustic_habc,elastic}.py and the loop in
+ * seistorch/rnn.py + seistorch/cell.py).  Plain pointers, sizes and a
+ * cudaStream_t only; no torch types.  All pointers are device pointers unless
+ * a field says otherwise.  Every entry point returns an sgb_status.
+ *
+ * Layout: wavefields are float32 [nshots][nz][pitch] (x fastest), models and
+ * coefficient planes float32 [nz][pitch]; pitch is a multiple of 4 floats
+ * and >= nx; columns nx..pitch-1 are never read as data (zero padding is
+ * implied, as conv2d(padding=order/2) in acoustic.py:71).
+ */
+#ifndef SEISTORCH_GB300_H
+#define SEISTORCH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *sgb_stream_t; /* == cudaStream_t */
+
+typedef enum {
+  SGB_OK = 0,
+  SGB_ERR_ARG = 1,         /* null pointer / bad enum / bad size              */
+  SGB_ERR_SHAPE = 2,       /* inconsistent nz/nx/pitch/nshots                 */
+  SGB_ERR_ALIGN = 3,       /* pointer not 16-byte aligned / pitch % 4 != 0    */
+  SGB_ERR_CUDA = 4,        /* a CUDA runtime call failed (see sgb_last_cuda_error) */
+  SGB_ERR_UNSUPPORTED = 5, /* order / option outside what the kernels cover   */
+  SGB_ERR_NONFINITE = 6,   /* NaN/Inf found in records (rnn.py:215 -> type.py:41-46) */
+  SGB_ERR_CAPACITY = 7     /* too many sources inside one tile                */
+} sgb_status;
+
+/* Grid shared by every equation. dt, h in seconds / metres. */
+typedef struct {
+  int32_t nz, nx;    /* padded grid (interior + boundary layers)          */
+  int32_t pitch;     /* row stride in floats                              */
+  int32_t nshots;    /* batch of shots (wavefield leading dimension)      */
+  float dt, h;
+} sgb_grid;
+
+/* Acquisition for one time loop (rnn.py:158-212, source.py:47-57,
+ * probe.py:42-44).  Sources: CSR by shot; each point receives
+ * wavelet[wrow * nt + t] at step t (the smask*X add; the caller removes
+ * duplicate points within a shot, as the 0/1 mask does).  Receivers: CSR by
+ * (shot, row) -- rec_row_ptr[b * nz + z] .. rec_row_ptr[b * nz + z + 1] --
+ * each with its column x and its output column in records[t][col][ch]. */
+typedef struct {
+  const int32_t *src_ptr;     /* [nshots + 1]                         */
+  const int32_t *src_z;       /* [nsrc]                               */
+  const int32_t *src_x;       /* [nsrc]                               */
+  const int32_t *src_wrow;    /* [nsrc] row of `wavelet` per source   */
+  const float *wavelet;       /* [nwrows][nt]                         */
+  int32_t nsrc;
+  int32_t nt;
+  const int32_t *rec_row_ptr; /* [nshots * nz + 1]                    */
+  const int32_t *rec_x;       /* [nrec]                               */
+  const int32_t *rec_col;     /* [nrec] column in the record matrix   */
+  int32_t nrec;               /* record matrix width                  */
+  int32_t nch;                /* channels per record (receiver types) */
+  float *records;             /* [nt][nrec][nch] out (may be NULL)    */
+} sgb_acquisition;
+
+/* 2nd-order-in-time acoustic model (acoustic.py:73-86, acoustic_habc.py:206-221).
+ * coef = [g plane | k plane] from sgb_acoustic_coefficients:
+ *   u+ = g (u - u-) + u- + k * L(u),  g = 2/(1 + d dt),
+ *   k = vp^2 dt^2 / (h^2 (1 + d dt)),  L = cross stencil of `order`
+ * (PML: d = damping; HABC: d = 0 in the update, `damp` is the blend
+ * weight of habc.py:42-81). */
+typedef struct {
+  int32_t order;        /* 2, 4, 6 or 8                                       */
+  int32_t boundary;     /* 0 = PML, 1 = HABC                                   */
+  int32_t habc_width;   /* 50 (acoustic_habc.py:79, habc.py)                  */
+  int32_t multiple;     /* free surface at the top (no top absorbing layer)    */
+  const float *coef;    /* [2][nz][pitch]                                      */
+  const float *vp;      /* [nz][pitch] (HABC one-way coefficients)            */
+  const float *damp;    /* [nz][pitch] PML d or HABC blend weight             */
+} sgb_acoustic_model;
+
+/* Boundary-saving store for the adjoint (checkpoint_new.py:109-217 saves
+ * 1-cell strips; here `ring` cells on every side of the undamped interior
+ * box [iz0,iz1) x [ix0,ix1), clipped to the grid) plus full checkpoints of
+ * (U_n, U_{n-1}) every ckpt_every steps. */
+typedef struct {
+  int32_t iz0, iz1, ix0, ix1;
+  int32_t ring;
+  int32_t ring_size;        /* floats per shot per step (sgb_ring_size)     */
+  float *ring_store;        /* [nt][nshots][ring_size]                      */
+  int32_t ckpt_every;       /* 0: none                                      */
+  float *ckpt_store;        /* [nt / ckpt_every][2][nshots][nz][pitch]      */
+} sgb_bs_store;
+
+/* Library identification and diagnostics. */
+const char *sgb_version(void);
+const char *sgb_status_string(int status);
+int sgb_last_cuda_error(void);
+
+/* Reads (and with reset != 0 clears) the device status word that kernels set
+ * on capacity faults (bit 1: too many sources in one tile).  Synchronous. */
+int sgb_device_status(int *out, int reset);
+
+/* Floats per shot per step of the boundary ring (host-only helper). */
+int sgb_ring_size(const sgb_grid *grid, int32_t iz0, int32_t iz1, int32_t ix0, int32_t ix1,
+                  int32_t ring, int32_t *size_out);
+
+/* Coefficient planes for sgb_acoustic_model.coef.  Replaces the per-step
+ * (dt^-2 + b/dt)^-1 and c.pow(2) work of acoustic.py:81-84. */
+int sgb_acoustic_coefficients(const sgb_grid *grid, const float *vp, const float *damp,
+                              int32_t boundary, float *coef_out, sgb_stream_t stream);
+
+/* One time step: unext = step(u, um).  Replaces acoustic._time_step
+ * (acoustic.py:73-86) and acoustic_habc._time_step (acoustic_habc.py:206-221);
+ * unext must not alias u or um. */
+int sgb_acoustic_step(const sgb_grid *grid, const sgb_acoustic_model *model, const float *u,
+                      const float *um, float *unext, sgb_stream_t stream);
+
+/* Vector-Jacobian product of one PML step (autograd of acoustic.py:73-86):
+ * given gy = dJ/dy and gh1 = dJ/d(second output h1), writes
+ * gu = dJ/du (h1), gum = dJ/dum (h2) and accumulates gvp_acc += sum over
+ * shots of gy * L(u) (caller multiplies by 2k/vp).  gh1 may be NULL. */
+int sgb_acoustic_step_vjp(const sgb_grid *grid, const sgb_acoustic_model *model, const float *u,
+                          const float *gy, const float *gh1, float *gu, float *gum,
+                          float *gvp_acc, sgb_stream_t stream);
+
+/* Whole time loop (rnn.py:178-205) in one call: nt steps of the model with
+ * source injection and receiver sampling fused into the step kernel.
+ * buf[0..2] are three [nshots][nz][pitch] buffers; on entry buf[0] = U_0 and
+ * buf[1] = U_{-1} (zeros for a cold start).  On return *cur_out / *prev_out
+ * index the buffers holding U_nt and U_{nt-1}.  illum (nullable, [nz][pitch])
+ * accumulates sum_b u^2 of the source field (rnn.py:204-205).  bs (nullable)
+ * saves the boundary ring every step and checkpoints every ckpt_every. */
+int sgb_acoustic_forward(const sgb_grid *grid, const sgb_acoustic_model *model,
+                         const sgb_acquisition *acq, float *const buf[3], float *illum,
+                         const sgb_bs_store *bs, int32_t *cur_out, int32_t *prev_out,
+                         sgb_stream_t stream);
+
+/* Adjoint of sgb_acoustic_forward (PML): boundary-saving reconstruction of
+ * the forward wavefield in the interior box + adjoint time stepping + vp
+ * gradient, in one fused kernel per step.  Replaces the autograd path of
+ * checkpoint_new.py:146-217 with an exact discrete adjoint.
+ *   ubuf[0..2]: [nshots][nz][pitch]; on entry ubuf[ucur] = U_nt and
+ *               ubuf[uprev] = U_{nt-1} (as left by sgb_acoustic_forward);
+ *   lbuf[0..2]: [nshots][nz][pitch] adjoint scratch (zeroed here);
+ *   acq->records: dJ/d(records) [nt][nrec][nch] (the adjoint source);
+ *   grad_shot: [nshots][nz][pitch] per-shot accumulation, zeroed here;
+ *   grad_vp: [nz][pitch] out, dJ/dvp inside the interior box, 0 outside. */
+int sgb_acoustic_backward(const sgb_grid *grid, const sgb_acoustic_model *model,
+                          const sgb_acquisition *acq, const sgb_bs_store *bs,
+                          float *const ubuf[3], int32_t ucur, int32_t uprev,
+                          float *const lbuf[3], float *grad_shot, float *grad_vp,
+                          sgb_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEISTORCH_GB300_H */

@@ -1,0 +1,365 @@
+// extern "C" entry points of libseistorch_gb300 (see include/seistorch_gb300.h).
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "sgb_common.cuh"
+#include "acoustic_args.cuh"
+
+namespace sgb {
+
+static thread_local int g_last_cuda_error = 0;
+
+int set_cuda_error(cudaError_t e) {
+  g_last_cuda_error = (int)e;
+  return SGB_ERR_CUDA;
+}
+
+// Device status word (bit flags set by kernels, e.g. DEV_ERR_CAPACITY).
+__device__ int g_dev_status;
+
+static int* status_ptr() {
+  static int* p = nullptr;
+  static int dev = -1;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (p == nullptr || dev != cur) {
+    if (cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_dev_status) != cudaSuccess) return nullptr;
+    dev = cur;
+  }
+  return p;
+}
+
+FdWeights fd_weights(int order) {
+  // Exact rationals of the order-2..8 central second-derivative weights
+  // (the solution of the Taylor system in acoustic.py:5-30).
+  FdWeights w;
+  for (int i = 0; i < 5; ++i) w.c[i] = 0.f;
+  double c[5] = {0, 0, 0, 0, 0};
+  switch (order) {
+    case 2: c[1] = 1.0; break;
+    case 4: c[1] = 4.0 / 3.0; c[2] = -1.0 / 12.0; break;
+    case 6: c[1] = 3.0 / 2.0; c[2] = -3.0 / 20.0; c[3] = 1.0 / 90.0; break;
+    case 8: c[1] = 8.0 / 5.0; c[2] = -1.0 / 5.0; c[3] = 8.0 / 315.0; c[4] = -1.0 / 560.0; break;
+  }
+  double s = 0;
+  for (int j = 1; j <= 4; ++j) s += c[j];
+  w.c[0] = (float)(-4.0 * s);
+  for (int j = 1; j <= 4; ++j) w.c[j] = (float)c[j];
+  return w;
+}
+
+// kernels in acoustic.cu
+cudaError_t launch_acoustic_fwd(int R, bool habc, int tz, const AcStepArgs& a, cudaStream_t s);
+cudaError_t launch_acoustic_bwd(int R, int tz, const AcBwdArgs& a, cudaStream_t s);
+cudaError_t launch_acoustic_vjp(int R, const AcVjpArgs& a, cudaStream_t s);
+cudaError_t launch_acoustic_coef(const sgb_grid& gr, const float* vp, const float* damp, int boundary,
+                                 float* g, float* k, cudaStream_t s);
+cudaError_t launch_acoustic_grad_reduce(const sgb_grid& gr, const float* grad_shot, const float* vp,
+                                        const Ring& ring, float* grad_vp, cudaStream_t s);
+int pick_tz(int nz, int nx, int nshots, int tz_max);
+
+}  // namespace sgb
+
+#include "acoustic_args.cuh"
+
+using namespace sgb;
+
+namespace {
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+int check_grid(const sgb_grid* g) {
+  if (g == nullptr) return SGB_ERR_ARG;
+  if (g->nz <= 0 || g->nx <= 0 || g->nshots <= 0 || g->pitch < g->nx) return SGB_ERR_SHAPE;
+  if (g->pitch % 4 != 0) return SGB_ERR_ALIGN;
+  if (!(g->dt > 0.f) || !(g->h > 0.f)) return SGB_ERR_ARG;
+  return SGB_OK;
+}
+
+int check_model(const sgb_grid* g, const sgb_acoustic_model* m) {
+  if (m == nullptr || m->coef == nullptr) return SGB_ERR_ARG;
+  if (m->order != 2 && m->order != 4 && m->order != 6 && m->order != 8) return SGB_ERR_UNSUPPORTED;
+  if (m->boundary != 0 && m->boundary != 1) return SGB_ERR_ARG;
+  if (!aligned16(m->coef)) return SGB_ERR_ALIGN;
+  if (m->boundary == 1) {
+    if (m->vp == nullptr || m->damp == nullptr) return SGB_ERR_ARG;
+    // the one-way extrapolation reads two cells inward of each 50-cell strip
+    if (m->habc_width <= 0 || m->habc_width + 2 > g->nx || m->habc_width + 2 > g->nz) return SGB_ERR_SHAPE;
+  }
+  return SGB_OK;
+}
+
+AcStepArgs base_step_args(const sgb_grid* g, const sgb_acoustic_model* m) {
+  AcStepArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nz = g->nz;
+  a.nx = g->nx;
+  a.pitch = g->pitch;
+  a.nshots = g->nshots;
+  a.ntx = (g->nx + TX - 1) / TX;
+  a.sstride = (long long)g->nz * g->pitch;
+  a.g = m->coef;
+  a.k = m->coef + (long long)g->nz * g->pitch;
+  a.w = fd_weights(m->order);
+  a.vp = m->vp;
+  a.hb = m->damp;
+  a.lamf = 2.f * g->dt / g->h;
+  a.muf = (g->dt * g->dt) / (g->h * g->h);
+  a.hw = m->habc_width;
+  a.multiple = m->multiple;
+  a.ring.size = 0;
+  a.ring.iz0 = a.ring.iz1 = a.ring.ix0 = a.ring.ix1 = 0;
+  a.ring.rt = a.ring.rb = a.ring.rl = a.ring.rr = 0;
+  a.status = status_ptr();
+  return a;
+}
+
+int check_acq(const sgb_grid* g, const sgb_acquisition* q) {
+  if (q == nullptr) return SGB_ERR_ARG;
+  if (q->nt <= 0) return SGB_ERR_ARG;
+  if (q->nsrc > 0 && (q->src_ptr == nullptr || q->src_z == nullptr || q->src_x == nullptr ||
+                      q->src_wrow == nullptr || q->wavelet == nullptr))
+    return SGB_ERR_ARG;
+  if (q->records != nullptr && (q->rec_row_ptr == nullptr || q->rec_x == nullptr || q->rec_col == nullptr))
+    return SGB_ERR_ARG;
+  if (q->records != nullptr && q->nch <= 0) return SGB_ERR_ARG;
+  (void)g;
+  return SGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sgb_version(void) { return "seistorch_gb300 0.1.0 (sm_103a)"; }
+
+const char* sgb_status_string(int s) {
+  switch (s) {
+    case SGB_OK: return "ok";
+    case SGB_ERR_ARG: return "invalid argument";
+    case SGB_ERR_SHAPE: return "inconsistent shape";
+    case SGB_ERR_ALIGN: return "misaligned pointer or pitch";
+    case SGB_ERR_CUDA: return "CUDA runtime error";
+    case SGB_ERR_UNSUPPORTED: return "unsupported option";
+    case SGB_ERR_NONFINITE: return "non-finite values in the records";
+    case SGB_ERR_CAPACITY: return "too many sources inside one tile";
+  }
+  return "unknown status";
+}
+
+int sgb_last_cuda_error(void) { return g_last_cuda_error; }
+
+int sgb_device_status(int* out, int reset) {
+  int* p = status_ptr();
+  if (p == nullptr || out == nullptr) return SGB_ERR_ARG;
+  SGB_CUDA_CHECK(cudaMemcpy(out, p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (reset) SGB_CUDA_CHECK(cudaMemset(p, 0, sizeof(int)));
+  return SGB_OK;
+}
+
+int sgb_ring_size(const sgb_grid* grid, int32_t iz0, int32_t iz1, int32_t ix0, int32_t ix1, int32_t ring,
+                  int32_t* size_out) {
+  if (int e = check_grid(grid)) return e;
+  if (size_out == nullptr || ring < 1) return SGB_ERR_ARG;
+  if (iz0 < 0 || ix0 < 0 || iz1 > grid->nz || ix1 > grid->nx || iz0 >= iz1 || ix0 >= ix1) return SGB_ERR_SHAPE;
+  *size_out = make_ring(*grid, iz0, iz1, ix0, ix1, ring).size;
+  return SGB_OK;
+}
+
+int sgb_acoustic_coefficients(const sgb_grid* grid, const float* vp, const float* damp, int32_t boundary,
+                              float* coef_out, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (vp == nullptr || coef_out == nullptr) return SGB_ERR_ARG;
+  if (boundary != 0 && boundary != 1) return SGB_ERR_ARG;
+  SGB_CUDA_CHECK(launch_acoustic_coef(*grid, vp, damp, boundary, coef_out,
+                                      coef_out + (long long)grid->nz * grid->pitch, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_acoustic_step(const sgb_grid* grid, const sgb_acoustic_model* model, const float* u, const float* um,
+                      float* unext, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (int e = check_model(grid, model)) return e;
+  if (u == nullptr || um == nullptr || unext == nullptr) return SGB_ERR_ARG;
+  if (!aligned16(u) || !aligned16(um) || !aligned16(unext)) return SGB_ERR_ALIGN;
+  if (unext == u || unext == um) return SGB_ERR_ARG;
+  AcStepArgs a = base_step_args(grid, model);
+  a.u = u;
+  a.um = um;
+  a.un = unext;
+  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 32);
+  SGB_CUDA_CHECK(launch_acoustic_fwd(model->order / 2, model->boundary == 1, tz, a, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_acoustic_step_vjp(const sgb_grid* grid, const sgb_acoustic_model* model, const float* u,
+                          const float* gy, const float* gh1, float* gu, float* gum, float* gvp_acc,
+                          sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (int e = check_model(grid, model)) return e;
+  if (model->boundary != 0) return SGB_ERR_UNSUPPORTED;
+  if (model->vp == nullptr) return SGB_ERR_ARG;
+  if (u == nullptr || gy == nullptr || gu == nullptr || gum == nullptr || gvp_acc == nullptr) return SGB_ERR_ARG;
+  if (!aligned16(u) || !aligned16(gy) || !aligned16(gu) || !aligned16(gum) || (gh1 && !aligned16(gh1)))
+    return SGB_ERR_ALIGN;
+  AcVjpArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nz = grid->nz; a.nx = grid->nx; a.pitch = grid->pitch; a.nshots = grid->nshots;
+  a.ntx = (grid->nx + TX - 1) / TX;
+  a.sstride = (long long)grid->nz * grid->pitch;
+  a.u = u; a.gy = gy; a.gh1 = gh1; a.gu = gu; a.gum = gum; a.gvp = gvp_acc;
+  a.g = model->coef;
+  a.k = model->coef + (long long)grid->nz * grid->pitch;
+  a.vp = model->vp;
+  a.w = fd_weights(model->order);
+  SGB_CUDA_CHECK(launch_acoustic_vjp(model->order / 2, a, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
+                         float* const buf[3], float* illum, const sgb_bs_store* bs, int32_t* cur_out,
+                         int32_t* prev_out, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (int e = check_model(grid, model)) return e;
+  if (int e = check_acq(grid, acq)) return e;
+  if (buf == nullptr || cur_out == nullptr || prev_out == nullptr) return SGB_ERR_ARG;
+  for (int i = 0; i < 3; ++i) {
+    if (buf[i] == nullptr) return SGB_ERR_ARG;
+    if (!aligned16(buf[i])) return SGB_ERR_ALIGN;
+  }
+  if (acq->records != nullptr && acq->nch != 1) return SGB_ERR_UNSUPPORTED;
+  cudaStream_t s = (cudaStream_t)stream;
+  AcStepArgs a = base_step_args(grid, model);
+  a.src_ptr = acq->nsrc > 0 ? acq->src_ptr : nullptr;
+  a.src_z = acq->src_z;
+  a.src_x = acq->src_x;
+  a.src_wrow = acq->src_wrow;
+  a.wavelet = acq->wavelet;
+  a.nt = acq->nt;
+  a.rec_row_ptr = acq->rec_row_ptr;
+  a.rec_x = acq->rec_x;
+  a.rec_col = acq->rec_col;
+  a.nrec = acq->nrec;
+  a.nch = acq->nch;
+  a.illum = illum;
+  const long long plane = (long long)grid->nz * grid->pitch;
+  const long long field = plane * grid->nshots;
+  if (bs != nullptr) {
+    if (bs->ring < 1 || bs->ring_store == nullptr) return SGB_ERR_ARG;
+    if (bs->iz0 < 0 || bs->ix0 < 0 || bs->iz1 > grid->nz || bs->ix1 > grid->nx || bs->iz0 >= bs->iz1 ||
+        bs->ix0 >= bs->ix1)
+      return SGB_ERR_SHAPE;
+    a.ring = make_ring(*grid, bs->iz0, bs->iz1, bs->ix0, bs->ix1, bs->ring);
+    if (a.ring.size != bs->ring_size) return SGB_ERR_SHAPE;
+    if (bs->ckpt_every > 0 && bs->ckpt_store == nullptr) return SGB_ERR_ARG;
+  }
+  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 32);
+  const int R = model->order / 2;
+  const bool habc = model->boundary == 1;
+  int cur = 0, prev = 1, nxt = 2;
+  for (int t = 0; t < acq->nt; ++t) {
+    a.u = buf[cur];
+    a.um = buf[prev];
+    a.un = buf[nxt];
+    a.t = t;
+    a.records = acq->records ? acq->records + (long long)t * acq->nrec * acq->nch : nullptr;
+    a.ring_out = bs ? bs->ring_store + (long long)t * grid->nshots * a.ring.size : nullptr;
+    SGB_CUDA_CHECK(launch_acoustic_fwd(R, habc, tz, a, s));
+    if (bs != nullptr && bs->ckpt_every > 0 && (t + 1) % bs->ckpt_every == 0) {
+      float* slot = bs->ckpt_store + (long long)((t + 1) / bs->ckpt_every - 1) * 2 * field;
+      SGB_CUDA_CHECK(cudaMemcpyAsync(slot, buf[nxt], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      SGB_CUDA_CHECK(cudaMemcpyAsync(slot + field, buf[cur], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+    prev = cur;
+    cur = nxt;
+    nxt = 3 - prev - cur;
+  }
+  *cur_out = cur;
+  *prev_out = prev;
+  return SGB_OK;
+}
+
+int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
+                          const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur, int32_t uprev,
+                          float* const lbuf[3], float* grad_shot, float* grad_vp, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (int e = check_model(grid, model)) return e;
+  if (int e = check_acq(grid, acq)) return e;
+  if (model->boundary != 0) return SGB_ERR_UNSUPPORTED;
+  if (model->vp == nullptr) return SGB_ERR_ARG;
+  if (bs == nullptr || bs->ring_store == nullptr || ubuf == nullptr || lbuf == nullptr || grad_shot == nullptr ||
+      grad_vp == nullptr)
+    return SGB_ERR_ARG;
+  if (ucur < 0 || ucur > 2 || uprev < 0 || uprev > 2 || ucur == uprev) return SGB_ERR_ARG;
+  for (int i = 0; i < 3; ++i) {
+    if (ubuf[i] == nullptr || lbuf[i] == nullptr) return SGB_ERR_ARG;
+    if (!aligned16(ubuf[i]) || !aligned16(lbuf[i])) return SGB_ERR_ALIGN;
+  }
+  if (!aligned16(grad_shot)) return SGB_ERR_ALIGN;
+  if (acq->records != nullptr && acq->nch != 1) return SGB_ERR_UNSUPPORTED;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long plane = (long long)grid->nz * grid->pitch;
+  const long long field = plane * grid->nshots;
+  AcBwdArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nz = grid->nz; a.nx = grid->nx; a.pitch = grid->pitch; a.nshots = grid->nshots;
+  a.ntx = (grid->nx + TX - 1) / TX;
+  a.sstride = plane;
+  a.g = model->coef;
+  a.k = model->coef + plane;
+  a.w = fd_weights(model->order);
+  a.grad_shot = grad_shot;
+  a.ring = make_ring(*grid, bs->iz0, bs->iz1, bs->ix0, bs->ix1, bs->ring);
+  if (a.ring.size != bs->ring_size) return SGB_ERR_SHAPE;
+  a.src_ptr = acq->nsrc > 0 ? acq->src_ptr : nullptr;
+  a.src_z = acq->src_z; a.src_x = acq->src_x; a.src_wrow = acq->src_wrow; a.wavelet = acq->wavelet;
+  a.nt = acq->nt;
+  a.rec_row_ptr = acq->rec_row_ptr; a.rec_x = acq->rec_x; a.rec_col = acq->rec_col;
+  a.nrec = acq->nrec; a.nch = acq->nch;
+  a.status = status_ptr();
+  for (int i = 0; i < 3; ++i) SGB_CUDA_CHECK(cudaMemsetAsync(lbuf[i], 0, field * sizeof(float), s));
+  SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot, 0, field * sizeof(float), s));
+  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 16);
+  const int R = model->order / 2;
+  const int nt = acq->nt;
+  const int K = bs->ckpt_every;
+  const int nslots = K > 0 ? nt / K : 0;
+  int uj = ucur, ujm1 = uprev, ufree = 3 - ucur - uprev;
+  int l1 = 0, l2 = 1, lfree = 2;
+  for (int j = nt; j >= 2; --j) {
+    const int n = j - 1;
+    const bool ck = K > 0 && n % K == 0 && n / K >= 1 && n / K <= nslots;
+    if (ck && n < nt) {
+      const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
+      SGB_CUDA_CHECK(cudaMemcpyAsync(ubuf[ujm1], slot, field * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+    a.ucur = ubuf[ujm1];
+    a.unext = ubuf[uj];
+    a.uout = ubuf[ufree];
+    a.l1 = lbuf[l1];
+    a.l2 = lbuf[l2];
+    a.lout = lbuf[lfree];
+    a.do_recon = j >= 3;
+    a.ring_in = j >= 3 ? bs->ring_store + (long long)(j - 3) * grid->nshots * a.ring.size : nullptr;
+    a.t_src = j - 1;
+    a.resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
+    SGB_CUDA_CHECK(launch_acoustic_bwd(R, tz, a, s));
+    if (ck && j >= 3) {
+      const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
+      SGB_CUDA_CHECK(cudaMemcpyAsync(ubuf[ufree], slot + field, field * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+    const int old_uj = uj;
+    uj = ujm1;
+    ujm1 = ufree;
+    ufree = old_uj;
+    const int old_l2 = l2;
+    l2 = l1;
+    l1 = lfree;
+    lfree = old_l2;
+  }
+  SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, model->vp, a.ring, grad_vp, s));
+  return SGB_OK;
+}
+
+}  // extern "C"

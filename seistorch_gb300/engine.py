@@ -1,0 +1,307 @@
+"""Host engine over the C ABI: pitched buffers, acquisition tables, time loops.
+
+The hot path (every time step, source injection, receiver sampling, the
+boundary ring, the adjoint) runs in the CUDA kernels of libseistorch_gb300;
+this module only lays out device memory (torch tensors) and calls the C ABI
+with raw pointers on the current torch stream.  There is no CPU path: calls
+raise when CUDA or the library is unavailable.
+"""
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+BOUNDARY_PML = 0
+BOUNDARY_HABC = 1
+
+
+def pitch_of(nx):
+    """Row stride (floats) of every device plane: nx rounded up to 4."""
+    return (int(nx) + 3) // 4 * 4
+
+
+def require_cuda(t, what):
+    if not torch.cuda.is_available():
+        raise RuntimeError(f"{what}: seistorch_gb300 needs a CUDA GPU (sm_103a); no CPU fallback")
+    if t is not None and not t.is_cuda:
+        raise RuntimeError(f"{what}: expected a CUDA tensor, got {t.device}")
+
+
+def to_pitched(a, pitch, dtype=torch.float32):
+    """(..., nz, nx) -> contiguous (..., nz, pitch) float32 with zero pad columns."""
+    a = a.to(dtype)
+    nx = a.shape[-1]
+    if nx == pitch and a.is_contiguous():
+        return a
+    out = torch.zeros(*a.shape[:-1], pitch, dtype=dtype, device=a.device)
+    out[..., :nx] = a
+    return out
+
+
+def grid_struct(nz, nx, pitch, nshots, dt, h):
+    return N.Grid(int(nz), int(nx), int(pitch), int(nshots), float(dt), float(h))
+
+
+class Acquisition:
+    """Device tables for one batch of shots (rnn.py:158-212 semantics).
+
+    sources:   per shot, a list of (z, x) padded-grid points; duplicates in a
+               shot inject once (the 0/1 ``smask`` of rnn.py:158-166);
+    src_wrow:  per shot, per point, the row of ``wavelet`` it injects
+               (0 for the shared wavelet of the batched path);
+    receivers: per shot, (zs, xs); records come back in the concatenated
+               order of the shots (the super-probe order of rnn.py:51-73).
+    """
+
+    def __init__(self, nz, nx, sources, receivers, wavelet, device, src_wrow=None):
+        nshots = len(sources)
+        if len(receivers) != nshots:
+            raise ValueError("sources and receivers must list the same number of shots")
+        wav = torch.as_tensor(wavelet, dtype=torch.float32, device=device)
+        if wav.ndim == 1:
+            wav = wav[None]
+        self.wavelet = wav.contiguous()
+        self.nt = int(wav.shape[-1])
+        sp, sz, sx, sw = [0], [], [], []
+        for b, pts in enumerate(sources):
+            seen = set()
+            rows = src_wrow[b] if src_wrow is not None else [0] * len(pts)
+            for (z, x), wr in zip(pts, rows):
+                z, x = int(z), int(x)
+                if not (0 <= z < nz and 0 <= x < nx):
+                    raise IndexError(f"source ({z}, {x}) of shot {b} is outside the {nz}x{nx} grid")
+                if (z, x) in seen:
+                    continue
+                seen.add((z, x))
+                sz.append(z)
+                sx.append(x)
+                sw.append(int(wr))
+            sp.append(len(sz))
+        self.nshots = nshots
+        self.nsrc = len(sz)
+        if self.nsrc and max(sw) >= wav.shape[0]:
+            raise IndexError("a source refers to a wavelet row that does not exist")
+        it = lambda v: torch.as_tensor(np.asarray(v, np.int32), device=device)
+        self.src_ptr, self.src_z, self.src_x, self.src_wrow = it(sp), it(sz), it(sx), it(sw)
+        bz, zz, xx = [], [], []
+        self.reccounts = []
+        for b, (zs, xs) in enumerate(receivers):
+            zs = np.asarray(zs, np.int64).reshape(-1)
+            xs = np.asarray(xs, np.int64).reshape(-1)
+            if zs.shape != xs.shape:
+                raise ValueError(f"receiver z/x lists of shot {b} differ in length")
+            if len(zs) and (zs.min() < 0 or zs.max() >= nz or xs.min() < 0 or xs.max() >= nx):
+                raise IndexError(f"a receiver of shot {b} is outside the {nz}x{nx} grid")
+            bz.append(np.full(len(zs), b, np.int64))
+            zz.append(zs)
+            xx.append(xs)
+            self.reccounts.append(int(len(zs)))
+        bz = np.concatenate(bz) if bz else np.zeros(0, np.int64)
+        zz = np.concatenate(zz) if zz else np.zeros(0, np.int64)
+        xx = np.concatenate(xx) if xx else np.zeros(0, np.int64)
+        self.nrec = int(len(zz))
+        key = (bz * nz + zz) * nx + xx
+        order = np.argsort(key, kind="stable")
+        row = (bz * nz + zz)[order]
+        ptr = np.zeros(nshots * nz + 1, np.int64)
+        np.add.at(ptr, row + 1, 1)
+        ptr = np.cumsum(ptr)
+        self.rec_row_ptr = it(ptr)
+        self.rec_x = it(xx[order])
+        self.rec_col = it(order)
+        self.rec_b = torch.as_tensor(bz, device=device)
+        self.rec_z = torch.as_tensor(zz, device=device)
+        self.rec_xs = torch.as_tensor(xx, device=device)
+
+    def struct(self, records=None, nch=1):
+        return N.Acquisition(
+            N.ptr(self.src_ptr), N.ptr(self.src_z), N.ptr(self.src_x), N.ptr(self.src_wrow),
+            N.ptr(self.wavelet), self.nsrc, self.nt,
+            N.ptr(self.rec_row_ptr), N.ptr(self.rec_x), N.ptr(self.rec_col), self.nrec, int(nch),
+            N.ptr(records))
+
+
+def interior_box(nz, nx, bwidth, multiple):
+    """Undamped interior [iz0, iz1) x [ix0, ix1) of a padded grid."""
+    top = 0 if multiple else bwidth
+    return top, nz - bwidth, bwidth, nx - bwidth
+
+
+class AcousticState:
+    """Buffers one forward keeps for its adjoint."""
+
+    def __init__(self):
+        self.buf = None
+        self.cur = 0
+        self.prev = 1
+        self.ring_store = None
+        self.ckpt_store = None
+        self.bs = None
+
+
+class AcousticPropagator:
+    """2nd-order acoustic time loop (acoustic.py / acoustic_habc.py + rnn.py)."""
+
+    def __init__(self, nz, nx, dt, h, order=2, boundary="pml", bwidth=50, multiple=False,
+                 device=None):
+        if order not in (2, 4, 6, 8):
+            raise ValueError(f"spatial order {order} is not supported (2, 4, 6 or 8)")
+        self.nz, self.nx = int(nz), int(nx)
+        self.pitch = pitch_of(nx)
+        self.dt, self.h = float(dt), float(h)
+        self.order = int(order)
+        self.boundary = BOUNDARY_HABC if boundary == "habc" else BOUNDARY_PML
+        self.bwidth = int(bwidth)
+        self.multiple = bool(multiple)
+        self.device = torch.device(device) if device is not None else torch.device("cuda")
+
+    # -- coefficients
+    def model(self, vp, damp):
+        """Pitched vp / damping planes and the (g, k) coefficient planes."""
+        require_cuda(vp, "AcousticPropagator.model")
+        vpp = to_pitched(vp.detach(), self.pitch).contiguous()
+        dp = to_pitched(damp.detach().to(vp.device), self.pitch).contiguous()
+        coef = torch.empty(2, self.nz, self.pitch, dtype=torch.float32, device=vp.device)
+        g = grid_struct(self.nz, self.nx, self.pitch, 1, self.dt, self.h)
+        N.call("sgb_acoustic_coefficients", ctypes.byref(g), N.ptr(vpp), N.ptr(dp), self.boundary,
+               N.ptr(coef), N.stream_handle())
+        m = N.AcousticModel(self.order, self.boundary, 50, int(self.multiple), N.ptr(coef),
+                            N.ptr(vpp), N.ptr(dp))
+        return m, (vpp, dp, coef)
+
+    def grid(self, nshots):
+        return grid_struct(self.nz, self.nx, self.pitch, nshots, self.dt, self.h)
+
+    # -- one step (equation-module drop-in)
+    def step(self, vp, damp, u, um):
+        m, keep = self.model(vp, damp)
+        B = u.shape[0]
+        up = to_pitched(u, self.pitch).contiguous()
+        ump = to_pitched(um, self.pitch).contiguous()
+        out = torch.empty_like(up)
+        g = self.grid(B)
+        N.call("sgb_acoustic_step", ctypes.byref(g), ctypes.byref(m), N.ptr(up), N.ptr(ump), N.ptr(out),
+               N.stream_handle())
+        return out[..., :self.nx]
+
+    def step_vjp(self, vp, damp, u, gy, gh1):
+        m, keep = self.model(vp, damp)
+        B = u.shape[0]
+        up = to_pitched(u, self.pitch).contiguous()
+        gyp = to_pitched(gy, self.pitch).contiguous()
+        gh1p = to_pitched(gh1, self.pitch).contiguous() if gh1 is not None else None
+        gu = torch.empty_like(up)
+        gum = torch.empty_like(up)
+        gvp = torch.zeros(self.nz, self.pitch, dtype=torch.float32, device=up.device)
+        g = self.grid(B)
+        N.call("sgb_acoustic_step_vjp", ctypes.byref(g), ctypes.byref(m), N.ptr(up), N.ptr(gyp),
+               N.ptr(gh1p), N.ptr(gu), N.ptr(gum), N.ptr(gvp), N.stream_handle())
+        return gu[..., :self.nx], gum[..., :self.nx], gvp[:, :self.nx]
+
+    # -- whole loop
+    def forward(self, vp, damp, acq, *, save_for_adjoint=False, illumination=False, ckpt_every=0,
+                init=None):
+        require_cuda(vp, "AcousticPropagator.forward")
+        m, keep = self.model(vp, damp)
+        B = acq.nshots
+        dev = vp.device
+        field = (B, self.nz, self.pitch)
+        buf = [torch.zeros(field, dtype=torch.float32, device=dev) for _ in range(3)]
+        if init is not None:
+            buf[0][..., :self.nx] = init[0]
+            buf[1][..., :self.nx] = init[1]
+        records = torch.empty(acq.nt, max(acq.nrec, 1), 1, dtype=torch.float32, device=dev)
+        illum = torch.zeros(self.nz, self.pitch, dtype=torch.float32, device=dev) if illumination else None
+        state = AcousticState()
+        bs_struct = None
+        if save_for_adjoint:
+            if self.boundary != BOUNDARY_PML:
+                raise NotImplementedError("the boundary-saving adjoint covers the PML acoustic equation")
+            iz0, iz1, ix0, ix1 = interior_box(self.nz, self.nx, self.bwidth, self.multiple)
+            if iz1 <= iz0 or ix1 <= ix0:
+                raise ValueError("grid too small for its boundary width")
+            dpl = keep[1][:, :self.nx]
+            if torch.count_nonzero(dpl[iz0:iz1, ix0:ix1]).item() != 0:
+                raise ValueError("the damping profile is not zero inside the interior box; "
+                                 "boundary-saving reconstruction needs an undamped interior")
+            r = self.order // 2
+            size = ctypes.c_int32(0)
+            g1 = self.grid(B)
+            N.call("sgb_ring_size", ctypes.byref(g1), iz0, iz1, ix0, ix1, r, ctypes.byref(size))
+            state.ring_store = torch.empty(acq.nt, B, max(size.value, 1), dtype=torch.float32, device=dev)
+            K = int(ckpt_every) if ckpt_every else 0
+            nslots = acq.nt // K if K > 0 else 0
+            state.ckpt_store = (torch.empty(max(nslots, 1), 2, *field, dtype=torch.float32, device=dev)
+                                if K > 0 else None)
+            bs_struct = N.BsStore(iz0, iz1, ix0, ix1, r, size.value, N.ptr(state.ring_store), K,
+                                  N.ptr(state.ckpt_store))
+            state.bs = bs_struct
+        cur = ctypes.c_int32(0)
+        prev = ctypes.c_int32(0)
+        g = self.grid(B)
+        q = acq.struct(records if acq.nrec else None, 1)
+        bufs = N.PTR3(*[b.data_ptr() for b in buf])
+        N.call("sgb_acoustic_forward", ctypes.byref(g), ctypes.byref(m), ctypes.byref(q), bufs,
+               N.ptr(illum), ctypes.byref(bs_struct) if bs_struct is not None else None,
+               ctypes.byref(cur), ctypes.byref(prev), N.stream_handle())
+        state.buf, state.cur, state.prev = buf, cur.value, prev.value
+        state.keep = keep
+        state.model = m
+        return records[:, :acq.nrec], state, (illum[:, :self.nx] if illum is not None else None)
+
+    def backward(self, state, acq, grad_records):
+        """dJ/dvp (nz, nx) from dJ/d(records) through the fused adjoint."""
+        B = acq.nshots
+        dev = state.buf[0].device
+        resid = torch.zeros(acq.nt, max(acq.nrec, 1), 1, dtype=torch.float32, device=dev)
+        if acq.nrec:
+            resid[:, :acq.nrec] = grad_records.to(torch.float32).reshape(acq.nt, acq.nrec, 1)
+        field = (B, self.nz, self.pitch)
+        lbuf = [torch.empty(field, dtype=torch.float32, device=dev) for _ in range(3)]
+        grad_shot = torch.empty(field, dtype=torch.float32, device=dev)
+        grad = torch.empty(self.nz, self.pitch, dtype=torch.float32, device=dev)
+        g = self.grid(B)
+        q = acq.struct(resid, 1)
+        ub = N.PTR3(*[b.data_ptr() for b in state.buf])
+        lb = N.PTR3(*[b.data_ptr() for b in lbuf])
+        N.call("sgb_acoustic_backward", ctypes.byref(g), ctypes.byref(state.model), ctypes.byref(q),
+               ctypes.byref(state.bs), ub, state.cur, state.prev, lb, N.ptr(grad_shot), N.ptr(grad),
+               N.stream_handle())
+        return grad[:, :self.nx]
+
+
+class _AcousticLoop(torch.autograd.Function):
+    """Whole acoustic time loop as one differentiable op: vp -> records."""
+
+    @staticmethod
+    def forward(ctx, vp, prop, damp, acq, illumination, ckpt_every):
+        need = ctx.needs_input_grad[0]
+        rec, state, illum = prop.forward(vp, damp, acq, save_for_adjoint=need, illumination=illumination,
+                                         ckpt_every=ckpt_every)
+        ctx.prop, ctx.acq, ctx.state = prop, acq, state
+        ctx.mark_non_differentiable(illum) if illum is not None else None
+        fields = (state.buf[state.cur][..., :prop.nx], state.buf[state.prev][..., :prop.nx])
+        ctx.fields = fields
+        return rec, illum if illum is not None else rec.new_zeros(0)
+
+    @staticmethod
+    def backward(ctx, grad_rec, grad_illum):
+        if ctx.state.bs is None:
+            return None, None, None, None, None, None
+        grad_vp = ctx.prop.backward(ctx.state, ctx.acq, grad_rec.contiguous())
+        ctx.state = None
+        return grad_vp, None, None, None, None, None
+
+
+def acoustic_loop(vp, prop, damp, acq, illumination=False, ckpt_every=0):
+    """records (nt, nrec, 1) [, illum] of the acoustic loop; differentiable in vp."""
+    rec, illum = _AcousticLoop.apply(vp, prop, damp, acq, illumination, ckpt_every)
+    return rec, (illum if illumination else None)
+
+
+def default_ckpt_every(nt):
+    """Checkpoint spacing of the reconstruction: about sqrt(nt), at most 256."""
+    return int(min(256, max(16, round(math.sqrt(max(nt, 1))))))

@@ -1,0 +1,39 @@
+"""Equation registry: model parameters and wavefields per equation
+(seistorch/eqconfigure.py:6-127).  The positional order of these lists is the
+argument order of every ``_time_step`` (model params, then wavefields)."""
+
+
+class Parameters:
+    @staticmethod
+    def valid_model_paras():
+        return {"acoustic": ["vp"],
+                "acoustic_habc": ["vp"],
+                "elastic": ["vp", "vs", "rho"]}
+
+    @staticmethod
+    def secondorder_equations():
+        return ["acoustic", "acoustic_habc"]
+
+
+class Wavefield:
+    _FIELDS = {"acoustic": ["h1", "h2"],
+               "acoustic_habc": ["h1", "h2"],
+               "elastic": ["vx", "vz", "txx", "tzz", "txz"]}
+
+    def __init__(self, equation="acoustic"):
+        if equation not in self._FIELDS:
+            raise AttributeError(f"equation '{equation}' is not implemented by seistorch_gb300 "
+                                 f"(available: {sorted(self._FIELDS)})")
+        self.wavefields = list(self._FIELDS[equation])
+
+    @property
+    def acoustic(self):
+        return list(self._FIELDS["acoustic"])
+
+    @property
+    def acoustic_habc(self):
+        return list(self._FIELDS["acoustic_habc"])
+
+    @property
+    def elastic(self):
+        return list(self._FIELDS["elastic"])

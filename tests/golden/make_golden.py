@@ -88,11 +88,18 @@ def run_case(ref, equation, models_int, *, order=2, width=20, multiple=False, ns
         for n in names_wf:
             out["field_" + n] = getattr(rnn, n).numpy()[0]  # shot 0 keeps fixtures small
     else:
-        obs_padded = {n: np.pad(obs_models[n], ((top, width), (width, width)), mode="edge")
-                      for n in names}
-        with torch.no_grad():
-            _, _, yobs = forward(obs_padded)
-        obs = [t.clone() for t in yobs.data]
+        if obs_models is None:
+            # zero observed data: J = sum(syn^2), a residual free of cancellation
+            obs_padded = padded
+            with torch.no_grad():
+                _, _, yobs = forward(obs_padded)
+            obs = [torch.zeros_like(t) for t in yobs.data]
+        else:
+            obs_padded = {n: np.pad(obs_models[n], ((top, width), (width, width)), mode="edge")
+                          for n in names}
+            with torch.no_grad():
+                _, _, yobs = forward(obs_padded)
+            obs = [t.clone() for t in yobs.data]
         geom, rnn, y = forward(padded, requires_grad=tuple(grad))
         loss = sum(torch.nn.functional.mse_loss(s, o, reduction="sum") for s, o in zip(y.data, obs))
         loss.backward()
@@ -139,14 +146,22 @@ def cases():
                                      grad=["vp"], obs_models=a_obs)
     C["grad_acoustic_pml_o8"] = dict(equation="acoustic", models_int=a, order=8, nt=150,
                                      grad=["vp"], obs_models=a_obs)
+    C["grad_acoustic_pml_o4_zeroobs"] = dict(equation="acoustic", models_int=a, order=4, nt=150,
+                                             grad=["vp"], obs_models=None)
+    C["grad_acoustic_pml_o8_zeroobs"] = dict(equation="acoustic", models_int=a, order=8, nt=150,
+                                             grad=["vp"], obs_models=None)
+    C["grad_elastic_zeroobs"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,
+                                     nt=200, grad=["vp", "vs", "rho"], obs_models=None)
     C["grad_elastic"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,
                              nt=200, grad=["vp", "vs", "rho"], obs_models=e_obs)
     return C
 
 
-def main():
+def main(only=None):
     ref = RL.load("cpu")
     for name, kw in cases().items():
+        if only and name not in only:
+            continue
         res64 = run_case(ref, dtype=torch.float64, **kw)
         if kw.get("grad") is None:
             res32 = run_case(ref, dtype=torch.float32, **kw)
@@ -160,4 +175,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

@@ -1,0 +1,181 @@
+"""CPU tests: the C-ABI library loads and exports what the header declares,
+host-side logic (acquisition tables, config reader, coefficient generators)
+matches the reference's semantics.  No kernel is launched here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+from tests.golden_cases import load, rel_l2
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for fn in os.listdir(inc):
+        if fn.endswith(".h"):
+            text = open(os.path.join(inc, fn)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names.update(re.findall(r"\b(sgb_\w+)\s*\(", text))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from seistorch_gb300 import _native
+    _native.build()
+    return _native.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    syms = _declared_symbols()
+    assert len(syms) >= 8
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_host_only_entry_points(lib):
+    from seistorch_gb300 import _native as N
+    assert b"sm_103a" in lib.sgb_version()
+    assert lib.sgb_status_string(0) == b"ok"
+    assert lib.sgb_status_string(7).startswith(b"too many")
+    g = N.Grid(120, 140, 140, 2, 0.001, 10.0)
+    out = ctypes.c_int32(0)
+    assert lib.sgb_ring_size(ctypes.byref(g), 50, 70, 50, 90, 4, ctypes.byref(out)) == 0
+    # (20+8) x (40+8) box minus the 20 x 40 interior
+    assert out.value == 28 * 48 - 20 * 40
+    assert lib.sgb_ring_size(ctypes.byref(g), 0, 70, 50, 90, 4, ctypes.byref(out)) == 0
+    assert out.value == (70 + 4) * 48 - 70 * 40  # no top band at the free surface
+    bad = N.Grid(120, 140, 141, 2, 0.001, 10.0)
+    assert lib.sgb_ring_size(ctypes.byref(bad), 50, 70, 50, 90, 4, ctypes.byref(out)) == 3  # pitch % 4
+    assert lib.sgb_ring_size(ctypes.byref(g), 50, 70, 50, 90, 0, ctypes.byref(out)) == 1
+
+
+def test_calls_validate_before_touching_the_gpu(lib):
+    from seistorch_gb300 import _native as N
+    g = N.Grid(64, 64, 64, 1, 0.001, 10.0)
+    m = N.AcousticModel(3, 0, 50, 0, None, None, None)
+    assert lib.sgb_acoustic_step(ctypes.byref(g), ctypes.byref(m), None, None, None, None) == 1
+    m = N.AcousticModel(3, 0, 50, 0, ctypes.c_void_p(16), None, None)
+    assert lib.sgb_acoustic_step(ctypes.byref(g), ctypes.byref(m), None, None, None, None) == 5
+    m = N.AcousticModel(4, 0, 50, 0, ctypes.c_void_p(18), None, None)
+    assert lib.sgb_acoustic_step(ctypes.byref(g), ctypes.byref(m), ctypes.c_void_p(16), ctypes.c_void_p(16),
+                                 ctypes.c_void_p(32), None) == 3
+    g0 = N.Grid(64, 64, 64, 0, 0.001, 10.0)
+    assert lib.sgb_acoustic_step(ctypes.byref(g0), ctypes.byref(m), None, None, None, None) == 2
+
+
+def test_acquisition_tables():
+    from seistorch_gb300.engine import Acquisition
+    nz, nx = 30, 40
+    sources = [[(3, 4), (3, 4), (5, 6)], [(7, 8)]]
+    receivers = [([2, 2, 9], [30, 1, 5]), ([4], [4])]
+    acq = Acquisition(nz, nx, sources, receivers, np.zeros(10, np.float32), "cpu")
+    assert acq.nsrc == 3  # duplicate point injects once (0/1 mask)
+    assert acq.src_ptr.tolist() == [0, 2, 3]
+    assert acq.nrec == 4 and acq.reccounts == [3, 1]
+    ptr = acq.rec_row_ptr.numpy()
+    # shot 0 row 2 holds x = 1, 30 (sorted), output columns 1, 0
+    s, e = ptr[0 * nz + 2], ptr[0 * nz + 3]
+    assert acq.rec_x[s:e].tolist() == [1, 30] and acq.rec_col[s:e].tolist() == [1, 0]
+    s, e = ptr[1 * nz + 4], ptr[1 * nz + 5]
+    assert acq.rec_col[s:e].tolist() == [3]
+    with pytest.raises(IndexError):
+        Acquisition(nz, nx, [[(30, 0)]], [([0], [0])], np.zeros(3), "cpu")
+    with pytest.raises(IndexError):
+        Acquisition(nz, nx, [[(0, 0)]], [([0], [40])], np.zeros(3), "cpu")
+
+
+@pytest.mark.parametrize("name", ["acoustic_pml_o4", "acoustic_pml_o4_multiple", "acoustic_habc_o2",
+                                  "acoustic_habc_o2_multiple"])
+def test_boundary_coefficients_match_reference(name):
+    from seistorch_gb300 import habc, pml
+    g = load(name)
+    torch.set_default_dtype(torch.float64)
+    try:
+        shape = g["models"]["vp"].shape
+        if g["habc"]:
+            d = habc.generate_habc_coefficients_2d(shape, g["width"], multiple=g["multiple"])
+        else:
+            d = pml.generate_pml_coefficients_2d(shape, g["width"], multiple=g["multiple"])
+    finally:
+        torch.set_default_dtype(torch.float32)
+    np.testing.assert_allclose(d.numpy(), g["d"], rtol=1e-13, atol=1e-12)
+
+
+def test_habc_masks_match_oracle():
+    from oracle import fd2d
+    from seistorch_gb300 import habc
+    for multiple in (False, True):
+        a = habc.bound_mask(120, 130, 50, "cpu", return_idx=True, multiple=multiple)
+        b = fd2d.habc_masks(120, 130, 50, multiple)
+        for x, y in zip(a, b):
+            if y is None:
+                assert x is None
+            else:
+                assert np.array_equal(x.numpy(), y)
+
+
+def test_config_reader_handles_template_subset():
+    from seistorch_gb300.config import loads
+    text = """
+# comment
+dtype: float32
+equation: acoustic
+geom:
+  dt: 0.001
+  h: 10.0
+  multiple: false
+  boundary:
+    type: pml
+    width: 50
+  source_type:
+    - h1
+  invlist:
+    vp: true
+    rho: false
+  wavelet:
+  multiscale:
+    - - 1.0
+      - 3.0
+    - 5.0
+    - all
+  shape: [3, 4]
+"""
+    c = loads(text)
+    assert c["dtype"] == "float32" and c["geom"]["dt"] == 0.001
+    assert c["geom"]["boundary"] == {"type": "pml", "width": 50}
+    assert c["geom"]["source_type"] == ["h1"]
+    assert c["geom"]["invlist"] == {"vp": True, "rho": False}
+    assert c["geom"]["wavelet"] is None
+    assert c["geom"]["multiscale"] == [[1.0, 3.0], 5.0, "all"]
+    assert c["geom"]["shape"] == [3, 4]
+
+
+def test_ricker_matches_oracle():
+    from oracle import fd2d
+    from seistorch_gb300.utils import ricker_wave
+    assert np.array_equal(ricker_wave(12.0, 0.0005, 300, delay=90, dtype="numpy"),
+                          fd2d.ricker(12.0, 0.0005, 300, delay=90))
+
+
+def test_product_path_never_imports_the_oracle():
+    pkg = os.path.join(ROOT, "seistorch_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for fn in files:
+            if fn.endswith(".py"):
+                text = open(os.path.join(dirpath, fn)).read()
+                assert "import oracle" not in text and "from oracle" not in text, fn
+
+
+def test_gpu_entry_points_fail_loudly_without_cuda():
+    from seistorch_gb300 import engine
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(RuntimeError, match="CUDA"):
+        engine.require_cuda(None, "x")
