@@ -18,7 +18,8 @@ def _inject(fields, b, zs, xs, vals):
     np.add.at(fields[b], (np.asarray(zs, int), np.asarray(xs, int)), vals)
 
 
-def acoustic_pml_gradient(vp, d, dt, h, wavelet, sources, receivers, record_grads, order=2):
+def acoustic_pml_gradient(vp, d, dt, h, wavelet, sources, receivers, record_grads, order=2,
+                          dtype=np.float64):
     """dJ/dvp for the 2nd-order acoustic PML loop (acoustic.py:73-86).
 
     Forward: U_{i+1} = A U_i - Bc U_{i-1} + Kv Lh(U_i) + S w_i with
@@ -28,36 +29,37 @@ def acoustic_pml_gradient(vp, d, dt, h, wavelet, sources, receivers, record_grad
       lam_k = R^T g_{k-1} + A lam_{k+1} + Lh(Kv lam_{k+1}) - Bc lam_{k+2}
     Gradient: dJ/dvp = sum_i lam_{i+1} * 2 vp inv * Lh(U_i).
     """
-    vp = np.asarray(vp, np.float64)
-    d = np.asarray(d, np.float64)
+    vp = np.asarray(vp, dtype)
+    d = np.asarray(d, dtype)
+    dt = dtype(dt)
     nt = len(wavelet)
     B = len(sources)
     nz, nx = vp.shape
-    inv = 1.0 / (dt ** -2 + d / dt)
-    A = 2.0 * inv / dt ** 2
+    inv = dtype(1.0) / (dt ** -2 + d / dt)
+    A = dtype(2.0) * inv / dt ** 2
     Bc = inv * (dt ** -2 - d / dt)
     Kv = inv * vp ** 2
-    smask = np.zeros((B, nz, nx))
+    smask = np.zeros((B, nz, nx), dtype)
     for b, pts in enumerate(sources):
         for (z, x) in pts:
             smask[b, z, x] = 1
-    U = [np.zeros((B, nz, nx)), np.zeros((B, nz, nx))]  # U_{-1}, U_0
+    U = [np.zeros((B, nz, nx), dtype), np.zeros((B, nz, nx), dtype)]  # U_{-1}, U_0
     for i in range(nt):
         un = U[-1]
-        y = A * un - Bc * U[-2] + Kv * fd2d.laplacian(un, order, h)
-        U.append(y + smask * np.float64(np.float32(wavelet[i])))
+        y = A * un - Bc * U[-2] + Kv * fd2d.laplacian(un, order, h, dtype)
+        U.append(y + smask * dtype(np.float32(wavelet[i])))
     # U[k+1] holds U_k for k = -1..nt
-    grad = np.zeros((nz, nx))
-    lam1 = np.zeros((B, nz, nx))   # lam_{k+1}
-    lam2 = np.zeros((B, nz, nx))   # lam_{k+2}
+    grad = np.zeros((nz, nx), dtype)
+    lam1 = np.zeros((B, nz, nx), dtype)   # lam_{k+1}
+    lam2 = np.zeros((B, nz, nx), dtype)   # lam_{k+2}
     for k in range(nt, 0, -1):
-        lam = A * lam1 + fd2d.laplacian(Kv * lam1, order, h) - Bc * lam2
+        lam = A * lam1 + fd2d.laplacian(Kv * lam1, order, h, dtype) - Bc * lam2
         for b, (zs, xs) in enumerate(receivers):
-            _inject(lam, b, zs, xs, record_grads[b][k - 1][:, 0])
+            _inject(lam, b, zs, xs, np.asarray(record_grads[b][k - 1][:, 0], dtype))
         # term i = k-1: lam_k * dU_k/dvp = lam_k * 2 vp inv Lh(U_{k-1})
-        grad += np.sum(lam * fd2d.laplacian(U[k], order, h), axis=0)
+        grad += np.sum(lam * fd2d.laplacian(U[k], order, h, dtype), axis=0)
         lam2, lam1 = lam1, lam
-    return grad * 2.0 * vp * inv
+    return grad * dtype(2.0) * vp * inv
 
 
 def _dfwd_T(g, axis):
