@@ -284,10 +284,10 @@ def main():
                    "parallelism": f"shots x{world}"},
         "shots_per_s": NSHOTS * world / (ms_step * 1e-3),
         "phases_ms": {"forward": fwd_ms, "adjoint": bwd_ms},
-        "roofline": {"kernel": "acoustic_bwd_kernel", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": "acoustic_bwd_tile_kernel", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "bytes_per_launch": bwd_bytes, "launch_ms": bwd_launch_ms},
-        "roofline_forward": {"kernel": "acoustic_fwd_kernel", "achieved": fwd_bytes / (fwd_launch_ms * 1e-3) / 1e9,
+        "roofline_forward": {"kernel": "acoustic_fwd_tile_kernel", "achieved": fwd_bytes / (fwd_launch_ms * 1e-3) / 1e9,
                              "frac": fwd_bytes / (fwd_launch_ms * 1e-3) / 1e9 / peak, "unit": "GB/s",
                              "launch_ms": fwd_launch_ms},
         "gpu_launches": args.steps * (NT + (NT - 1) + 2),

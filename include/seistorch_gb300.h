@@ -43,7 +43,9 @@ typedef struct {
 } sgb_grid;
 
 /* Acquisition for one time loop (rnn.py:158-212, source.py:47-57,
- * probe.py:42-44).  Sources: CSR by shot; each point receives
+ * probe.py:42-44).  The optional per-shot row ranges let the kernels skip
+ * the source / receiver lookups for tiles away from them.
+ * Sources: CSR by shot; each point receives
  * wavelet[wrow * nt + t] at step t (the smask*X add; the caller removes
  * duplicate points within a shot, as the 0/1 mask does).  Receivers: CSR by
  * (shot, row) -- rec_row_ptr[b * nz + z] .. rec_row_ptr[b * nz + z + 1] --
@@ -62,6 +64,8 @@ typedef struct {
   int32_t nrec;               /* record matrix width                  */
   int32_t nch;                /* channels per record (receiver types) */
   float *records;             /* [nt][nrec][nch] out (may be NULL)    */
+  const int32_t *src_zr;      /* [nshots][2] first source row, last+1 (nullable) */
+  const int32_t *rec_zr;      /* [nshots][2] first receiver row, last+1 (nullable) */
 } sgb_acquisition;
 
 /* 2nd-order-in-time acoustic model (acoustic.py:73-86, acoustic_habc.py:206-221).
@@ -101,6 +105,12 @@ int sgb_last_cuda_error(void);
 /* Reads (and with reset != 0 clears) the device status word that kernels set
  * on capacity faults (bit 1: too many sources in one tile).  Synchronous. */
 int sgb_device_status(int *out, int reset);
+
+/* Select the tile-pipeline variant used by later PML calls (host-only,
+ * process-wide): fwd_cfg in [0, 6) and bwd_cfg in [0, 4) index the compiled
+ * (rows per tile, warps per CTA, pipeline stages) variants; `reserved` must
+ * be 0.  The autotuner (seistorch_gb300.tuning) times the variants per grid. */
+int sgb_set_stream_config(int32_t fwd_cfg, int32_t bwd_cfg, int32_t reserved);
 
 /* Floats per shot per step of the boundary ring (host-only helper). */
 int sgb_ring_size(const sgb_grid *grid, int32_t iz0, int32_t iz1, int32_t ix0, int32_t ix1,

@@ -19,7 +19,8 @@ INCLUDE = os.path.join(ROOT_DIR, "include")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_NAME = "libseistorch_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
-SOURCES = ["acoustic.cu", "elastic.cu", "capi.cu"]
+SOURCES = ["acoustic.cu", "acoustic_stream.cu", "acoustic_stream_fwd.cu", "acoustic_stream_bwd.cu",
+           "elastic.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -80,7 +81,8 @@ class Acquisition(ctypes.Structure):
     _fields_ = [("src_ptr", c_ptr), ("src_z", c_ptr), ("src_x", c_ptr), ("src_wrow", c_ptr),
                 ("wavelet", c_ptr), ("nsrc", c_i32), ("nt", c_i32),
                 ("rec_row_ptr", c_ptr), ("rec_x", c_ptr), ("rec_col", c_ptr),
-                ("nrec", c_i32), ("nch", c_i32), ("records", c_ptr)]
+                ("nrec", c_i32), ("nch", c_i32), ("records", c_ptr),
+                ("src_zr", c_ptr), ("rec_zr", c_ptr)]
 
 
 class AcousticModel(ctypes.Structure):
@@ -106,6 +108,7 @@ SIGNATURES = {
     "sgb_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "sgb_last_cuda_error": (ctypes.c_int, []),
     "sgb_device_status": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
+    "sgb_set_stream_config": (ctypes.c_int, [c_i32, c_i32, c_i32]),
     "sgb_ring_size": (ctypes.c_int, [ctypes.POINTER(Grid), c_i32, c_i32, c_i32, c_i32, c_i32,
                                      ctypes.POINTER(c_i32)]),
     "sgb_acoustic_coefficients": (ctypes.c_int, [ctypes.POINTER(Grid), c_ptr, c_ptr, c_i32, c_ptr, c_ptr]),

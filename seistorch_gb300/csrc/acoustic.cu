@@ -252,174 +252,6 @@ __global__ void __launch_bounds__(NTHREADS) acoustic_fwd_kernel(const AcStepArgs
   }
 }
 
-// ------------------------------------------------ adjoint (PML, fused) ---
-
-
-template <int R, int TZ>
-__global__ void __launch_bounds__(NTHREADS) acoustic_bwd_kernel(const AcBwdArgs a) {
-  constexpr int HR = R;
-  constexpr int RPW = TZ / NW;
-  extern __shared__ __align__(16) float smem[];
-  float* s_u = smem;                         // U_{j-1}, haloed
-  float* s_l = s_u + (TZ + 2 * HR) * SROW;    // Lambda_{j+1}, haloed
-  float* s_k = s_l + (TZ + 2 * HR) * SROW;    // k, haloed
-  float* s_un = s_k + (TZ + 2 * HR) * SROW;   // U_j
-  float* s_l2 = s_un + TZ * TX;               // Lambda_{j+2}
-  float* s_g = s_l2 + TZ * TX;
-  float* s_inj = s_g + TZ * TX;               // adjoint source tile
-  int* s_src = reinterpret_cast<int*>(s_inj + TZ * TX);
-  float* s_srcv = reinterpret_cast<float*>(s_src + 2 * MAX_TILE_SRC + 1);
-
-  const int tid = threadIdx.x;
-  const int b = blockIdx.x % a.nshots;
-  const int tile = blockIdx.x / a.nshots;
-  const int x0 = (tile % a.ntx) * TX;
-  const int z0 = (tile / a.ntx) * TZ;
-  const long long base = (long long)b * a.sstride;
-
-  constexpr int UCH = SROW / 4;
-  for (int c = tid; c < (TZ + 2 * HR) * UCH; c += NTHREADS) {
-    const int r = c / UCH, cc = c - r * UCH;
-    const int z = z0 - HR + r, x = x0 - HX + 4 * cc;
-    const int nb = chunk_bytes(z, x, a.nz, a.nx);
-    const long long off = (long long)z * a.pitch + x;
-    cp_async16(s_u + r * SROW + 4 * cc, nb ? a.ucur + base + off : a.ucur, nb);
-    cp_async16(s_l + r * SROW + 4 * cc, nb ? a.l1 + base + off : a.l1, nb);
-    cp_async16(s_k + r * SROW + 4 * cc, nb ? a.k + off : a.k, nb);
-  }
-  constexpr int PCH = TX / 4;
-  for (int c = tid; c < TZ * PCH; c += NTHREADS) {
-    const int r = c / PCH, cc = c - r * PCH;
-    const int z = z0 + r, x = x0 + 4 * cc;
-    const int nb = chunk_bytes(z, x, a.nz, a.nx);
-    const long long off = (long long)z * a.pitch + x;
-    cp_async16(s_un + r * TX + 4 * cc, nb ? a.unext + base + off : a.unext, nb);
-    cp_async16(s_l2 + r * TX + 4 * cc, nb ? a.l2 + base + off : a.l2, nb);
-    cp_async16(s_g + r * TX + 4 * cc, nb ? a.g + off : a.g, nb);
-    sts4(s_inj + r * TX + 4 * cc, make_float4(0.f, 0.f, 0.f, 0.f));
-  }
-  cp_async_commit();
-  if (tid == 0) s_src[2 * MAX_TILE_SRC] = 0;
-  __syncthreads();
-  // adjoint sources (R^T of the record gather) into the tile
-  if (a.resid != nullptr) {
-    const int lane = tid & 31, wid = tid >> 5;
-    for (int lr = wid; lr < TZ; lr += NW) {
-      const int z = z0 + lr;
-      if (z >= a.nz) break;
-      const int p0 = a.rec_row_ptr[b * a.nz + z], p1 = a.rec_row_ptr[b * a.nz + z + 1];
-      for (int q = p0 + lane; q < p1; q += 32) {
-        const int rx = a.rec_x[q] - x0;
-        if (rx >= 0 && rx < TX) atomicAdd(s_inj + lr * TX + rx, a.resid[(long long)a.rec_col[q] * a.nch]);
-      }
-    }
-  }
-  // forward sources of time j-1, removed from U_j before reversing
-  if (a.do_recon && a.src_ptr != nullptr) {
-    const int p0 = a.src_ptr[b], p1 = a.src_ptr[b + 1];
-    for (int q = p0 + tid; q < p1; q += NTHREADS) {
-      const int zs = a.src_z[q] - z0, xs = a.src_x[q] - x0;
-      if (zs >= 0 && zs < TZ && xs >= 0 && xs < TX) {
-        const int slot = atomicAdd(&s_src[2 * MAX_TILE_SRC], 1);
-        if (slot < MAX_TILE_SRC) {
-          s_src[2 * slot] = zs;
-          s_src[2 * slot + 1] = xs;
-          s_srcv[slot] = a.wavelet[(long long)a.src_wrow[q] * a.nt + a.t_src];
-        } else {
-          atomicOr(a.status, DEV_ERR_CAPACITY);
-        }
-      }
-    }
-  }
-  cp_async_wait_all();
-  __syncthreads();
-  const int lane = tid & 31, wid = tid >> 5;
-  const int xl = 4 * lane;
-  const int x = x0 + xl;
-  const int sr0 = HR + wid * RPW;
-  // centre values of Lambda_{j+1} before the tile becomes k * Lambda_{j+1}
-  float4 l1c[RPW];
-#pragma unroll
-  for (int i = 0; i < RPW; ++i) l1c[i] = lds4(s_l + (sr0 + i) * SROW + HX + xl);
-  const int nsrc = min(s_src[2 * MAX_TILE_SRC], MAX_TILE_SRC);
-  __syncthreads();
-  for (int c = tid; c < (TZ + 2 * HR) * UCH; c += NTHREADS) {
-    float4 ll = lds4(s_l + 4 * c);
-    const float4 kk = lds4(s_k + 4 * c);
-    ll.x *= kk.x; ll.y *= kk.y; ll.z *= kk.z; ll.w *= kk.w;
-    sts4(s_l + 4 * c, ll);
-  }
-  for (int s = tid; s < nsrc; s += NTHREADS)  // U~_j = U_j - s w_{j-1}
-    s_un[s_src[2 * s] * TX + s_src[2 * s + 1]] -= s_srcv[s];
-  __syncthreads();
-
-  const bool ring_tile = a.ring.touches(z0, TZ, x0, TX);
-  float4 wu[2 * R + 1], wl[2 * R + 1];
-#pragma unroll
-  for (int j = 0; j < 2 * R; ++j) {
-    wu[j] = lds4(s_u + (sr0 - R + j) * SROW + HX + xl);
-    wl[j] = lds4(s_l + (sr0 - R + j) * SROW + HX + xl);
-  }
-#pragma unroll
-  for (int i = 0; i < RPW; ++i) {
-    const int sr = sr0 + i;
-    const int lr = wid * RPW + i;
-    const int z = z0 + lr;
-    wu[2 * R] = lds4(s_u + (sr + R) * SROW + HX + xl);
-    wl[2 * R] = lds4(s_l + (sr + R) * SROW + HX + xl);
-    const float4 LU = lap4<R>(wu, lds4(s_u + sr * SROW + xl), lds4(s_u + sr * SROW + 2 * HX + xl), a.w);
-    const float4 LK = lap4<R>(wl, lds4(s_l + sr * SROW + xl), lds4(s_l + sr * SROW + 2 * HX + xl), a.w);
-    const float4 l1 = l1c[i];
-    const float4 l2 = lds4(s_l2 + lr * TX + xl);
-    const float4 vg = lds4(s_g + lr * TX + xl);
-    const float4 vk = lds4(s_k + sr * SROW + HX + xl);
-    const float4 inj = lds4(s_inj + lr * TX + xl);
-    // Lambda_j = g (L1 - L2) + L2 + L(k L1) + R^T resid
-    float4 lj;
-    lj.x = fmaf(vg.x, l1.x - l2.x, l2.x) + LK.x + inj.x;
-    lj.y = fmaf(vg.y, l1.y - l2.y, l2.y) + LK.y + inj.y;
-    lj.z = fmaf(vg.z, l1.z - l2.z, l2.z) + LK.z + inj.z;
-    lj.w = fmaf(vg.w, l1.w - l2.w, l2.w) + LK.w + inj.w;
-    if (z < a.nz && x < a.nx) {
-      const long long off = base + (long long)z * a.pitch + x;
-      *reinterpret_cast<float4*>(a.lout + off) = lj;
-      // gradient term i = j-1: Lambda_j * L(U_{j-1}), interior box only
-      if (z >= a.ring.iz0 && z < a.ring.iz1 && x + 3 >= a.ring.ix0 && x < a.ring.ix1) {
-        float4 gs = *reinterpret_cast<const float4*>(a.grad_shot + off);
-#pragma unroll
-        for (int m = 0; m < 4; ++m)
-          if (x + m >= a.ring.ix0 && x + m < a.ring.ix1)
-            set_comp(gs, m, fmaf(comp(lj, m), comp(LU, m), comp(gs, m)));
-        *reinterpret_cast<float4*>(a.grad_shot + off) = gs;
-      }
-      if (a.do_recon) {
-        // U_{j-2} = g (U_{j-1} - U~_j) + U~_j + k L(U_{j-1})  (g = 2 inside the box),
-        // the ring from the saved strips, 0 in the damped band
-        const float4 un = lds4(s_un + lr * TX + xl);
-        float4 uo;
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          const int xm = x + m;
-          float v = 0.f;
-          if (a.ring.inside(z, xm)) {
-            v = fmaf(comp(vk, m), comp(LU, m), fmaf(comp(vg, m), comp(wu[R], m) - comp(un, m), comp(un, m)));
-          } else if (ring_tile && a.ring_in != nullptr && xm < a.nx) {
-            const int ri = a.ring.index(z, xm);
-            if (ri >= 0) v = a.ring_in[(long long)b * a.ring.size + ri];
-          }
-          set_comp(uo, m, v);
-        }
-        *reinterpret_cast<float4*>(a.uout + off) = uo;
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < 2 * R; ++j) {
-      wu[j] = wu[j + 1];
-      wl[j] = wl[j + 1];
-    }
-  }
-}
-
 // ------------------------------------------- single-step VJP (PML) ---
 
 
@@ -531,7 +363,7 @@ __global__ void acoustic_coef_kernel(int nz, int nx, int pitch, const float* __r
 
 __global__ void acoustic_grad_reduce_kernel(int nz, int nx, int pitch, int nshots, long long sstride,
                                             const float* __restrict__ grad_shot,
-                                            const float* __restrict__ vp, float dt2_h2, Ring ring,
+                                            const float* __restrict__ vp, Ring ring,
                                             float* __restrict__ grad_vp) {
   const long long n = (long long)nz * pitch;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -539,8 +371,9 @@ __global__ void acoustic_grad_reduce_kernel(int nz, int nx, int pitch, int nshot
     const int z = (int)(i / pitch), x = (int)(i % pitch);
     float s = 0.f;
     if (x < nx && ring.inside(z, x)) {
+      // the adjoint is carried as nu = k * Lambda: dJ/dvp = (2/vp) sum nu L(U)
       for (int b = 0; b < nshots; ++b) s += grad_shot[b * sstride + i];
-      s *= 2.f * vp[i] * dt2_h2;
+      s *= 2.f / vp[i];
     }
     grad_vp[i] = s;
   }
@@ -552,10 +385,6 @@ template <int R, int TZ, bool HABC>
 static size_t fwd_smem() {
   constexpr int HR = (HABC && R < 2) ? 2 : R;
   return sizeof(float) * ((TZ + 2 * HR) * SROW + 3 * TZ * TX) + sizeof(int) * (3 * MAX_TILE_SRC + 1);
-}
-template <int R, int TZ>
-static size_t bwd_smem() {
-  return sizeof(float) * (3 * (TZ + 2 * R) * SROW + 4 * TZ * TX) + sizeof(int) * (3 * MAX_TILE_SRC + 1);
 }
 template <int R, int TZ>
 static size_t vjp_smem() {
@@ -574,21 +403,6 @@ static cudaError_t launch_fwd_t(const AcStepArgs& a, int ntz, cudaStream_t s) {
   }
   const long long nblk = (long long)a.nshots * a.ntx * ntz;
   acoustic_fwd_kernel<R, TZ, HABC><<<(unsigned)nblk, NTHREADS, sm, s>>>(a);
-  return cudaGetLastError();
-}
-
-template <int R, int TZ>
-static cudaError_t launch_bwd_t(const AcBwdArgs& a, int ntz, cudaStream_t s) {
-  const size_t sm = bwd_smem<R, TZ>();
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(acoustic_bwd_kernel<R, TZ>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
-  const long long nblk = (long long)a.nshots * a.ntx * ntz;
-  acoustic_bwd_kernel<R, TZ><<<(unsigned)nblk, NTHREADS, sm, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -641,26 +455,6 @@ cudaError_t launch_acoustic_fwd(int R, bool habc, int tz, const AcStepArgs& a, c
   return fwd_by_r<8, false>(R, a, ntz, s);
 }
 
-cudaError_t launch_acoustic_bwd(int R, int tz, const AcBwdArgs& a, cudaStream_t s) {
-  const int ntz = (a.nz + tz - 1) / tz;
-  if (tz == 16) {
-    switch (R) {
-      case 1: return launch_bwd_t<1, 16>(a, ntz, s);
-      case 2: return launch_bwd_t<2, 16>(a, ntz, s);
-      case 3: return launch_bwd_t<3, 16>(a, ntz, s);
-      case 4: return launch_bwd_t<4, 16>(a, ntz, s);
-    }
-  } else {
-    switch (R) {
-      case 1: return launch_bwd_t<1, 8>(a, ntz, s);
-      case 2: return launch_bwd_t<2, 8>(a, ntz, s);
-      case 3: return launch_bwd_t<3, 8>(a, ntz, s);
-      case 4: return launch_bwd_t<4, 8>(a, ntz, s);
-    }
-  }
-  return cudaErrorInvalidValue;
-}
-
 cudaError_t launch_acoustic_vjp(int R, const AcVjpArgs& a, cudaStream_t s) {
   constexpr int TZ = 16;
   const int ntz = (a.nz + TZ - 1) / TZ;
@@ -685,10 +479,8 @@ cudaError_t launch_acoustic_grad_reduce(const sgb_grid& gr, const float* grad_sh
                                         const Ring& ring, float* grad_vp, cudaStream_t s) {
   const long long n = (long long)gr.nz * gr.pitch;
   const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
-  const float dt2_h2 = (gr.dt * gr.dt) / (gr.h * gr.h);
   acoustic_grad_reduce_kernel<<<blocks, 256, 0, s>>>(gr.nz, gr.nx, gr.pitch, gr.nshots,
-                                                     (long long)gr.nz * gr.pitch, grad_shot, vp, dt2_h2,
-                                                     ring, grad_vp);
+                                                     (long long)gr.nz * gr.pitch, grad_shot, vp, ring, grad_vp);
   return cudaGetLastError();
 }
 

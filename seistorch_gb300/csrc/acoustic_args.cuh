@@ -39,40 +39,6 @@ struct AcStepArgs {
   int* status;
 };
 
-// Fused adjoint step (PML): Lambda_j, U_{j-2} and the gradient term.
-struct AcBwdArgs {
-  int nz, nx, pitch, nshots, ntx;
-  long long sstride;
-  const float* __restrict__ ucur;   // U_{j-1} (stencil)
-  const float* __restrict__ unext;  // U_j
-  float* __restrict__ uout;         // U_{j-2}
-  const float* __restrict__ l1;     // Lambda_{j+1} (stencil)
-  const float* __restrict__ l2;     // Lambda_{j+2}
-  float* __restrict__ lout;         // Lambda_j
-  const float* __restrict__ g;
-  const float* __restrict__ k;
-  FdWeights w;
-  float* __restrict__ grad_shot;  // [nshots][nz][pitch]
-  // reconstruction
-  int do_recon;
-  const float* __restrict__ ring_in;  // [nshots][ring.size] of U_{j-2}, or null (U_{j-2} = 0)
-  Ring ring;
-  // forward sources at time j-1 (subtracted from U_j)
-  const int* __restrict__ src_ptr;
-  const int* __restrict__ src_z;
-  const int* __restrict__ src_x;
-  const int* __restrict__ src_wrow;
-  const float* __restrict__ wavelet;
-  int nt, t_src;
-  // adjoint sources: dJ/d records at time j-1
-  const int* __restrict__ rec_row_ptr;
-  const int* __restrict__ rec_x;
-  const int* __restrict__ rec_col;
-  int nrec, nch;
-  const float* __restrict__ resid;  // resid + (j-1)*nrec*nch (channel 0)
-  int* status;
-};
-
 // Single-step vector-Jacobian product (PML).
 struct AcVjpArgs {
   int nz, nx, pitch, nshots, ntx;
@@ -87,6 +53,68 @@ struct AcVjpArgs {
   const float* __restrict__ k;
   const float* __restrict__ vp;
   FdWeights w;
+};
+
+// Streaming forward step (PML): TMA-fed per-warp strips.
+struct AcStreamArgs {
+  int nz, nx, pitch, nshots, ntx, zc, nzc;
+  int nseg, tpu;  // tiles per column band and per unit (1: every tile stands alone)
+  const float* __restrict__ um;   // U_{n-1}
+  const float* __restrict__ g;    // coefficient planes
+  const float* __restrict__ k;
+  const int* __restrict__ src_zr;
+  const int* __restrict__ rec_zr;
+  long long sstride;
+  float* __restrict__ un;
+  FdWeights w;
+  const int* __restrict__ src_ptr;
+  const int* __restrict__ src_z;
+  const int* __restrict__ src_x;
+  const int* __restrict__ src_wrow;
+  const float* __restrict__ wavelet;
+  int nt, t;
+  const int* __restrict__ rec_row_ptr;
+  const int* __restrict__ rec_x;
+  const int* __restrict__ rec_col;
+  int nrec, nch;
+  float* __restrict__ records;
+  float* __restrict__ illum;
+  float* __restrict__ ring_out;
+  Ring ring;
+  int* status;
+};
+
+// Fused adjoint step (PML) of the TMA tile pipeline; the adjoint is carried
+// as nu = k * Lambda.
+struct AcBwdStreamArgs {
+  int nz, nx, pitch, nshots, ntx, zc, nzc;
+  int nseg, tpu;
+  const float* __restrict__ unext;  // U_j
+  const float* __restrict__ n2;     // nu_{j+2}
+  const float* __restrict__ g;
+  const float* __restrict__ k;
+  const int* __restrict__ src_zr;
+  const int* __restrict__ rec_zr;
+  long long sstride;
+  float* __restrict__ lout;       // nu_j
+  float* __restrict__ uout;       // U_{j-2}
+  float* __restrict__ grad_shot;  // read through TMA, written here
+  FdWeights w;
+  int do_recon;
+  const float* __restrict__ ring_in;
+  Ring ring;
+  const int* __restrict__ src_ptr;
+  const int* __restrict__ src_z;
+  const int* __restrict__ src_x;
+  const int* __restrict__ src_wrow;
+  const float* __restrict__ wavelet;
+  int nt, t_src;
+  const int* __restrict__ rec_row_ptr;
+  const int* __restrict__ rec_x;
+  const int* __restrict__ rec_col;
+  int nrec, nch;
+  const float* __restrict__ resid;
+  int* status;
 };
 
 }  // namespace sgb

@@ -1,0 +1,201 @@
+// Forward step of the acoustic PML equation as a TMA tile pipeline (see
+// stream_common.cuh): u+ = g (u - u-) + u- + k L(u) (acoustic.py:73-86),
+// with source injection (source.py:47-57), receiver sampling (probe.py:42-44),
+// the boundary ring for the adjoint and the illumination sum fused in.
+#include "stream_common.cuh"
+
+namespace sgb {
+
+// PT: the previous field travels through the TMA stage (prefetched S-1
+// tiles ahead) instead of a global load issued before the stage wait.
+template <int R, int TZ, int S, bool PT>
+struct FwdTileLayout {
+  static constexpr int UW = Row<R>::W;
+  static constexpr int UROWS = TZ + 2 * R;
+  static constexpr int UF = round32(UROWS * UW);
+  static constexpr int STAGE = UF + (PT ? TZ * TX : 0);
+  static constexpr size_t BYTES = (size_t)S * STAGE * 4 + S * 8;
+  static constexpr uint32_t TX_BYTES = (UROWS * UW + (PT ? TZ * TX : 0)) * 4;
+};
+
+template <int R, int TZ, int NWP, int S, bool PT>
+__global__ void __launch_bounds__(32 * NWP) acoustic_fwd_tile_kernel(
+    const __grid_constant__ CUtensorMap tm_u,   // U_n [nshots][nz][nx], box {W, TZ+2R, 1}
+    const __grid_constant__ CUtensorMap tm_um,  // U_{n-1} box {128, TZ, 1} (used when PT)
+    const AcStreamArgs a) {
+  using Lay = FwdTileLayout<R, TZ, S, PT>;
+  constexpr int RPW = TZ / NWP;
+  constexpr int UW = Lay::UW, LO = Row<R>::LO;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float* smem = reinterpret_cast<float*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * Lay::STAGE);
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int ntiles = a.nshots * a.ntx * a.nzc;
+  const int G = gridDim.x;
+
+  auto issue = [&](int t, int stage) {
+    const Tile g = tile_geom(t, a.nshots, a.ntx, TZ);
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&bars[stage], Lay::TX_BYTES);
+    tma_load_3d(smem + stage * Lay::STAGE, &tm_u, g.x0 - LO, g.z0 - R, g.b, &bars[stage]);
+    if (PT) tma_load_3d(smem + stage * Lay::STAGE + Lay::UF, &tm_um, g.x0, g.z0, g.b, &bars[stage]);
+  };
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
+    fence_mbar_init();
+    s_abort = 0;
+    for (int s = 0; s < S; ++s)
+      if ((int)blockIdx.x + s * G < ntiles) issue(blockIdx.x + s * G, s);
+  }
+  __syncthreads();
+  int k = 0;
+  for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
+    const int stage = k % S;
+    const Tile g = tile_geom(t, a.nshots, a.ntx, TZ);
+    const int x = g.x0 + 4 * lane;
+    const bool xin = x < a.nx;
+    const int zw = g.z0 + wid * RPW;  // first row of this warp
+    // point operands of this warp's rows, issued before the stage wait
+    float4 vm[RPW], vg[RPW], vk[RPW];
+    const long long fbase = (long long)g.b * a.sstride;
+#pragma unroll
+    for (int i = 0; i < RPW; ++i) {
+      const int z = zw + i;
+      if (xin && z < a.nz) {
+        const long long mo = (long long)z * a.pitch + x;
+        if (!PT) vm[i] = ldg4(a.um + fbase + mo);
+        vg[i] = ldg4(a.g + mo);
+        vk[i] = ldg4(a.k + mo);
+      } else {
+        vm[i] = vg[i] = vk[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    WarpSrc src{0u, -1, 0, 0.f};
+    if (a.src_ptr != nullptr) {
+      const int2 zr = __ldg(reinterpret_cast<const int2*>(a.src_zr) + g.b);
+      if (zr.x < zw + RPW && zr.y > zw)
+        src = warp_sources(lane, g.b, zw, RPW, g.x0, a.src_ptr, a.src_z, a.src_x, a.src_wrow, a.wavelet, a.nt,
+                           a.t, a.status);
+    }
+    bool has_rec = false;
+    if (a.records != nullptr) {
+      const int2 zr = __ldg(reinterpret_cast<const int2*>(a.rec_zr) + g.b);
+      has_rec = zr.x < g.z0 + TZ && zr.y > g.z0;
+    }
+    if (!mbar_wait(&bars[stage], (k / S) & 1, a.status)) s_abort = 1;
+    const float* st = smem + stage * Lay::STAGE;
+    const bool ring_tile = a.ring_out != nullptr && a.ring.touches(g.z0, TZ, g.x0, TX);
+    const int lr0 = wid * RPW;
+    if (PT) {
+#pragma unroll
+      for (int i = 0; i < RPW; ++i) vm[i] = lds4(st + Lay::UF + (lr0 + i) * TX + 4 * lane);
+    }
+    float4 win[2 * R + 1];
+#pragma unroll
+    for (int j = 0; j < 2 * R; ++j) win[j] = lds4(st + (lr0 + j) * UW + LO + 4 * lane);
+    float* outp = a.un + fbase + (long long)zw * a.pitch + x;
+#pragma unroll
+    for (int i = 0; i < RPW; ++i) {
+      const int lr = lr0 + i;
+      const int z = zw + i;
+      win[2 * R] = lds4(st + (lr + 2 * R) * UW + LO + 4 * lane);
+      const float4 L = lap_row<R>(win, st + (lr + R) * UW, lane, a.w);
+      const float4 c = win[R];
+      float4 y;
+      y.x = fmaf(vk[i].x, L.x, fmaf(vg[i].x, c.x - vm[i].x, vm[i].x));
+      y.y = fmaf(vk[i].y, L.y, fmaf(vg[i].y, c.y - vm[i].y, vm[i].y));
+      y.z = fmaf(vk[i].z, L.z, fmaf(vg[i].z, c.z - vm[i].z, vm[i].z));
+      y.w = fmaf(vk[i].w, L.w, fmaf(vg[i].w, c.w - vm[i].w, vm[i].w));
+      if (src.mask) apply_sources(src, i, lane, 1.f, y);
+      if (z < a.nz && xin) {
+        *reinterpret_cast<float4*>(outp) = y;
+        if (ring_tile) {
+#pragma unroll
+          for (int m = 0; m < 4; ++m) {
+            const int ri = (x + m < a.nx) ? a.ring.index(z, x + m) : -1;
+            if (ri >= 0) a.ring_out[(long long)g.b * a.ring.size + ri] = comp(y, m);
+          }
+        }
+        if (a.illum != nullptr) {
+#pragma unroll
+          for (int m = 0; m < 4; ++m)
+            if (x + m < a.nx) atomicAdd(a.illum + (long long)z * a.pitch + x + m, comp(y, m) * comp(y, m));
+        }
+      }
+      outp += a.pitch;
+#pragma unroll
+      for (int j = 0; j < 2 * R; ++j) win[j] = win[j + 1];
+    }
+    // stage free; this tile's outputs visible to the CTA; abort is uniform
+    if (__syncthreads_or(s_abort)) break;
+    if (tid == 0 && t + S * G < ntiles) issue(t + S * G, stage);
+    if (has_rec) {
+      const int* rp = a.rec_row_ptr + (long long)g.b * a.nz;
+      for (int lr = wid; lr < TZ && g.z0 + lr < a.nz; lr += NWP) {
+        const int z = g.z0 + lr;
+        const int p1 = rp[z + 1];
+        for (int q = rp[z] + lane; q < p1; q += 32) {
+          const int rx = a.rec_x[q];
+          if (rx >= g.x0 && rx < g.x0 + TX)
+            a.records[(long long)a.rec_col[q] * a.nch] = a.un[fbase + (long long)z * a.pitch + rx];
+        }
+      }
+    }
+  }
+  // drain: wait (bounded) for the boxes this CTA issued but did not consume
+  if (s_abort && tid == 0)
+    for (int q = k; q < k + S; ++q)
+      if ((int)blockIdx.x + q * G < ntiles) mbar_wait(&bars[q % S], (q / S) & 1, nullptr);
+}
+
+// ------------------------------------------------------------- launch ---
+
+struct FwdCfg {
+  int tz, nwp, s;
+};
+static const FwdCfg FWD_TILE_CFGS[] = {{16, 4, 3}, {16, 4, 3}, {8, 4, 4}, {32, 8, 2}, {16, 4, 2}, {8, 4, 3}};
+
+template <int R, int TZ, int NWP, int S, bool PT>
+static cudaError_t fwd_tile_t(const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s) {
+  using Lay = FwdTileLayout<R, TZ, S, PT>;
+  const size_t smem = Lay::BYTES + 128;  // + alignment slack
+  auto kern = acoustic_fwd_tile_kernel<R, TZ, NWP, S, PT>;
+  static int blocks = 0;
+  if (blocks == 0) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    blocks = resident_blocks(kern, 32 * NWP, smem);
+  }
+  const int tiles = a.nshots * a.ntx * a.nzc;
+  kern<<<(unsigned)(tiles < blocks ? tiles : blocks), 32 * NWP, smem, s>>>(maps[0], maps[1], a);
+  return cudaGetLastError();
+}
+
+template <int R>
+static cudaError_t fwd_tile_r(const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s) {
+  switch (g_fwd_cfg) {
+    case 0: return fwd_tile_t<R, 16, 4, 3, false>(maps, a, s);
+    case 1: return fwd_tile_t<R, 16, 4, 3, true>(maps, a, s);
+    case 2: return fwd_tile_t<R, 8, 4, 4, true>(maps, a, s);
+    case 3: return fwd_tile_t<R, 32, 8, 2, true>(maps, a, s);
+    case 4: return fwd_tile_t<R, 16, 4, 2, true>(maps, a, s);
+    case 5: return fwd_tile_t<R, 8, 4, 3, true>(maps, a, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+int fwd_tile_rows() { return FWD_TILE_CFGS[g_fwd_cfg].tz; }
+int stencil_box_width(int R) { return (R % 2 == 0) ? TX + 8 : TX + 16; }
+
+cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s) {
+  switch (R) {
+    case 1: return fwd_tile_r<1>(maps, a, s);
+    case 2: return fwd_tile_r<2>(maps, a, s);
+    case 3: return fwd_tile_r<3>(maps, a, s);
+    case 4: return fwd_tile_r<4>(maps, a, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace sgb

@@ -5,6 +5,7 @@
 
 #include "sgb_common.cuh"
 #include "acoustic_args.cuh"
+#include "tma.cuh"
 
 namespace sgb {
 
@@ -51,13 +52,23 @@ FdWeights fd_weights(int order) {
 
 // kernels in acoustic.cu
 cudaError_t launch_acoustic_fwd(int R, bool habc, int tz, const AcStepArgs& a, cudaStream_t s);
-cudaError_t launch_acoustic_bwd(int R, int tz, const AcBwdArgs& a, cudaStream_t s);
 cudaError_t launch_acoustic_vjp(int R, const AcVjpArgs& a, cudaStream_t s);
 cudaError_t launch_acoustic_coef(const sgb_grid& gr, const float* vp, const float* damp, int boundary,
                                  float* g, float* k, cudaStream_t s);
 cudaError_t launch_acoustic_grad_reduce(const sgb_grid& gr, const float* grad_shot, const float* vp,
                                         const Ring& ring, float* grad_vp, cudaStream_t s);
 int pick_tz(int nz, int nx, int nshots, int tz_max);
+// streaming kernels in acoustic_stream.cu
+cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s);
+cudaError_t launch_acoustic_bwd_stream(int R, const CUtensorMap* maps, const AcBwdStreamArgs& a,
+                                       cudaStream_t s);
+int field_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int nshots, int boxw, int rb);
+int coef_map(CUtensorMap* m, const float* coef, int nz, int nx, int pitch, int rb);
+int plane_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int boxw, int rb);
+int fwd_tile_rows();
+int bwd_tile_rows();
+int stencil_box_width(int R);
+int set_stream_config(int fwd, int bwd, int zc);
 
 }  // namespace sgb
 
@@ -156,6 +167,10 @@ int sgb_device_status(int* out, int reset) {
   SGB_CUDA_CHECK(cudaMemcpy(out, p, sizeof(int), cudaMemcpyDeviceToHost));
   if (reset) SGB_CUDA_CHECK(cudaMemset(p, 0, sizeof(int)));
   return SGB_OK;
+}
+
+int sgb_set_stream_config(int32_t fwd_cfg, int32_t bwd_cfg, int32_t zc) {
+  return set_stream_config(fwd_cfg, bwd_cfg, zc) == 0 ? SGB_OK : SGB_ERR_ARG;
 }
 
 int sgb_ring_size(const sgb_grid* grid, int32_t iz0, int32_t iz1, int32_t ix0, int32_t ix1, int32_t ring,
@@ -257,6 +272,38 @@ int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, 
   const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 32);
   const int R = model->order / 2;
   const bool habc = model->boundary == 1;
+  // PML: TMA tile pipeline; HABC: tile kernel (needs the strip neighbours)
+  CUtensorMap mu[3], mum[3];
+  AcStreamArgs sa;
+  std::memset(&sa, 0, sizeof(sa));
+  if (!habc) {
+    const int tzr = fwd_tile_rows();
+    const int bw = stencil_box_width(R);
+    for (int i = 0; i < 3; ++i)
+      if (field_map(&mu[i], buf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R) ||
+          field_map(&mum[i], buf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr))
+        return SGB_ERR_CUDA;
+    sa.nz = a.nz; sa.nx = a.nx; sa.pitch = a.pitch; sa.nshots = a.nshots; sa.ntx = a.ntx;
+    sa.zc = tzr;
+    sa.nzc = (grid->nz + tzr - 1) / tzr;
+    sa.nseg = sa.nzc;
+    sa.tpu = 1;
+    sa.g = a.g;
+    sa.k = a.k;
+    sa.src_zr = acq->src_zr;
+    sa.rec_zr = acq->rec_zr;
+    sa.sstride = a.sstride;
+    sa.w = a.w;
+    sa.src_ptr = a.src_ptr; sa.src_z = a.src_z; sa.src_x = a.src_x; sa.src_wrow = a.src_wrow;
+    sa.wavelet = a.wavelet; sa.nt = a.nt;
+    sa.rec_row_ptr = a.rec_row_ptr; sa.rec_x = a.rec_x; sa.rec_col = a.rec_col;
+    sa.nrec = a.nrec; sa.nch = a.nch;
+    sa.illum = illum;
+    sa.ring = a.ring;
+    sa.status = a.status;
+    if ((a.src_ptr != nullptr && acq->src_zr == nullptr) || (acq->records != nullptr && acq->rec_zr == nullptr))
+      return SGB_ERR_ARG;
+  }
   int cur = 0, prev = 1, nxt = 2;
   for (int t = 0; t < acq->nt; ++t) {
     a.u = buf[cur];
@@ -265,7 +312,17 @@ int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, 
     a.t = t;
     a.records = acq->records ? acq->records + (long long)t * acq->nrec * acq->nch : nullptr;
     a.ring_out = bs ? bs->ring_store + (long long)t * grid->nshots * a.ring.size : nullptr;
-    SGB_CUDA_CHECK(launch_acoustic_fwd(R, habc, tz, a, s));
+    if (habc) {
+      SGB_CUDA_CHECK(launch_acoustic_fwd(R, habc, tz, a, s));
+    } else {
+      sa.un = buf[nxt];
+      sa.um = buf[prev];
+      sa.t = t;
+      sa.records = a.records;
+      sa.ring_out = a.ring_out;
+      const CUtensorMap maps[2] = {mu[cur], mum[prev]};
+      SGB_CUDA_CHECK(launch_acoustic_fwd_stream(R, maps, sa, s));
+    }
     if (bs != nullptr && bs->ckpt_every > 0 && (t + 1) % bs->ckpt_every == 0) {
       float* slot = bs->ckpt_store + (long long)((t + 1) / bs->ckpt_every - 1) * 2 * field;
       SGB_CUDA_CHECK(cudaMemcpyAsync(slot, buf[nxt], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
@@ -301,30 +358,49 @@ int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model,
   cudaStream_t s = (cudaStream_t)stream;
   const long long plane = (long long)grid->nz * grid->pitch;
   const long long field = plane * grid->nshots;
-  AcBwdArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.nz = grid->nz; a.nx = grid->nx; a.pitch = grid->pitch; a.nshots = grid->nshots;
-  a.ntx = (grid->nx + TX - 1) / TX;
-  a.sstride = plane;
-  a.g = model->coef;
-  a.k = model->coef + plane;
-  a.w = fd_weights(model->order);
-  a.grad_shot = grad_shot;
-  a.ring = make_ring(*grid, bs->iz0, bs->iz1, bs->ix0, bs->ix1, bs->ring);
-  if (a.ring.size != bs->ring_size) return SGB_ERR_SHAPE;
-  a.src_ptr = acq->nsrc > 0 ? acq->src_ptr : nullptr;
-  a.src_z = acq->src_z; a.src_x = acq->src_x; a.src_wrow = acq->src_wrow; a.wavelet = acq->wavelet;
-  a.nt = acq->nt;
-  a.rec_row_ptr = acq->rec_row_ptr; a.rec_x = acq->rec_x; a.rec_col = acq->rec_col;
-  a.nrec = acq->nrec; a.nch = acq->nch;
-  a.status = status_ptr();
+  const Ring ring = make_ring(*grid, bs->iz0, bs->iz1, bs->ix0, bs->ix1, bs->ring);
+  if (ring.size != bs->ring_size) return SGB_ERR_SHAPE;
   for (int i = 0; i < 3; ++i) SGB_CUDA_CHECK(cudaMemsetAsync(lbuf[i], 0, field * sizeof(float), s));
   SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot, 0, field * sizeof(float), s));
-  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 16);
   const int R = model->order / 2;
   const int nt = acq->nt;
   const int K = bs->ckpt_every;
   const int nslots = K > 0 ? nt / K : 0;
+  // tensor maps: haloed stencil boxes (136 x (TZ+2R)) and point boxes
+  // (128 x TZ) of every rotating buffer; lbuf carries nu = k * Lambda
+  const int tzr = bwd_tile_rows();
+  const int bw = stencil_box_width(R);
+  CUtensorMap uf[3], nf[3], mgrad;
+  for (int i = 0; i < 3; ++i) {
+    if (field_map(&uf[i], ubuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R) ||
+        field_map(&nf[i], lbuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R))
+      return SGB_ERR_CUDA;
+  }
+  if (field_map(&mgrad, grad_shot, grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr)) return SGB_ERR_CUDA;
+  if ((acq->nsrc > 0 && acq->src_zr == nullptr) || (acq->records != nullptr && acq->rec_zr == nullptr))
+    return SGB_ERR_ARG;
+  AcBwdStreamArgs sb;
+  std::memset(&sb, 0, sizeof(sb));
+  sb.nz = grid->nz; sb.nx = grid->nx; sb.pitch = grid->pitch; sb.nshots = grid->nshots;
+  sb.ntx = (grid->nx + TX - 1) / TX;
+  sb.zc = tzr;
+  sb.nzc = (grid->nz + tzr - 1) / tzr;
+  sb.nseg = sb.nzc;
+  sb.tpu = 1;
+  sb.g = model->coef;
+  sb.k = model->coef + plane;
+  sb.src_zr = acq->src_zr;
+  sb.rec_zr = acq->rec_zr;
+  sb.sstride = plane;
+  sb.grad_shot = grad_shot;
+  sb.w = fd_weights(model->order);
+  sb.ring = ring;
+  sb.src_ptr = acq->nsrc > 0 ? acq->src_ptr : nullptr;
+  sb.src_z = acq->src_z; sb.src_x = acq->src_x; sb.src_wrow = acq->src_wrow; sb.wavelet = acq->wavelet;
+  sb.nt = acq->nt;
+  sb.rec_row_ptr = acq->rec_row_ptr; sb.rec_x = acq->rec_x; sb.rec_col = acq->rec_col;
+  sb.nrec = acq->nrec; sb.nch = acq->nch;
+  sb.status = status_ptr();
   int uj = ucur, ujm1 = uprev, ufree = 3 - ucur - uprev;
   int l1 = 0, l2 = 1, lfree = 2;
   for (int j = nt; j >= 2; --j) {
@@ -334,17 +410,16 @@ int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model,
       const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
       SGB_CUDA_CHECK(cudaMemcpyAsync(ubuf[ujm1], slot, field * sizeof(float), cudaMemcpyDeviceToDevice, s));
     }
-    a.ucur = ubuf[ujm1];
-    a.unext = ubuf[uj];
-    a.uout = ubuf[ufree];
-    a.l1 = lbuf[l1];
-    a.l2 = lbuf[l2];
-    a.lout = lbuf[lfree];
-    a.do_recon = j >= 3;
-    a.ring_in = j >= 3 ? bs->ring_store + (long long)(j - 3) * grid->nshots * a.ring.size : nullptr;
-    a.t_src = j - 1;
-    a.resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
-    SGB_CUDA_CHECK(launch_acoustic_bwd(R, tz, a, s));
+    sb.lout = lbuf[lfree];
+    sb.uout = ubuf[ufree];
+    sb.unext = ubuf[uj];
+    sb.n2 = lbuf[l2];
+    sb.do_recon = j >= 3;
+    sb.ring_in = j >= 3 ? bs->ring_store + (long long)(j - 3) * grid->nshots * ring.size : nullptr;
+    sb.t_src = j - 1;
+    sb.resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
+    const CUtensorMap maps[3] = {uf[ujm1], nf[l1], mgrad};
+    SGB_CUDA_CHECK(launch_acoustic_bwd_stream(R, maps, sb, s));
     if (ck && j >= 3) {
       const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
       SGB_CUDA_CHECK(cudaMemcpyAsync(ubuf[ufree], slot + field, field * sizeof(float), cudaMemcpyDeviceToDevice, s));
@@ -358,7 +433,7 @@ int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model,
     l1 = lfree;
     lfree = old_l2;
   }
-  SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, model->vp, a.ring, grad_vp, s));
+  SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, model->vp, ring, grad_vp, s));
   return SGB_OK;
 }
 

@@ -112,6 +112,19 @@ class Acquisition:
         self.rec_row_ptr = it(ptr)
         self.rec_x = it(xx[order])
         self.rec_col = it(order)
+        # per-shot [first, last+1) rows of sources and receivers
+        szr = np.zeros((nshots, 2), np.int32)
+        rzr = np.zeros((nshots, 2), np.int32)
+        for b in range(nshots):
+            zs_b = [int(z) for z in sz[sp[b]:sp[b + 1]]]
+            if zs_b:
+                szr[b] = (min(zs_b), max(zs_b) + 1)
+        for b in range(nshots):
+            zs_b = zz[bz == b]
+            if len(zs_b):
+                rzr[b] = (int(zs_b.min()), int(zs_b.max()) + 1)
+        self.src_zr = it(szr)
+        self.rec_zr = it(rzr)
         self.rec_b = torch.as_tensor(bz, device=device)
         self.rec_z = torch.as_tensor(zz, device=device)
         self.rec_xs = torch.as_tensor(xx, device=device)
@@ -121,7 +134,7 @@ class Acquisition:
             N.ptr(self.src_ptr), N.ptr(self.src_z), N.ptr(self.src_x), N.ptr(self.src_wrow),
             N.ptr(self.wavelet), self.nsrc, self.nt,
             N.ptr(self.rec_row_ptr), N.ptr(self.rec_x), N.ptr(self.rec_col), self.nrec, int(nch),
-            N.ptr(records))
+            N.ptr(records), N.ptr(self.src_zr), N.ptr(self.rec_zr))
 
 
 def interior_box(nz, nx, bwidth, multiple):
