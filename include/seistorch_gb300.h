@@ -31,7 +31,9 @@ typedef enum {
   SGB_ERR_CUDA = 4,        /* a CUDA runtime call failed (see sgb_last_cuda_error) */
   SGB_ERR_UNSUPPORTED = 5, /* order / option outside what the kernels cover   */
   SGB_ERR_NONFINITE = 6,   /* NaN/Inf found in records (rnn.py:215 -> type.py:41-46) */
-  SGB_ERR_CAPACITY = 7     /* too many sources inside one tile                */
+  SGB_ERR_CAPACITY = 7,    /* too many sources inside one tile                */
+  SGB_ERR_SCRATCH = 8      /* problem larger than the fixed scratch of an
+                              allocation-free entry point                    */
 } sgb_status;
 
 /* Grid shared by every equation. dt, h in seconds / metres. */
@@ -162,6 +164,26 @@ int sgb_acoustic_backward(const sgb_grid *grid, const sgb_acoustic_model *model,
                           float *const ubuf[3], int32_t ucur, int32_t uprev,
                           float *const lbuf[3], float *grad_shot, float *grad_vp,
                           sgb_stream_t stream);
+
+/* Allocation-free adjoint.  No counterpart in the reference: an addition for
+ * callers that cannot allocate device memory themselves (a host application
+ * or plugin framework that owns all device memory and forbids cudaMalloc /
+ * cudaFree on its threads, or a loop that must not allocate while it runs).
+ * Same contract as sgb_acoustic_backward, without the lbuf / grad_shot
+ * scratch arguments: the scratch lives in a fixed 32 MiB device array inside
+ * this library (held by every GPU that loads it until the process exits), so
+ * 4 * nshots * nz * pitch must not exceed 8,388,608 floats; larger problems
+ * return SGB_ERR_SCRATCH before any work.  The first call on a device looks
+ * up the array's address there (cudaGetSymbolAddress with that device
+ * current); make that first call before any stream capture.  All calls share
+ * the one array, which keeps the last call's contents (the adjoint clears what
+ * must start at zero), so calls that overlap on the GPU -- on different
+ * streams or threads -- race and must be serialised by the caller.  No
+ * cudaMalloc, cudaFree or allocating library routine is called. */
+int sgb_acoustic_backward_noalloc(const sgb_grid *grid, const sgb_acoustic_model *model,
+                                  const sgb_acquisition *acq, const sgb_bs_store *bs,
+                                  float *const ubuf[3], int32_t ucur, int32_t uprev, float *grad_vp,
+                                  sgb_stream_t stream);
 
 #ifdef __cplusplus
 }

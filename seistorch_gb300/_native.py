@@ -20,7 +20,7 @@ BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_NAME = "libseistorch_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 SOURCES = ["acoustic.cu", "acoustic_stream.cu", "acoustic_stream_fwd.cu", "acoustic_stream_bwd.cu",
-           "elastic.cu", "capi.cu"]
+           "elastic.cu", "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -122,6 +122,9 @@ SIGNATURES = {
     "sgb_acoustic_backward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel),
                                              ctypes.POINTER(Acquisition), ctypes.POINTER(BsStore), PTR3,
                                              c_i32, c_i32, PTR3, c_ptr, c_ptr, c_ptr]),
+    "sgb_acoustic_backward_noalloc": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel),
+                                                     ctypes.POINTER(Acquisition), ctypes.POINTER(BsStore), PTR3,
+                                                     c_i32, c_i32, c_ptr, c_ptr]),
     "sgb_elastic_coefficients": (ctypes.c_int, [ctypes.POINTER(Grid), c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                                                 c_ptr]),
     "sgb_elastic_step": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ElasticModel), c_ptr * 5,

@@ -155,6 +155,7 @@ const char* sgb_status_string(int s) {
     case SGB_ERR_UNSUPPORTED: return "unsupported option";
     case SGB_ERR_NONFINITE: return "non-finite values in the records";
     case SGB_ERR_CAPACITY: return "too many sources inside one tile";
+    case SGB_ERR_SCRATCH: return "problem larger than the fixed scratch of the allocation-free entry point";
   }
   return "unknown status";
 }
