@@ -43,6 +43,7 @@ METRIC = "Gpts/s fwd+adjoint"
 # algorithmic bytes per shot per padded point per time step (fp32)
 BYTES_FWD = 12          # read U_n, U_{n-1}; write U_{n+1}
 BYTES_BWD = 32          # reconstruction 12 + adjoint 12 + gradient accumulate 8
+CPU_SAMPLE_STEPS = 200  # time steps per shot of the CPU sample (about 10 s of work per process)
 BYTES_COEF = 8          # (g, k) planes, read once per point per step, shared by the shots
 
 
@@ -155,7 +156,7 @@ def run_reference(args):
     d = fd2d.pml_profile_2d(vp_init.shape, WIDTH).astype(np.float32)
     wav = fd2d.ricker(FM, DT, NT, delay=int(1.2 / FM / DT))
     sources, receivers = acquisition_lists()
-    nsteps = 60
+    nsteps = CPU_SAMPLE_STEPS
     vals = []
     for _ in range(args.warmup if args.warmup < 1 else 1):
         cpu_baseline(vp_init, d, wav, sources, receivers, nsteps=5)
@@ -193,8 +194,9 @@ def main():
     import torch
     import torch.distributed as dist
 
-    from oracle import fd2d  # checker-side generator of the damping profile only
     from seistorch_gb300 import _native, engine
+    from seistorch_gb300.pml import generate_pml_coefficients_2d
+    from seistorch_gb300.utils import ricker_wave
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -208,8 +210,8 @@ def main():
     NT, NSHOTS = args.nt, args.shots
     vp_true, vp_init = make_models(seed=0)
     nz, nx = vp_true.shape
-    d = fd2d.pml_profile_2d((nz, nx), WIDTH).astype(np.float32)
-    wav = fd2d.ricker(FM, DT, NT, delay=int(1.2 / FM / DT))
+    d = generate_pml_coefficients_2d((nz, nx), WIDTH).to(torch.float32).numpy()
+    wav = ricker_wave(FM, DT, NT, delay=int(1.2 / FM / DT), dtype="numpy")
     sources, receivers = acquisition_lists()
     sources, receivers = sources[:NSHOTS], receivers[:NSHOTS]
     ckpt = engine.default_ckpt_every(NT)
@@ -274,7 +276,7 @@ def main():
     fwd_bytes = NSHOTS * npts * BYTES_FWD + npts * BYTES_COEF
     peak, peak_kind = measured_peaks()
     achieved = bwd_bytes / (bwd_launch_ms * 1e-3) / 1e9
-    traffic = profile_traffic().get("acoustic_bwd_kernel_per_launch_bytes")
+    traffic = profile_traffic().get("acoustic_bwd_tile_kernel_per_launch_bytes")
     line = {
         "metric": METRIC, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -296,7 +298,7 @@ def main():
     if not args.no_e2e:
         line["e2e"] = e2e_through_api(args, dev, vp_init, obs.cpu(), wav, sources, receivers, world)
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(vp_init, d, wav, sources, receivers, nsteps=60)
+        line["cpu_baseline"] = cpu_baseline(vp_init, d, wav, sources, receivers, nsteps=CPU_SAMPLE_STEPS)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
