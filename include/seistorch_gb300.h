@@ -185,6 +185,132 @@ int sgb_acoustic_backward_noalloc(const sgb_grid *grid, const sgb_acoustic_model
                                   float *const ubuf[3], int32_t ucur, int32_t uprev, float *grad_vp,
                                   sgb_stream_t stream);
 
+/* ------------------------------------------------------ uneven batch --- */
+
+/* One grid of an uneven batch: its own shape and shots (grid), PML model,
+ * acquisition (its own nt: trace lengths may differ between groups) and
+ * three [nshots][nz][pitch] field buffers.  Every group must use the same
+ * spatial order.  No counterpart in the reference, which runs one grid per
+ * process (seistorch_dist.py:79-303); this is the batch-descriptor launch of
+ * its hot path. */
+typedef struct {
+  sgb_grid grid;
+  sgb_acoustic_model model;
+  sgb_acquisition acq;
+  float *buf[3];
+  float *illum; /* nullable */
+} sgb_batch_group;
+
+#define SGB_MAX_BATCH_GROUPS 8
+
+/* Time loops of up to SGB_MAX_BATCH_GROUPS grids, one persistent launch per
+ * step covering the tiles of every group still running (a group stops after
+ * its own nt steps).  Buffers start from zero here.  cur_out / prev_out
+ * (host arrays [ngroups]) name each group's buffers holding U_nt and
+ * U_{nt-1}. */
+int sgb_acoustic_batch_forward(const sgb_batch_group *groups, int32_t ngroups, int32_t *cur_out,
+                               int32_t *prev_out, sgb_stream_t stream);
+
+/* The same loop recorded once as a CUDA graph (zeroing of the buffers, one
+ * kernel node per step) for replay with sgb_plan_launch; replays reuse the
+ * descriptors' pointers, so the buffers and tables must stay allocated and
+ * in place until sgb_plan_destroy.  Records the variant current at creation
+ * (sgb_set_stream_config).  cur_out / prev_out as above. */
+typedef struct sgb_plan_st *sgb_plan;
+int sgb_acoustic_batch_plan(const sgb_batch_group *groups, int32_t ngroups, int32_t *cur_out,
+                            int32_t *prev_out, sgb_plan *plan_out);
+int sgb_plan_launch(sgb_plan plan, sgb_stream_t stream);
+int sgb_plan_destroy(sgb_plan plan);
+
+/* ----------------------------------------------------------- elastic --- */
+
+/* Field order of the elastic state, as Wavefield('elastic') lists it
+ * (eqconfigure.py:45-127): vx, vz, txx, tzz, txz. */
+enum { SGB_VX = 0, SGB_VZ = 1, SGB_TXX = 2, SGB_TZZ = 3, SGB_TXZ = 4, SGB_ELASTIC_FIELDS = 5 };
+
+/* Isotropic elastic velocity-stress model (elastic.py:7-37).  coef holds
+ * six planes [q | e | pa | la | ma | bv] from sgb_elastic_coefficients, with
+ * c = dt d / 2, lambda = rho (vp^2 - 2 vs^2), mu = rho vs^2:
+ *   q = (1 - c) / (1 + c),  e = dt / (h (1 + c)),
+ *   pa = e (lambda + 2 mu),  la = e lambda,  ma = e mu,  bv = e / rho.
+ * One step (Dx-/Dz- backward, Dx+/Dz+ forward one-cell differences with the
+ * first / last index zero, equations2d/utils.py:3-48):
+ *   txx' = q txx + pa Dx- vx + la Dz+ vz,  tzz' = q tzz + pa Dz+ vz + la Dx- vx,
+ *   txz' = q txz + ma (Dx+ vz + Dz- vx),
+ *   vx'  = q vx + bv (Dx+ txx' + Dz+ txz'),  vz' = q vz + bv (Dx- txz' + Dz- tzz'). */
+typedef struct {
+  int32_t multiple;  /* free surface (no top absorbing layer)           */
+  const float *coef; /* [6][nz][pitch]                                   */
+} sgb_elastic_model;
+
+/* Elastic source / receiver channels: src_fields is a bit mask over the
+ * field order above (source_type of the config; explosive = txx | tzz);
+ * rec_fields[ch] is the field that record channel ch samples (receiver_type,
+ * nch <= 4); illum_field is the field whose square the illumination sums
+ * (the last source type, rnn.py:204-205). */
+typedef struct {
+  int32_t src_fields;
+  int32_t rec_fields[4];
+  int32_t illum_field;
+} sgb_elastic_io;
+
+/* Coefficient planes for sgb_elastic_model.coef from vp, vs, rho and the PML
+ * damping d (all [nz][pitch]); computed in double precision, zero in the
+ * padding columns.  Replaces the per-step lambda / mu / (1+c)^-1 work of
+ * elastic.py:11-14. */
+int sgb_elastic_coefficients(const sgb_grid *grid, const float *vp, const float *vs, const float *rho,
+                             const float *damp, float *coef_out, sgb_stream_t stream);
+
+/* One step: out = step(in) (elastic._time_step, elastic.py:7-37).  in[5]
+ * and out[5] are [nshots][nz][pitch] fields in the order above; out must
+ * not alias in. */
+int sgb_elastic_step(const sgb_grid *grid, const sgb_elastic_model *model, const float *const in[5],
+                     float *const out[5], sgb_stream_t stream);
+
+/* Vector-Jacobian product of one step (autograd of elastic._time_step):
+ * given the step's input velocities vin[2] (vx, vz), its output stresses
+ * sout[3] (txx', tzz', txz') and gout[5] = dJ/d(outputs), writes
+ * gin[5] = dJ/d(inputs) and accumulates into grad_shot (three
+ * [nshots][nz][pitch] planes: the lambda, mu and buoyancy terms before the
+ * chain rule; sgb_elastic_gradient turns them into vp / vs / rho). */
+int sgb_elastic_step_vjp(const sgb_grid *grid, const sgb_elastic_model *model, const float *const vin[2],
+                         const float *const sout[3], const float *const gout[5], float *const gin[5],
+                         float *const grad_shot[3], sgb_stream_t stream);
+
+/* Whole elastic time loop (rnn.py:178-205): nt steps with source injection
+ * and receiver sampling fused into the step kernel.  buf[0..4] and
+ * buf[5..9] are two sets of five fields; set 0 holds the initial state
+ * (zeros for a cold start).  On return *cur_out (0 or 1) names the set that
+ * holds the final state.  bs (nullable): the ring (width 1) of all five
+ * fields is saved every step ([nt][5][nshots][ring_size]) and full states
+ * every ckpt_every steps ([nt / ckpt_every][5][nshots][nz][pitch]). */
+int sgb_elastic_forward(const sgb_grid *grid, const sgb_elastic_model *model, const sgb_acquisition *acq,
+                        const sgb_elastic_io *io, float *const buf[10], float *illum, const sgb_bs_store *bs,
+                        int32_t *cur_out, sgb_stream_t stream);
+
+/* Adjoint of sgb_elastic_forward: boundary-saving reconstruction of the
+ * forward state inside the interior box, the exact discrete adjoint of the
+ * step and the lambda / mu / buoyancy gradient terms, one fused kernel per
+ * step.  Replaces the reconstruct-then-replay of checkpoint.py:108-230.
+ *   sbuf[10], scur: the state sets as left by sgb_elastic_forward;
+ *   abuf[10]: adjoint scratch (zeroed here);
+ *   acq->records: dJ/d(records) [nt][nrec][nch];
+ *   grad_shot[3]: [nshots][nz][pitch] accumulators (zeroed here);
+ *   vp, vs, rho: the model; grad_out[3]: dJ/dvp, dJ/dvs, dJ/drho
+ *   ([nz][pitch] each, may be NULL to skip), inside the box, 0 outside. */
+int sgb_elastic_backward(const sgb_grid *grid, const sgb_elastic_model *model, const sgb_acquisition *acq,
+                         const sgb_elastic_io *io, const sgb_bs_store *bs, float *const sbuf[10], int32_t scur,
+                         float *const abuf[10], float *const grad_shot[3], const float *vp, const float *vs,
+                         const float *rho, float *const grad_out[3], sgb_stream_t stream);
+
+/* Chain rule of the elastic gradient terms: sums grad_shot[3] over shots and
+ * maps the lambda / mu / buoyancy terms to dJ/dvp, dJ/dvs, dJ/drho
+ * (grad_out entries may be NULL).  box != 0 restricts the result to the
+ * interior box of bs (0 outside), as sgb_elastic_backward does. */
+int sgb_elastic_gradient(const sgb_grid *grid, const sgb_elastic_model *model, const float *const grad_shot[3],
+                         const float *vp, const float *vs, const float *rho, const sgb_bs_store *bs, int32_t box,
+                         float *const grad_out[3], sgb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

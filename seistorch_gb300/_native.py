@@ -20,7 +20,7 @@ BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_NAME = "libseistorch_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 SOURCES = ["acoustic.cu", "acoustic_stream.cu", "acoustic_stream_fwd.cu", "acoustic_stream_bwd.cu",
-           "elastic.cu", "capi.cu", "noalloc.cu"]
+           "elastic.cu", "capi.cu", "capi_elastic.cu", "capi_batch.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -97,10 +97,22 @@ class BsStore(ctypes.Structure):
 
 
 class ElasticModel(ctypes.Structure):
-    _fields_ = [("coef", c_ptr), ("multiple", c_i32), ("src_mask", c_i32), ("rec_fields", c_i32 * 4)]
+    _fields_ = [("multiple", c_i32), ("coef", c_ptr)]
+
+
+class ElasticIO(ctypes.Structure):
+    _fields_ = [("src_fields", c_i32), ("rec_fields", c_i32 * 4), ("illum_field", c_i32)]
+
+
+class BatchGroup(ctypes.Structure):
+    _fields_ = [("grid", Grid), ("model", AcousticModel), ("acq", Acquisition), ("buf", c_ptr * 3),
+                ("illum", c_ptr)]
 
 
 PTR3 = c_ptr * 3
+PTR2 = c_ptr * 2
+PTR5 = c_ptr * 5
+PTR10 = c_ptr * 10
 
 # name -> (restype, argtypes)
 SIGNATURES = {
@@ -125,16 +137,27 @@ SIGNATURES = {
     "sgb_acoustic_backward_noalloc": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel),
                                                      ctypes.POINTER(Acquisition), ctypes.POINTER(BsStore), PTR3,
                                                      c_i32, c_i32, c_ptr, c_ptr]),
+    "sgb_acoustic_batch_forward": (ctypes.c_int, [ctypes.POINTER(BatchGroup), c_i32, ctypes.POINTER(c_i32),
+                                                  ctypes.POINTER(c_i32), c_ptr]),
+    "sgb_acoustic_batch_plan": (ctypes.c_int, [ctypes.POINTER(BatchGroup), c_i32, ctypes.POINTER(c_i32),
+                                               ctypes.POINTER(c_i32), ctypes.POINTER(c_ptr)]),
+    "sgb_plan_launch": (ctypes.c_int, [c_ptr, c_ptr]),
+    "sgb_plan_destroy": (ctypes.c_int, [c_ptr]),
     "sgb_elastic_coefficients": (ctypes.c_int, [ctypes.POINTER(Grid), c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                                                 c_ptr]),
-    "sgb_elastic_step": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ElasticModel), c_ptr * 5,
-                                        c_ptr * 5, c_ptr]),
+    "sgb_elastic_step": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ElasticModel), PTR5, PTR5,
+                                        c_ptr]),
+    "sgb_elastic_step_vjp": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ElasticModel), PTR2, PTR3,
+                                            PTR5, PTR5, PTR3, c_ptr]),
     "sgb_elastic_forward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ElasticModel),
-                                           ctypes.POINTER(Acquisition), c_ptr * 10, c_ptr,
-                                           ctypes.POINTER(BsStore), ctypes.POINTER(c_i32), c_ptr]),
+                                           ctypes.POINTER(Acquisition), ctypes.POINTER(ElasticIO), PTR10,
+                                           c_ptr, ctypes.POINTER(BsStore), ctypes.POINTER(c_i32), c_ptr]),
     "sgb_elastic_backward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ElasticModel),
-                                            ctypes.POINTER(Acquisition), ctypes.POINTER(BsStore), c_ptr * 10,
-                                            c_i32, c_ptr * 10, c_ptr, c_ptr, c_ptr]),
+                                            ctypes.POINTER(Acquisition), ctypes.POINTER(ElasticIO),
+                                            ctypes.POINTER(BsStore), PTR10, c_i32, PTR10, PTR3, c_ptr, c_ptr,
+                                            c_ptr, PTR3, c_ptr]),
+    "sgb_elastic_gradient": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ElasticModel), PTR3, c_ptr,
+                                            c_ptr, c_ptr, ctypes.POINTER(BsStore), c_i32, PTR3, c_ptr]),
 }
 
 _LIB = None

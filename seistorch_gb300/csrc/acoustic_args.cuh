@@ -1,6 +1,8 @@
 // Kernel argument blocks of the acoustic kernels (filled by capi.cu).
 #pragma once
 
+#include <cuda.h>
+
 #include "sgb_common.cuh"
 
 namespace sgb {
@@ -82,6 +84,18 @@ struct AcStreamArgs {
   float* __restrict__ ring_out;
   Ring ring;
   int* status;
+};
+
+// Forward steps of up to MAXG grids in one launch (tiles numbered group
+// after group from tile0[g]); MAXG = 1 is the single-grid path.
+constexpr int MAX_BATCH_GROUPS = 8;
+template <int MAXG>
+struct AcFwdBatch {
+  CUtensorMap tm_u[MAXG];
+  CUtensorMap tm_um[MAXG];
+  AcStreamArgs g[MAXG];
+  int tile0[MAXG + 1];
+  int ngroups;
 };
 
 // Fused adjoint step (PML) of the TMA tile pipeline; the adjoint is carried

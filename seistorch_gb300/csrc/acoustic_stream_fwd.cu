@@ -18,11 +18,42 @@ struct FwdTileLayout {
   static constexpr uint32_t TX_BYTES = (UROWS * UW + (PT ? TZ * TX : 0)) * 4;
 };
 
-template <int R, int TZ, int NWP, int S, bool PT>
-__global__ void __launch_bounds__(32 * NWP) acoustic_fwd_tile_kernel(
-    const __grid_constant__ CUtensorMap tm_u,   // U_n [nshots][nz][nx], box {W, TZ+2R, 1}
-    const __grid_constant__ CUtensorMap tm_um,  // U_{n-1} box {128, TZ, 1} (used when PT)
-    const AcStreamArgs a) {
+// Tile providers: the single-grid kernel takes its tensor maps and argument
+// block as separate parameters (the argument block stays in the constant
+// bank); the batch kernel covers every tile of up to MAXG grids (an uneven
+// batch: each group has its own shape, shots, buffers and step), tiles
+// numbered group after group from tile0[g].
+struct FwdOne {
+  const CUtensorMap* tu;
+  const CUtensorMap* tum;
+  AcStreamArgs a;
+  __device__ __forceinline__ int ntiles() const { return a.nshots * a.ntx * a.nzc; }
+  __device__ __forceinline__ int group(int) const { return 0; }
+  __device__ __forceinline__ int first(int) const { return 0; }
+  __device__ __forceinline__ const AcStreamArgs& args(int) const { return a; }
+  __device__ __forceinline__ const CUtensorMap* map_u(int) const { return tu; }
+  __device__ __forceinline__ const CUtensorMap* map_um(int) const { return tum; }
+};
+
+template <int MAXG>
+struct FwdMany {
+  const AcFwdBatch<MAXG>& B;
+  __device__ __forceinline__ int ntiles() const { return B.tile0[B.ngroups]; }
+  __device__ __forceinline__ int group(int t) const {
+    int gi = 0;
+    while (gi + 1 < B.ngroups && t >= B.tile0[gi + 1]) ++gi;
+    return gi;
+  }
+  __device__ __forceinline__ int first(int gi) const { return B.tile0[gi]; }
+  __device__ __forceinline__ const AcStreamArgs& args(int gi) const { return B.g[gi]; }
+  __device__ __forceinline__ const CUtensorMap* map_u(int gi) const { return &B.tm_u[gi]; }
+  __device__ __forceinline__ const CUtensorMap* map_um(int gi) const { return &B.tm_um[gi]; }
+};
+
+// per group: map_u = U_n [nshots][nz][nx], box {W, TZ+2R, 1};
+//            map_um = U_{n-1}, box {128, TZ, 1} (used when PT)
+template <int R, int TZ, int NWP, int S, bool PT, class P>
+__device__ __forceinline__ void fwd_tiles(const P& prov) {
   using Lay = FwdTileLayout<R, TZ, S, PT>;
   constexpr int RPW = TZ / NWP;
   constexpr int UW = Lay::UW, LO = Row<R>::LO;
@@ -31,15 +62,17 @@ __global__ void __launch_bounds__(32 * NWP) acoustic_fwd_tile_kernel(
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * Lay::STAGE);
   __shared__ int s_abort;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int ntiles = a.nshots * a.ntx * a.nzc;
+  const int ntiles = prov.ntiles();
   const int G = gridDim.x;
 
   auto issue = [&](int t, int stage) {
-    const Tile g = tile_geom(t, a.nshots, a.ntx, TZ);
+    const int gi = prov.group(t);
+    const AcStreamArgs& a = prov.args(gi);
+    const Tile g = tile_geom(t - prov.first(gi), a.nshots, a.ntx, TZ);
     fence_proxy_async_smem();
     mbar_arrive_expect_tx(&bars[stage], Lay::TX_BYTES);
-    tma_load_3d(smem + stage * Lay::STAGE, &tm_u, g.x0 - LO, g.z0 - R, g.b, &bars[stage]);
-    if (PT) tma_load_3d(smem + stage * Lay::STAGE + Lay::UF, &tm_um, g.x0, g.z0, g.b, &bars[stage]);
+    tma_load_3d(smem + stage * Lay::STAGE, prov.map_u(gi), g.x0 - LO, g.z0 - R, g.b, &bars[stage]);
+    if (PT) tma_load_3d(smem + stage * Lay::STAGE + Lay::UF, prov.map_um(gi), g.x0, g.z0, g.b, &bars[stage]);
   };
   if (tid == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
@@ -52,7 +85,9 @@ __global__ void __launch_bounds__(32 * NWP) acoustic_fwd_tile_kernel(
   int k = 0;
   for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
     const int stage = k % S;
-    const Tile g = tile_geom(t, a.nshots, a.ntx, TZ);
+    const int gi = prov.group(t);
+    const AcStreamArgs& a = prov.args(gi);
+    const Tile g = tile_geom(t - prov.first(gi), a.nshots, a.ntx, TZ);
     const int x = g.x0 + 4 * lane;
     const bool xin = x < a.nx;
     const int zw = g.z0 + wid * RPW;  // first row of this warp
@@ -149,6 +184,18 @@ __global__ void __launch_bounds__(32 * NWP) acoustic_fwd_tile_kernel(
       if ((int)blockIdx.x + q * G < ntiles) mbar_wait(&bars[q % S], (q / S) & 1, nullptr);
 }
 
+template <int R, int TZ, int NWP, int S, bool PT>
+__global__ void __launch_bounds__(32 * NWP) acoustic_fwd_tile_kernel(const __grid_constant__ CUtensorMap tm_u,
+                                                                     const __grid_constant__ CUtensorMap tm_um,
+                                                                     const AcStreamArgs a) {
+  fwd_tiles<R, TZ, NWP, S, PT>(FwdOne{&tm_u, &tm_um, a});
+}
+
+template <int R, int TZ, int NWP, int S, bool PT, int MAXG>
+__global__ void __launch_bounds__(32 * NWP) acoustic_fwd_batch_kernel(const __grid_constant__ AcFwdBatch<MAXG> B) {
+  fwd_tiles<R, TZ, NWP, S, PT>(FwdMany<MAXG>{B});
+}
+
 // ------------------------------------------------------------- launch ---
 
 struct FwdCfg {
@@ -156,31 +203,60 @@ struct FwdCfg {
 };
 static const FwdCfg FWD_TILE_CFGS[] = {{16, 4, 3}, {16, 4, 3}, {8, 4, 4}, {32, 8, 2}, {16, 4, 2}, {8, 4, 3}};
 
-template <int R, int TZ, int NWP, int S, bool PT>
-static cudaError_t fwd_tile_t(const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s) {
+// Launches the variant on batch b; with s == nullptr and prepare_only it
+// only sets the kernel's shared-memory attribute (done once per variant, and
+// before any stream capture).
+template <int R, int TZ, int NWP, int S, bool PT, int MAXG>
+static cudaError_t fwd_tile_t(const AcFwdBatch<MAXG>& b, cudaStream_t s, bool prepare_only) {
   using Lay = FwdTileLayout<R, TZ, S, PT>;
   const size_t smem = Lay::BYTES + 128;  // + alignment slack
-  auto kern = acoustic_fwd_tile_kernel<R, TZ, NWP, S, PT>;
   static int blocks = 0;
-  if (blocks == 0) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    blocks = resident_blocks(kern, 32 * NWP, smem);
+  if constexpr (MAXG == 1) {
+    auto kern = acoustic_fwd_tile_kernel<R, TZ, NWP, S, PT>;
+    if (blocks == 0) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      blocks = resident_blocks(kern, 32 * NWP, smem);
+    }
+    if (prepare_only) return cudaSuccess;
+    const int tiles = b.tile0[b.ngroups];
+    if (tiles <= 0) return cudaSuccess;
+    kern<<<(unsigned)(tiles < blocks ? tiles : blocks), 32 * NWP, smem, s>>>(b.tm_u[0], b.tm_um[0], b.g[0]);
+  } else {
+    auto kern = acoustic_fwd_batch_kernel<R, TZ, NWP, S, PT, MAXG>;
+    if (blocks == 0) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      blocks = resident_blocks(kern, 32 * NWP, smem);
+    }
+    if (prepare_only) return cudaSuccess;
+    const int tiles = b.tile0[b.ngroups];
+    if (tiles <= 0) return cudaSuccess;
+    kern<<<(unsigned)(tiles < blocks ? tiles : blocks), 32 * NWP, smem, s>>>(b);
   }
-  const int tiles = a.nshots * a.ntx * a.nzc;
-  kern<<<(unsigned)(tiles < blocks ? tiles : blocks), 32 * NWP, smem, s>>>(maps[0], maps[1], a);
   return cudaGetLastError();
 }
 
-template <int R>
-static cudaError_t fwd_tile_r(const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s) {
+template <int R, int MAXG>
+static cudaError_t fwd_tile_r(const AcFwdBatch<MAXG>& b, cudaStream_t s, bool prep) {
   switch (g_fwd_cfg) {
-    case 0: return fwd_tile_t<R, 16, 4, 3, false>(maps, a, s);
-    case 1: return fwd_tile_t<R, 16, 4, 3, true>(maps, a, s);
-    case 2: return fwd_tile_t<R, 8, 4, 4, true>(maps, a, s);
-    case 3: return fwd_tile_t<R, 32, 8, 2, true>(maps, a, s);
-    case 4: return fwd_tile_t<R, 16, 4, 2, true>(maps, a, s);
-    case 5: return fwd_tile_t<R, 8, 4, 3, true>(maps, a, s);
+    case 0: return fwd_tile_t<R, 16, 4, 3, false>(b, s, prep);
+    case 1: return fwd_tile_t<R, 16, 4, 3, true>(b, s, prep);
+    case 2: return fwd_tile_t<R, 8, 4, 4, true>(b, s, prep);
+    case 3: return fwd_tile_t<R, 32, 8, 2, true>(b, s, prep);
+    case 4: return fwd_tile_t<R, 16, 4, 2, true>(b, s, prep);
+    case 5: return fwd_tile_t<R, 8, 4, 3, true>(b, s, prep);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int MAXG>
+static cudaError_t fwd_dispatch(int R, const AcFwdBatch<MAXG>& b, cudaStream_t s, bool prep) {
+  switch (R) {
+    case 1: return fwd_tile_r<1>(b, s, prep);
+    case 2: return fwd_tile_r<2>(b, s, prep);
+    case 3: return fwd_tile_r<3>(b, s, prep);
+    case 4: return fwd_tile_r<4>(b, s, prep);
   }
   return cudaErrorInvalidValue;
 }
@@ -189,13 +265,25 @@ int fwd_tile_rows() { return FWD_TILE_CFGS[g_fwd_cfg].tz; }
 int stencil_box_width(int R) { return (R % 2 == 0) ? TX + 8 : TX + 16; }
 
 cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s) {
-  switch (R) {
-    case 1: return fwd_tile_r<1>(maps, a, s);
-    case 2: return fwd_tile_r<2>(maps, a, s);
-    case 3: return fwd_tile_r<3>(maps, a, s);
-    case 4: return fwd_tile_r<4>(maps, a, s);
-  }
-  return cudaErrorInvalidValue;
+  AcFwdBatch<1> b;
+  b.tm_u[0] = maps[0];
+  b.tm_um[0] = maps[1];
+  b.g[0] = a;
+  b.ngroups = 1;
+  b.tile0[0] = 0;
+  b.tile0[1] = a.nshots * a.ntx * a.nzc;
+  return fwd_dispatch<1>(R, b, s, false);
+}
+
+cudaError_t launch_acoustic_fwd_batch(int R, const AcFwdBatch<MAX_BATCH_GROUPS>& b, cudaStream_t s) {
+  return fwd_dispatch<MAX_BATCH_GROUPS>(R, b, s, false);
+}
+
+cudaError_t prepare_acoustic_fwd_batch(int R) {
+  AcFwdBatch<MAX_BATCH_GROUPS> b;
+  b.ngroups = 0;
+  b.tile0[0] = 0;
+  return fwd_dispatch<MAX_BATCH_GROUPS>(R, b, nullptr, true);
 }
 
 }  // namespace sgb

@@ -5,6 +5,7 @@
 
 #include "sgb_common.cuh"
 #include "acoustic_args.cuh"
+#include "capi_util.cuh"
 #include "tma.cuh"
 
 namespace sgb {
@@ -19,7 +20,7 @@ int set_cuda_error(cudaError_t e) {
 // Device status word (bit flags set by kernels, e.g. DEV_ERR_CAPACITY).
 __device__ int g_dev_status;
 
-static int* status_ptr() {
+int* status_ptr() {
   static int* p = nullptr;
   static int dev = -1;
   int cur = 0;
@@ -78,15 +79,6 @@ using namespace sgb;
 
 namespace {
 
-bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
-
-int check_grid(const sgb_grid* g) {
-  if (g == nullptr) return SGB_ERR_ARG;
-  if (g->nz <= 0 || g->nx <= 0 || g->nshots <= 0 || g->pitch < g->nx) return SGB_ERR_SHAPE;
-  if (g->pitch % 4 != 0) return SGB_ERR_ALIGN;
-  if (!(g->dt > 0.f) || !(g->h > 0.f)) return SGB_ERR_ARG;
-  return SGB_OK;
-}
 
 int check_model(const sgb_grid* g, const sgb_acoustic_model* m) {
   if (m == nullptr || m->coef == nullptr) return SGB_ERR_ARG;
@@ -126,18 +118,6 @@ AcStepArgs base_step_args(const sgb_grid* g, const sgb_acoustic_model* m) {
   return a;
 }
 
-int check_acq(const sgb_grid* g, const sgb_acquisition* q) {
-  if (q == nullptr) return SGB_ERR_ARG;
-  if (q->nt <= 0) return SGB_ERR_ARG;
-  if (q->nsrc > 0 && (q->src_ptr == nullptr || q->src_z == nullptr || q->src_x == nullptr ||
-                      q->src_wrow == nullptr || q->wavelet == nullptr))
-    return SGB_ERR_ARG;
-  if (q->records != nullptr && (q->rec_row_ptr == nullptr || q->rec_x == nullptr || q->rec_col == nullptr))
-    return SGB_ERR_ARG;
-  if (q->records != nullptr && q->nch <= 0) return SGB_ERR_ARG;
-  (void)g;
-  return SGB_OK;
-}
 
 }  // namespace
 

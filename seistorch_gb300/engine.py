@@ -318,3 +318,83 @@ def acoustic_loop(vp, prop, damp, acq, illumination=False, ckpt_every=0):
 def default_ckpt_every(nt):
     """Checkpoint spacing of the reconstruction: about sqrt(nt), at most 256."""
     return int(min(256, max(16, round(math.sqrt(max(nt, 1))))))
+
+
+class UnevenBatch:
+    """Acoustic PML time loops of several grids (different shapes, shots and
+    trace lengths) run together: one persistent launch per step covers the
+    tiles of every grid still running (``sgb_acoustic_batch_forward``), and
+    ``plan()`` records the whole loop once as a CUDA graph that ``replay()``
+    relaunches with a single call.
+
+    groups: list of (AcousticPropagator, vp (nz, nx), damping (nz, nx),
+    Acquisition); every propagator must use the same spatial order.
+    """
+
+    MAX_GROUPS = 8
+
+    def __init__(self, groups):
+        if not 1 <= len(groups) <= self.MAX_GROUPS:
+            raise ValueError(f"an uneven batch holds 1 to {self.MAX_GROUPS} grids")
+        orders = {p.order for p, _, _, _ in groups}
+        if len(orders) != 1:
+            raise ValueError("every grid of an uneven batch must use the same spatial order")
+        self.groups = groups
+        self._keep = []
+        structs = []
+        self.records = []
+        self.buffers = []
+        for prop, vp, damp, acq in groups:
+            require_cuda(vp, "UnevenBatch")
+            if prop.boundary != BOUNDARY_PML:
+                raise NotImplementedError("the uneven batch covers the PML acoustic equation")
+            m, keep = prop.model(vp, damp)
+            B = acq.nshots
+            buf = [torch.zeros(B, prop.nz, prop.pitch, dtype=torch.float32, device=vp.device) for _ in range(3)]
+            rec = torch.zeros(acq.nt, max(acq.nrec, 1), 1, dtype=torch.float32, device=vp.device)
+            q = acq.struct(rec if acq.nrec else None, 1)
+            structs.append(N.BatchGroup(prop.grid(B), m, q, N.PTR3(*[b.data_ptr() for b in buf]), None))
+            self._keep.append((keep, buf, rec, acq))
+            self.records.append(rec)
+            self.buffers.append(buf)
+        self._arr = (N.BatchGroup * len(structs))(*structs)
+        self.cur = (ctypes.c_int32 * len(structs))()
+        self.prev = (ctypes.c_int32 * len(structs))()
+        self._plan = None
+
+    def points(self):
+        """Grid-point updates of one run: sum over grids of shots * nz * nx * nt."""
+        return sum(acq.nshots * p.nz * p.nx * acq.nt for p, _, _, acq in self.groups)
+
+    def run(self):
+        N.call("sgb_acoustic_batch_forward", self._arr, len(self.groups), self.cur, self.prev,
+               N.stream_handle())
+        return self.result()
+
+    def plan(self):
+        if self._plan is None:
+            h = ctypes.c_void_p(None)
+            N.call("sgb_acoustic_batch_plan", self._arr, len(self.groups), self.cur, self.prev, ctypes.byref(h))
+            self._plan = h
+        return self
+
+    def replay(self):
+        if self._plan is None:
+            self.plan()
+        N.call("sgb_plan_launch", self._plan, N.stream_handle())
+        return self.result()
+
+    def result(self):
+        """Per grid: records (nt, nrec, 1)."""
+        return [r[:, :acq.nrec] for r, (_, _, _, acq) in zip(self.records, self.groups)]
+
+    def close(self):
+        if self._plan is not None:
+            N.load().sgb_plan_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

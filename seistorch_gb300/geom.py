@@ -41,8 +41,9 @@ class WaveGeometryFreeForm(torch.nn.Module):
             self.bwidth = 50  # fixed for HABC (geom.py:62-65)
         self.multiple = bool(g.get("multiple", False))
         self.boundary_saving = bool(g.get("boundary_saving", True))
-        self.source_type = list(g.get("source_type") or ["h1"])
-        self.receiver_type = list(g.get("receiver_type") or ["h1"])
+        elastic = kwargs["equation"] == "elastic"
+        self.source_type = list(g.get("source_type") or (["txx", "tzz"] if elastic else ["h1"]))
+        self.receiver_type = list(g.get("receiver_type") or (["vx", "vz"] if elastic else ["h1"]))
         self.source_illumination = bool(g.get("source_illumination", False))
         self.spatial_order = int(g.get("spatial_order", 2))
         self.ckpt_every = int(g.get("ckpt_every", 0) or 0)

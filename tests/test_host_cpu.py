@@ -179,3 +179,35 @@ def test_gpu_entry_points_fail_loudly_without_cuda():
         pytest.skip("a GPU is present")
     with pytest.raises(RuntimeError, match="CUDA"):
         engine.require_cuda(None, "x")
+
+
+def test_elastic_io_maps_config_names_to_fields():
+    from seistorch_gb300 import elastic_engine
+    io, nch = elastic_engine.make_io(["txx", "tzz"], ["vx", "vz"])
+    assert io.src_fields == (1 << 2) | (1 << 3) and nch == 2
+    assert list(io.rec_fields)[:2] == [0, 1] and io.illum_field == 3
+    io, nch = elastic_engine.make_io(["vz"], ["txz"])
+    assert io.src_fields == 2 and list(io.rec_fields)[:1] == [4] and nch == 1
+    with pytest.raises(ValueError):
+        elastic_engine.make_io(["h1"], ["vx"])
+    with pytest.raises(ValueError):
+        elastic_engine.make_io(["txx"], ["vx", "vz", "txx", "tzz", "txz"])
+
+
+def test_elastic_calls_validate_before_touching_the_gpu(lib):
+    from seistorch_gb300 import _native as N
+    g = N.Grid(64, 64, 64, 1, 0.0005, 5.0)
+    fields = N.PTR5(*([16] * 5))
+    assert lib.sgb_elastic_step(ctypes.byref(g), None, fields, fields, None) == 1
+    m = N.ElasticModel(0, ctypes.c_void_p(20))
+    assert lib.sgb_elastic_step(ctypes.byref(g), ctypes.byref(m), fields, fields, None) == 3
+    m = N.ElasticModel(0, ctypes.c_void_p(16))
+    assert lib.sgb_elastic_step(ctypes.byref(g), ctypes.byref(m), N.PTR5(16, 16, 0, 16, 16), fields, None) == 1
+    bad = N.Grid(64, 66, 66, 1, 0.0005, 5.0)
+    assert lib.sgb_elastic_step(ctypes.byref(bad), ctypes.byref(m), fields, fields, None) == 3
+    io = N.ElasticIO(1 << 5, (ctypes.c_int32 * 4)(0, 1, 0, 0), 0)
+    q = N.Acquisition()
+    q.nt = 10
+    cur = ctypes.c_int32(0)
+    assert lib.sgb_elastic_forward(ctypes.byref(g), ctypes.byref(m), ctypes.byref(q), ctypes.byref(io),
+                                   N.PTR10(*([16] * 10)), None, None, ctypes.byref(cur), None) == 1
