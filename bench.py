@@ -187,7 +187,15 @@ def main():
     ap.add_argument("--shots", type=int, default=NSHOTS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="acoustic_gradient",
+                    choices=["acoustic_gradient", "elastic_gradient", "uneven_forward"],
+                    help="acoustic_gradient (default, the headline line); elastic_gradient: 300x800 + 50 PML "
+                         "elastic forward+adjoint; uneven_forward: 4 grid sizes x 64 shots in one launch per step")
     args = ap.parse_args()
+    if args.workload == "elastic_gradient":
+        return bench_elastic(args)
+    if args.workload == "uneven_forward":
+        return bench_uneven(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -357,6 +365,213 @@ def e2e_through_api(args, dev, vp_init, obs_host, wav, sources, receivers, world
     return {"value": len(sources) * nz * nx * NT * world / wall / 1e9, "unit": "Gpts/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(grad_host.numel() * 4 + 4),
             "ms_per_step": wall * 1e3, "api": "build_model -> WaveRNN.forward -> loss.backward"}
+
+
+# ------------------------------------------------------------ elastic ---
+# 300 x 800 interior + 50-cell PML (400 x 900), dx = 5 m, dt = 0.5 ms, 4000
+# steps; vp 2000-5000 m/s layered with a seeded dipping fault, vs = vp/1.73,
+# rho = 310 vp^0.25; 32 explosive shots (txx + tzz) on row 2, 12 Hz Ricker,
+# vx / vz receivers on every interior cell of row 2.  One step = forward +
+# L2 residual against data from the true model + fused adjoint + dJ/d(vp,
+# vs, rho).
+EL_NZI, EL_NXI, EL_W, EL_DT, EL_H, EL_NT, EL_FM, EL_SHOTS = 300, 800, 50, 0.0005, 5.0, 4000, 12.0, 32
+EL_BYTES_FWD = 40    # read 5 fields, write 5 fields
+EL_BYTES_REV = 104   # read s, a (10 fields) + 3 gradient terms, write s, a + 3 gradient terms
+EL_BYTES_COEF = 24   # 6 coefficient planes, shared by the shots
+
+
+def elastic_models(seed=0):
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    nl = 6
+    tops = np.sort(rng.choice(np.arange(20, EL_NZI - 20), nl - 1, replace=False))
+    vel = np.linspace(2000.0, 5000.0, nl) + rng.uniform(-150, 150, nl)
+    zz, xx = np.mgrid[0:EL_NZI, 0:EL_NXI]
+    x_f = EL_NXI * rng.uniform(0.35, 0.65)
+    throw = int(rng.integers(15, 40))
+    fault = (xx - x_f) > (zz - EL_NZI / 2) * 0.6  # dipping fault plane
+    depth = np.where(fault, zz - throw, zz)
+    layer = np.searchsorted(tops, depth, side="right")
+    vp = np.clip(vel[layer], 2000.0, 5000.0)
+    vp0 = gaussian_filter(vp, sigma=15)
+    pad = lambda m: np.pad(m, EL_W, mode="edge")
+    out = []
+    for v in (vp, vp0):
+        v = pad(v)
+        out.append({"vp": v, "vs": v / 1.73, "rho": 310.0 * v ** 0.25})
+    return out
+
+
+def bench_elastic(args):
+    import torch
+    from seistorch_gb300 import _native, elastic_engine, engine
+    from seistorch_gb300.pml import generate_pml_coefficients_2d
+    from seistorch_gb300.utils import ricker_wave
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm is timed on the acoustic "
+                          "gradient workload only"}))
+        return 0
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _native.load(build_if_missing=False)
+    nt = args.nt if args.nt != NT else EL_NT
+    shots = args.shots if args.shots != NSHOTS else EL_SHOTS
+    true_m, init_m = elastic_models()
+    nz, nx = true_m["vp"].shape
+    d = generate_pml_coefficients_2d((nz, nx), EL_W).to(torch.float32)
+    wav = ricker_wave(EL_FM, EL_DT, nt, delay=int(1.2 / EL_FM / EL_DT), dtype="numpy")
+    xs = np.linspace(0, EL_NXI - 1, shots).round().astype(int)
+    src = [[(EL_W + 2, EL_W + int(x))] for x in xs]
+    rec = [([EL_W + 2] * EL_NXI, list(range(EL_W, EL_W + EL_NXI)))] * shots
+    prop = elastic_engine.ElasticPropagator(nz, nx, EL_DT, EL_H, EL_W, False, dev)
+    acq = engine.Acquisition(nz, nx, src, rec, wav, dev)
+    io, nch = elastic_engine.make_io(["txx", "tzz"], ["vx", "vz"])
+    t = lambda a, rg=False: torch.tensor(a, dtype=torch.float32, device=dev, requires_grad=rg)
+    dd = d.to(dev)
+    ck = engine.default_ckpt_every(nt)
+    with torch.no_grad():
+        obs, _ = elastic_engine.elastic_records(t(true_m["vp"]), t(true_m["vs"]), t(true_m["rho"]), prop, dd,
+                                                acq, io, nch)
+    obs = obs.contiguous()
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def step(timing=None):
+        m = [t(init_m[k], True) for k in ("vp", "vs", "rho")]
+        e0, e1, e2 = ev(), ev(), ev()
+        e0.record(stream)
+        r, _ = elastic_engine.elastic_records(*m, prop, dd, acq, io, nch, False, ck)
+        e1.record(stream)
+        loss = ((r - obs) ** 2).sum()
+        loss.backward()
+        e2.record(stream)
+        if timing is not None:
+            timing.append((e0, e1, e2))
+        return loss
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    timing = []
+    with ClockSampler(0) as clocks:
+        t0, t1 = ev(), ev()
+        t0.record(stream)
+        for _ in range(args.steps):
+            step(timing)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    fwd_ms = float(np.median([a.elapsed_time(b) for a, b, _ in timing]))
+    rev_ms = float(np.median([b.elapsed_time(c) for _, b, c in timing]))
+    npts = nz * nx
+    rev_bytes = shots * npts * EL_BYTES_REV + npts * EL_BYTES_COEF
+    fwd_bytes = shots * npts * EL_BYTES_FWD + npts * EL_BYTES_COEF
+    peak, kind = measured_peaks()
+    rev_gbs = rev_bytes / (rev_ms / nt * 1e-3) / 1e9
+    fwd_gbs = fwd_bytes / (fwd_ms / nt * 1e-3) / 1e9
+    line = {"metric": "Gpts/s fwd+adjoint", "value": shots * npts * nt / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"elastic_l2_gradient_{EL_NZI}x{EL_NXI}_pml{EL_W}_nt{nt}_{shots}shots",
+                       "grid": [nz, nx], "shots": shots, "nt": nt, "ckpt_every": ck,
+                       "l2": "inputs larger than L2 (46 MB per field, 5 fields)"},
+            "shots_per_s": shots / (ms * 1e-3), "phases_ms": {"forward": fwd_ms, "adjoint": rev_ms},
+            "roofline": {"kernel": "elastic_bwd_kernel", "bound": "hbm", "achieved": rev_gbs, "peak": peak,
+                         "peak_kind": kind, "unit": "GB/s", "frac": rev_gbs / peak, "traffic": None,
+                         "bytes_per_launch": rev_bytes, "launch_ms": rev_ms / nt},
+            "roofline_forward": {"kernel": "elastic_fwd_kernel", "achieved": fwd_gbs, "frac": fwd_gbs / peak,
+                                 "unit": "GB/s", "launch_ms": fwd_ms / nt},
+            "gpu_launches": args.steps * (2 * nt + 2), "clocks": clocks.summary()}
+    print(json.dumps(line))
+    return 0
+
+
+# -------------------------------------------------------- uneven batch ---
+# 4 grid sizes (interior 200x400, 300x700, 400x1000, 600x1500 + 50-cell PML),
+# 64 shots each, trace lengths 1500 / 2000 / 3000 / 4000 steps, 8th order,
+# smooth random vp 1500-4500 m/s (seeded), forward with records on row 2.
+UNEVEN = [(200, 400, 1500), (300, 700, 2000), (400, 1000, 3000), (600, 1500, 4000)]
+
+
+def bench_uneven(args):
+    import torch
+    from scipy.ndimage import gaussian_filter
+    from seistorch_gb300 import _native, engine, tuning
+    from seistorch_gb300.pml import generate_pml_coefficients_2d
+    from seistorch_gb300.utils import ricker_wave
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm is timed on the acoustic "
+                          "gradient workload only"}))
+        return 0
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _native.load(build_if_missing=False)
+    shots = args.shots if args.shots != NSHOTS else 64
+    scale = 1.0 if args.nt == NT else args.nt / 4000.0
+    rng = np.random.default_rng(0)
+    groups = []
+    for nzi, nxi, nt in UNEVEN:
+        nt = max(8, int(nt * scale))
+        noise = gaussian_filter(rng.standard_normal((nzi, nxi)), sigma=20)
+        vp = 1500.0 + 3000.0 * (noise - noise.min()) / (noise.max() - noise.min())
+        vp = np.pad(vp, WIDTH, mode="edge")
+        nz, nx = vp.shape
+        d = generate_pml_coefficients_2d((nz, nx), WIDTH).to(device=dev, dtype=torch.float32)
+        xs = np.linspace(0, nxi - 1, shots).round().astype(int)
+        src = [[(WIDTH + 2, WIDTH + int(x))] for x in xs]
+        rec = [([WIDTH + 2] * nxi, list(range(WIDTH, WIDTH + nxi)))] * shots
+        wav = ricker_wave(FM, DT, nt, delay=int(1.2 / FM / DT), dtype="numpy")
+        prop = engine.AcousticPropagator(nz, nx, DT, H, ORDER, "pml", WIDTH, False, dev)
+        acq = engine.Acquisition(nz, nx, src, rec, wav, dev)
+        groups.append((prop, torch.tensor(vp, dtype=torch.float32, device=dev), d, acq))
+    # autotuner: per-grid winners, then the batch timed on each of them
+    per_grid = [tuning.tune_grid(p.nz, p.nx, shots, ORDER, DT, H, WIDTH, dev, steps=24, adjoint=False)[0][0]
+                for p, _, _, _ in groups]
+    batch = engine.UnevenBatch(groups)
+    best, tune_ms = tuning.tune_batch(batch.run, per_grid)
+    batch.plan()
+    pts = batch.points()
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        batch.replay()
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clocks:
+        t0, t1 = ev(), ev()
+        t0.record(stream)
+        for _ in range(args.steps):
+            batch.replay()
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    # same grids one after another, one loop each (no graph), for reference
+    t2, t3 = ev(), ev()
+    t2.record(stream)
+    for prop, vp, d, acq in groups:
+        prop.forward(vp, d, acq)
+    t3.record(stream)
+    torch.cuda.synchronize()
+    seq_ms = t2.elapsed_time(t3)
+    npts_step = sum(acq.nshots * p.nz * p.nx for p, _, _, acq in groups)
+    peak, kind = measured_peaks()
+    gbs = pts * BYTES_FWD / (ms * 1e-3) / 1e9
+    line = {"metric": "Gpts/s fwd (uneven batch)", "value": pts / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "uneven_forward_4grids_x%dshots" % shots,
+                       "grids": [[p.nz, p.nx, acq.nt] for p, _, _, acq in groups], "shots_per_grid": shots,
+                       "order": ORDER, "launch": "one persistent launch per step, whole loop one CUDA graph",
+                       "variant_per_grid": per_grid, "variant_batch": best,
+                       "l2": "inputs larger than L2"},
+            "shots_per_s": len(groups) * shots / (ms * 1e-3),
+            "sequential_loops_ms": seq_ms, "tuning_ms": tune_ms,
+            "roofline": {"kernel": "acoustic_fwd_batch_kernel", "bound": "hbm", "achieved": gbs, "peak": peak,
+                         "peak_kind": kind, "unit": "GB/s", "frac": gbs / peak, "traffic": None,
+                         "bytes_per_point": BYTES_FWD, "points_per_step_max": npts_step},
+            "gpu_launches": args.steps * max(acq.nt for _, _, _, acq in groups), "clocks": clocks.summary()}
+    batch.close()
+    print(json.dumps(line))
+    return 0
 
 
 if __name__ == "__main__":
