@@ -203,6 +203,7 @@ def main():
     import torch.distributed as dist
 
     from seistorch_gb300 import _native, engine
+    from seistorch_gb300.distributed import allreduce_gradient
     from seistorch_gb300.pml import generate_pml_coefficients_2d
     from seistorch_gb300.utils import ricker_wave
 
@@ -243,7 +244,7 @@ def main():
         loss = ((rec - obs) ** 2).sum()
         loss.backward()
         if world > 1:
-            dist.all_reduce(vp.grad)
+            allreduce_gradient(vp.grad)
         e2.record(stream)
         if timing is not None:
             timing.append((e0, e1, e2))
@@ -320,6 +321,7 @@ def e2e_through_api(args, dev, vp_init, obs_host, wav, sources, receivers, world
     import torch.distributed as dist
 
     from seistorch_gb300 import build_model
+    from seistorch_gb300.distributed import allreduce_gradient
 
     cfg = {"equation": "acoustic", "dtype": "float32",
            "geom": {"dt": DT, "h": H, "nt": NT, "boundary": {"type": "pml", "width": WIDTH},
@@ -348,7 +350,7 @@ def e2e_through_api(args, dev, vp_init, obs_host, wav, sources, receivers, world
         loss = ((syn - obs) ** 2).sum()
         loss.backward()
         if world > 1:
-            dist.all_reduce(param.grad)
+            allreduce_gradient(param.grad)
         grad_host.copy_(param.grad, non_blocking=True)
         loss_host.copy_(loss.detach().reshape(1), non_blocking=True)
 
