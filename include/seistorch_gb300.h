@@ -311,6 +311,52 @@ int sgb_elastic_gradient(const sgb_grid *grid, const sgb_elastic_model *model, c
                          const float *vp, const float *vs, const float *rho, const sgb_bs_store *bs, int32_t box,
                          float *const grad_out[3], sgb_stream_t stream);
 
+/* --------------------------------------------- learned preconditioner --- */
+/* BF16-weight / FP32-accumulate kernels of the convolutional gradient
+ * preconditioner (no counterpart in the reference, which preconditions by
+ * the illumination only, process.py:115-118).  Activations are bf16 NHWC
+ * [n][h][w][c]; 3x3 convolutions with zero padding 1 run as implicit GEMMs
+ * on the tcgen05 tensor cores (accumulator in tensor memory).  Channel
+ * counts of tensor-core convolutions are multiples of 32; w is a multiple
+ * of 64 (or 64 <= w < 128 with 128 % w == 0). */
+
+/* y = conv3x3(x, wt) (+ bias) (ReLU) (* [mask > 0]), written to out_bf16
+ * and/or out_f32 at [pixel * out_cstride + out_coff + co] (a channel slice
+ * of a wider tensor, e.g. a skip concatenation).  wt: bf16 [cout][9][cin]
+ * (tap = 3 ky + kx).  With wt flipped and transposed ([cin][9][cout], tap
+ * 8 - t) the same call gives the data gradient. */
+typedef struct {
+  int32_t n, h, w, cin, cout;
+  const void *x;
+  const void *wt;
+  const float *bias;  /* [cout] or NULL */
+  int32_t relu;
+  const void *mask;   /* bf16 NHWC or NULL */
+  int32_t mask_cstride;
+  void *out_bf16;     /* or NULL */
+  float *out_f32;     /* or NULL */
+  int32_t out_cstride, out_coff;
+} sgb_nn_conv;
+int sgb_nn_conv3x3(const sgb_nn_conv *c, sgb_stream_t stream);
+
+/* dw[tap][co][ci] += sum over pixels of dy[co] * x[ci] at the tap's offset.
+ * dy_chw: bf16 [n][cout][h][w]; x_chw[k]: bf16 [n][cin][h][w] holding the
+ * input shifted by k - 1 columns (x_chw[k][..][x] = x[..][x - 1 + k], zero
+ * outside), as sgb_nn_to_chw writes it; dw: fp32 [9][cout][cin]. */
+typedef struct {
+  int32_t n, h, w, cin, cout;
+  const void *dy_chw;
+  const void *x_chw[3];
+  float *dw;
+} sgb_nn_wgrad;
+int sgb_nn_conv3x3_wgrad(const sgb_nn_wgrad *p, sgb_stream_t stream);
+
+/* NHWC (channel slice [coff, coff + c) of a tensor with cstride channels)
+ * -> CHW bf16 [copies][n][c][h][w]: copies = 1 gives the plain transpose,
+ * copies = 3 the three column-shifted copies sgb_nn_conv3x3_wgrad reads. */
+int sgb_nn_to_chw(int32_t n, int32_t h, int32_t w, int32_t c, int32_t cstride, int32_t coff, const void *x_nhwc,
+                  int32_t copies, void *out, sgb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,8 @@ BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_NAME = "libseistorch_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 SOURCES = ["acoustic.cu", "acoustic_stream.cu", "acoustic_stream_fwd.cu", "acoustic_stream_bwd.cu",
-           "elastic.cu", "capi.cu", "capi_elastic.cu", "capi_batch.cu", "noalloc.cu"]
+           "elastic.cu", "capi.cu", "capi_elastic.cu", "capi_batch.cu", "noalloc.cu",
+           "nn_gemm.cu", "nn_ops.cu", "capi_nn.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -109,6 +110,18 @@ class BatchGroup(ctypes.Structure):
                 ("illum", c_ptr)]
 
 
+class NnConv(ctypes.Structure):
+    _fields_ = [("n", c_i32), ("h", c_i32), ("w", c_i32), ("cin", c_i32), ("cout", c_i32),
+                ("x", c_ptr), ("wt", c_ptr), ("bias", c_ptr), ("relu", c_i32), ("mask", c_ptr),
+                ("mask_cstride", c_i32), ("out_bf16", c_ptr), ("out_f32", c_ptr), ("out_cstride", c_i32),
+                ("out_coff", c_i32)]
+
+
+class NnWgrad(ctypes.Structure):
+    _fields_ = [("n", c_i32), ("h", c_i32), ("w", c_i32), ("cin", c_i32), ("cout", c_i32),
+                ("dy_chw", c_ptr), ("x_chw", c_ptr * 3), ("dw", c_ptr)]
+
+
 PTR3 = c_ptr * 3
 PTR2 = c_ptr * 2
 PTR5 = c_ptr * 5
@@ -143,6 +156,9 @@ SIGNATURES = {
                                                ctypes.POINTER(c_i32), ctypes.POINTER(c_ptr)]),
     "sgb_plan_launch": (ctypes.c_int, [c_ptr, c_ptr]),
     "sgb_plan_destroy": (ctypes.c_int, [c_ptr]),
+    "sgb_nn_conv3x3": (ctypes.c_int, [ctypes.POINTER(NnConv), c_ptr]),
+    "sgb_nn_conv3x3_wgrad": (ctypes.c_int, [ctypes.POINTER(NnWgrad), c_ptr]),
+    "sgb_nn_to_chw": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_i32, c_i32, c_ptr, c_i32, c_ptr, c_ptr]),
     "sgb_elastic_coefficients": (ctypes.c_int, [ctypes.POINTER(Grid), c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                                                 c_ptr]),
     "sgb_elastic_step": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ElasticModel), PTR5, PTR5,

@@ -1,0 +1,324 @@
+// BF16 x BF16 -> FP32 GEMM on the 5th-generation tensor cores (tcgen05) for
+// the learned gradient preconditioner's 3x3 convolutions.
+//
+// One CTA computes a 128 x BN tile of D = sum_k A[m, k] B[n, k] (both
+// operands K-major) with the accumulator in tensor memory:
+//   warp 0 lane 0  -- TMA producer: per K step one A box (128 rows x RB
+//                     bytes) and one B box (BN rows x RB bytes) into a stage
+//                     of an S-deep ring, 128/64-byte swizzled;
+//   warp 1 lane 0  -- MMA issuer: RB/32 tcgen05.mma (K = 16) per stage, then
+//                     tcgen05.commit to the stage's "empty" mbarrier;
+//   all 4 warps    -- epilogue: tcgen05.ld of their 32 TMEM lanes (= rows).
+// Warp 0 allocates and frees the TMEM columns.  Every wait is bounded; on a
+// timeout the CTA records DEV_ERR_TIMEOUT, waits (bounded) for what it
+// issued and frees its TMEM before returning.
+//
+// Two operand modes:
+//   CONV  : implicit GEMM of a 3x3 convolution (zero padding 1).  A = input
+//           activation NHWC, rows = 128 output pixels (TH rows x TW columns
+//           of one image), K step = (tap, 32/64-channel chunk) read at the
+//           tap's shifted (x, y) -- shifts are on the W and H dimensions of
+//           the tensor map, never on the innermost one; B = weights
+//           [Cout][9][Cin].  Used for the forward pass and, with flipped
+//           transposed weights, for the data gradient.
+//   WGRAD : weight gradient of one tap (blockIdx.z % 9) and 128 output
+//           channels (blockIdx.z / 9): A = dY in CHW (rows = output channels), B = the input in CHW shifted by the tap's x
+//           offset (one of three pre-shifted copies) and read at the tap's y
+//           offset; K = pixels, split over blockIdx.x; FP32 atomics into dW.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "sgb_common.cuh"
+#include "tma.cuh"
+#include "nn_args.cuh"
+
+namespace sgb {
+namespace nn {
+namespace {
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major, swizzled operand tile whose
+// rows are RB bytes (RB = 128: 128-byte swizzle, RB = 64: 64-byte swizzle);
+// 8-row groups are 8 * RB bytes apart.
+template <int RB>
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  constexpr uint64_t layout = RB == 128 ? 2ull : 4ull;  // SWIZZLE_128B : SWIZZLE_64B
+  constexpr uint64_t sbo = (8ull * RB) >> 4;
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | (1ull << 16) | (sbo << 32) | (1ull << 46) | (layout << 61);
+}
+
+// Instruction descriptor: D fp32, A and B bf16, both K-major, M = 128, N = BN.
+template <int BN>
+__device__ __forceinline__ uint32_t instr_desc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "setp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+      "}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+
+// 16 consecutive fp32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int BN, int RB, int S>
+struct GemmLayout {
+  static constexpr int A_BYTES = 128 * RB;
+  static constexpr int B_BYTES = BN * RB;
+  static constexpr int STAGE = A_BYTES + B_BYTES;  // multiple of 1024 for every (BN, RB) used
+  static constexpr int BYTES = S * STAGE + 1024 /*align*/ + 256 /*barriers + tmem slot*/;
+};
+
+template <int BN, int RB, int S>
+__global__ void __launch_bounds__(128, 1) nn_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                         const __grid_constant__ CUtensorMap tmB0,
+                                                         const __grid_constant__ CUtensorMap tmB1,
+                                                         const __grid_constant__ CUtensorMap tmB2,
+                                                         const GemmArgs g) {
+  using Lay = GemmLayout<BN, RB, S>;
+  constexpr int TMEM_COLS = BN < 32 ? 32 : BN;
+  constexpr int KSTEPS = RB / 32;  // tcgen05.mma K = 16 bf16 = 32 bytes
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + S * Lay::STAGE);
+  uint64_t* empty = full + S;
+  uint64_t* done = empty + S;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 2);
+  __shared__ int s_fail;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  // ---- tile of this CTA and its K range
+  int kbeg = 0, kend = g.kiters;
+  int n_img = 0, y0 = 0, x0 = 0, m0 = 0, tap = 0;
+  const int n0 = blockIdx.y * BN;
+  if (g.mode == MODE_CONV) {
+    const int t = blockIdx.x;
+    const int per_img = g.tiles_x * g.tiles_y;
+    n_img = t / per_img;
+    const int r = t % per_img;
+    y0 = (r / g.tiles_x) * g.TH;
+    x0 = (r % g.tiles_x) * g.TW;
+  } else {
+    tap = blockIdx.z % 9;
+    m0 = (blockIdx.z / 9) * 128;
+    kbeg = blockIdx.x * g.k_per_split;
+    kend = min(kbeg + g.k_per_split, g.kiters);
+  }
+  const CUtensorMap* tmB = &tmB0;
+  if (g.mode == MODE_WGRAD) {
+    const int kx = tap % 3;
+    tmB = kx == 0 ? &tmB0 : (kx == 1 ? &tmB1 : &tmB2);
+  }
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (threadIdx.x == 32) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done[0], 1);
+    mbar_init(&done[1], 1);
+    fence_mbar_init();
+    s_fail = 0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const int nk = kend - kbeg;
+  int issued = 0;  // K steps whose boxes the producer issued
+
+  if (warp == 0 && lane == 0) {
+    // ---- TMA producer
+    for (int i = 0; i < nk; ++i) {
+      const int s = i % S;
+      if (i >= S && !mbar_wait(&empty[s], ((i / S) - 1) & 1, g.status)) {
+        s_fail = 1;
+        break;
+      }
+      if (*reinterpret_cast<volatile int*>(&s_fail)) break;
+      unsigned char* sa = base + s * Lay::STAGE;
+      unsigned char* sb = sa + Lay::A_BYTES;
+      mbar_arrive_expect_tx(&full[s], Lay::STAGE);
+      const int k = kbeg + i;
+      if (g.mode == MODE_CONV) {
+        const int tp = k / g.nchunk, c0 = (k % g.nchunk) * (RB / 2);
+        const int ky = tp / 3, kx = tp % 3;
+        tma_load_4d(sa, &tmA, c0, x0 - 1 + kx, y0 - 1 + ky, n_img, &full[s]);
+        tma_load_3d(sb, tmB, c0, tp, n0, &full[s]);
+      } else {
+        const int xc = k % g.wchunks, rest = k / g.wchunks;
+        const int y = rest % g.H, n = rest / g.H;
+        const int ky = tap / 3;
+        tma_load_4d(sa, &tmA, xc * 64, y, m0, n, &full[s]);
+        tma_load_4d(sb, tmB, xc * 64, y - 1 + ky, n0, n, &full[s]);
+      }
+      issued = i + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer
+    const uint32_t idesc = instr_desc<BN>();
+    int i = 0;
+    for (; i < nk; ++i) {
+      const int s = i % S;
+      if (!mbar_wait(&full[s], (i / S) & 1, g.status)) {
+        s_fail = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t sa = smem_u32(base + s * Lay::STAGE);
+      const uint32_t sb = sa + Lay::A_BYTES;
+      const uint64_t da = smem_desc<RB>(sa), db = smem_desc<RB>(sb);
+#pragma unroll
+      for (int kk = 0; kk < KSTEPS; ++kk)
+        mma_bf16(tmem, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (i > 0 || kk > 0) ? 1u : 0u);
+      mma_commit(&empty[s]);
+    }
+    mma_commit(&done[0]);  // completes once every MMA issued above has finished
+  }
+  __syncwarp();
+  // ---- epilogue: wait for the accumulator (the decision is CTA-uniform:
+  // tcgen05.ld is a warp-collective)
+  const bool got = nk > 0 && mbar_wait(&done[0], 0, g.status);
+  tc_fence_after();
+  const bool ok = __syncthreads_and(got) && !s_fail;
+  if (ok) {
+    const int row = warp * 32 + lane;  // TMEM lane == tile row
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    if (g.mode == MODE_CONV) {
+      const int py = y0 + row / g.TW, px = x0 + row % g.TW;
+      const bool inrow = py < g.H && px < g.W;
+      const long long pix = ((long long)n_img * g.H + py) * g.W + px;
+#pragma unroll 1
+      for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tmem_ld16(taddr + c, v);
+        const int co = n0 + c;
+        if (!inrow || co >= g.Cout) continue;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          float a = v[j];
+          if (g.bias != nullptr) a += g.bias[co + j];
+          if (g.relu && a < 0.f) a = 0.f;
+          if (g.mask != nullptr) {
+            const float mk = __bfloat162float(g.mask[pix * g.mask_cstride + co + j]);
+            a = mk > 0.f ? a : 0.f;
+          }
+          v[j] = a;
+        }
+        if (g.out_f32 != nullptr) {
+          float* o = g.out_f32 + pix * g.out_cstride + g.out_coff + co;
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            if (co + j < g.Cout) o[j] = v[j];
+        }
+        if (g.out_bf16 != nullptr) {
+          __nv_bfloat16* o = g.out_bf16 + pix * g.out_cstride + g.out_coff + co;
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            if (co + j < g.Cout) o[j] = __float2bfloat16_rn(v[j]);
+        }
+      }
+    } else {
+      // dW[tap][co][ci] += D[co][ci]
+#pragma unroll 1
+      for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tmem_ld16(taddr + c, v);
+        const int co = m0 + row;
+        if (co >= g.Cout) continue;
+        float* o = g.out_f32 + ((long long)tap * g.Cout + co) * g.Cin + n0 + c;
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (n0 + c + j < g.Cin) atomicAdd(o + j, v[j]);
+      }
+    }
+  }
+  // ---- drain: boxes issued but never consumed (only after a failure)
+  if (warp == 0 && lane == 0 && !ok) {
+    for (int i = 0; i < issued; ++i) mbar_wait(&full[i % S], (i / S) & 1, nullptr);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+template <int BN, int RB>
+cudaError_t launch_t(const CUtensorMap* maps, const GemmArgs& g, dim3 grid, cudaStream_t s) {
+  constexpr int S = 4;
+  using Lay = GemmLayout<BN, RB, S>;
+  auto kern = nn_gemm_kernel<BN, RB, S>;
+  static bool set = false;
+  if (!set) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::BYTES);
+    if (e != cudaSuccess) return e;
+    set = true;
+  }
+  kern<<<grid, 128, Lay::BYTES, s>>>(maps[0], maps[1], maps[2], maps[3], g);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_gemm(int bn, int rb, const CUtensorMap* maps, const GemmArgs& g, dim3 grid, cudaStream_t s) {
+  if (rb == 128) {
+    switch (bn) {
+      case 32: return launch_t<32, 128>(maps, g, grid, s);
+      case 64: return launch_t<64, 128>(maps, g, grid, s);
+      case 128: return launch_t<128, 128>(maps, g, grid, s);
+    }
+  } else if (rb == 64) {
+    switch (bn) {
+      case 32: return launch_t<32, 64>(maps, g, grid, s);
+      case 64: return launch_t<64, 64>(maps, g, grid, s);
+      case 128: return launch_t<128, 64>(maps, g, grid, s);
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace nn
+}  // namespace sgb
