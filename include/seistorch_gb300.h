@@ -339,10 +339,10 @@ typedef struct {
 } sgb_nn_conv;
 int sgb_nn_conv3x3(const sgb_nn_conv *c, sgb_stream_t stream);
 
-/* dw[tap][co][ci] += sum over pixels of dy[co] * x[ci] at the tap's offset.
+/* dw[co][ci][tap] += sum over pixels of dy[co] * x[ci] at the tap's offset.
  * dy_chw: bf16 [n][cout][h][w]; x_chw[k]: bf16 [n][cin][h][w] holding the
  * input shifted by k - 1 columns (x_chw[k][..][x] = x[..][x - 1 + k], zero
- * outside), as sgb_nn_to_chw writes it; dw: fp32 [9][cout][cin]. */
+ * outside), as sgb_nn_to_chw writes it; dw: fp32 [cout][cin][3][3]. */
 typedef struct {
   int32_t n, h, w, cin, cout;
   const void *dy_chw;
@@ -356,6 +356,39 @@ int sgb_nn_conv3x3_wgrad(const sgb_nn_wgrad *p, sgb_stream_t stream);
  * copies = 3 the three column-shifted copies sgb_nn_conv3x3_wgrad reads. */
 int sgb_nn_to_chw(int32_t n, int32_t h, int32_t w, int32_t c, int32_t cstride, int32_t coff, const void *x_nhwc,
                   int32_t copies, void *out, sgb_stream_t stream);
+
+/* SIMT helpers of the network (h, w: the fine grid of the operation).
+ * Input convolution: fp32 [n][2][h][w] -> c channels, ReLU; W [c][2][3][3].
+ * Output convolution: c channels -> fp32 [n][h][w], linear; W [c][3][3].
+ * Its backward writes dx (bf16 NHWC, c channels) times [act > 0] and
+ * accumulates dW, db.  pool2: 2x2 average; up2: nearest 2x into a channel
+ * slice; up2_bwd: 2x2 sums of a slice of an fp32 gradient times [act > 0];
+ * pool2_bwd: gp / 4 (coarse, c channels) + an optional slice gs, times
+ * [act > 0].  pack_weights: fp32 [cout][cin][3][3] -> bf16 [cout][9][cin]
+ * and (if wflip) the flipped transpose [cin][9][cout] for data gradients.
+ * adam: one step (bias-corrected, step >= 1, decoupled weight decay wd).
+ * mse: grad = 2 (pred - target) / n and *loss += mean squared error. */
+int sgb_nn_conv_in(int32_t n, int32_t h, int32_t w, int32_t c, const float *in, const float *W, const float *b,
+                   void *out, int32_t cstride, int32_t coff, sgb_stream_t stream);
+int sgb_nn_conv_in_wgrad(int32_t n, int32_t h, int32_t w, int32_t c, const float *in, const void *dy,
+                         int32_t dy_cstride, float *dW, float *db, sgb_stream_t stream);
+int sgb_nn_conv_out(int32_t n, int32_t h, int32_t w, int32_t c, const void *in, int32_t cstride, const float *W,
+                    const float *b, float *out, sgb_stream_t stream);
+int sgb_nn_conv_out_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float *g, const float *W, const void *act,
+                        int32_t act_cstride, void *dx, float *dW, float *db, sgb_stream_t stream);
+int sgb_nn_pool2(int32_t n, int32_t h, int32_t w, int32_t c, const void *in, int32_t cs_in, int32_t coff_in,
+                 void *out, sgb_stream_t stream);
+int sgb_nn_up2(int32_t n, int32_t h, int32_t w, int32_t c, const void *in, void *out, int32_t cs_out,
+               int32_t coff_out, sgb_stream_t stream);
+int sgb_nn_up2_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float *g, int32_t cs_g, int32_t coff_g,
+                   const void *act, void *out, sgb_stream_t stream);
+int sgb_nn_pool2_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float *gp, const float *gs, int32_t cs_s,
+                     int32_t coff_s, const void *act, int32_t cs_a, int32_t coff_a, void *out, sgb_stream_t stream);
+int sgb_nn_bias_grad(int64_t npix, int32_t c, const void *dy, float *db, sgb_stream_t stream);
+int sgb_nn_pack_weights(int32_t cout, int32_t cin, const float *W, void *wt, void *wflip, sgb_stream_t stream);
+int sgb_nn_adam(int64_t n, float *p, const float *g, float *m, float *v, float lr, float b1, float b2, float eps,
+                int32_t step, float wd, sgb_stream_t stream);
+int sgb_nn_mse(int64_t n, const float *pred, const float *target, float *grad, float *loss, sgb_stream_t stream);
 
 #ifdef __cplusplus
 }

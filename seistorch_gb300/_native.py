@@ -159,6 +159,22 @@ SIGNATURES = {
     "sgb_nn_conv3x3": (ctypes.c_int, [ctypes.POINTER(NnConv), c_ptr]),
     "sgb_nn_conv3x3_wgrad": (ctypes.c_int, [ctypes.POINTER(NnWgrad), c_ptr]),
     "sgb_nn_to_chw": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_i32, c_i32, c_ptr, c_i32, c_ptr, c_ptr]),
+    "sgb_nn_conv_in": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_ptr, c_ptr, c_ptr, c_ptr, c_i32, c_i32, c_ptr]),
+    "sgb_nn_conv_in_wgrad": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_ptr, c_ptr, c_i32, c_ptr, c_ptr,
+                                            c_ptr]),
+    "sgb_nn_conv_out": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_ptr, c_i32, c_ptr, c_ptr, c_ptr, c_ptr]),
+    "sgb_nn_conv_out_bwd": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_ptr, c_ptr, c_ptr, c_i32, c_ptr, c_ptr,
+                                           c_ptr, c_ptr]),
+    "sgb_nn_pool2": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_ptr, c_i32, c_i32, c_ptr, c_ptr]),
+    "sgb_nn_up2": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_ptr, c_ptr, c_i32, c_i32, c_ptr]),
+    "sgb_nn_up2_bwd": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_ptr, c_i32, c_i32, c_ptr, c_ptr, c_ptr]),
+    "sgb_nn_pool2_bwd": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_ptr, c_ptr, c_i32, c_i32, c_ptr, c_i32,
+                                        c_i32, c_ptr, c_ptr]),
+    "sgb_nn_bias_grad": (ctypes.c_int, [ctypes.c_int64, c_i32, c_ptr, c_ptr, c_ptr]),
+    "sgb_nn_pack_weights": (ctypes.c_int, [c_i32, c_i32, c_ptr, c_ptr, c_ptr, c_ptr]),
+    "sgb_nn_adam": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_f32, c_f32, c_f32, c_f32, c_i32,
+                                   c_f32, c_ptr]),
+    "sgb_nn_mse": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr]),
     "sgb_elastic_coefficients": (ctypes.c_int, [ctypes.POINTER(Grid), c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                                                 c_ptr]),
     "sgb_elastic_step": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ElasticModel), PTR5, PTR5,

@@ -11,8 +11,31 @@
 namespace sgb {
 namespace nn {
 cudaError_t launch_gemm(int bn, int rb, const CUtensorMap* maps, const GemmArgs& g, dim3 grid, cudaStream_t s);
-cudaError_t launch_to_chw(int n, int h, int w, int c, int cstride, int coff, const __nv_bfloat16* x, int copies,
-                          __nv_bfloat16* out, cudaStream_t s);
+using bf16 = __nv_bfloat16;
+cudaError_t launch_to_chw(int n, int h, int w, int c, int cstride, int coff, const bf16* x, int copies, bf16* out,
+                          cudaStream_t s);
+cudaError_t launch_conv_in_fwd(int n, int h, int w, int c, const float* in, const float* W, const float* b, bf16* out,
+                               int cstride, int coff, cudaStream_t s);
+cudaError_t launch_conv_in_wgrad(int n, int h, int w, int c, const float* in, const bf16* dy, int dy_cstride,
+                                 float* dW, float* db, cudaStream_t s);
+cudaError_t launch_conv_out_fwd(int n, int h, int w, int c, const bf16* in, int cstride, const float* W,
+                                const float* b, float* out, cudaStream_t s);
+cudaError_t launch_conv_out_bwd(int n, int h, int w, int c, const float* g, const float* W, const bf16* act,
+                                int act_cstride, bf16* dx, float* dW, float* db, cudaStream_t s);
+cudaError_t launch_pool2(int n, int h, int w, int c, const bf16* in, int cs_in, int coff_in, bf16* out,
+                         cudaStream_t s);
+cudaError_t launch_up2(int n, int h, int w, int c, const bf16* in, bf16* out, int cs_out, int coff_out,
+                       cudaStream_t s);
+cudaError_t launch_up2_bwd(int n, int h, int w, int c, const float* g, int cs_g, int coff_g, const bf16* act,
+                           bf16* out, cudaStream_t s);
+cudaError_t launch_pool2_bwd(int n, int h, int w, int c, const float* gp, const float* gs, int cs_s, int coff_s,
+                             const bf16* act, int cs_a, int coff_a, bf16* out, cudaStream_t s);
+cudaError_t launch_bias_grad(long long npix, int c, const bf16* dy, float* db, cudaStream_t s);
+cudaError_t launch_pack_weights(int cout, int cin, const float* W, bf16* wt, bf16* wflip, cudaStream_t s);
+cudaError_t launch_adam(long long n, float* p, const float* g, float* m, float* v, float lr, float b1, float b2,
+                        float eps, int step, float wd, cudaStream_t s);
+cudaError_t launch_mse(long long n, const float* pred, const float* target, float* grad, float* loss,
+                       cudaStream_t s);
 }  // namespace nn
 }  // namespace sgb
 
@@ -173,8 +196,108 @@ int sgb_nn_to_chw(int32_t n, int32_t h, int32_t w, int32_t c, int32_t cstride, i
                   int32_t copies, void* out, sgb_stream_t stream) {
   if (x_nhwc == nullptr || out == nullptr || (copies != 1 && copies != 3)) return SGB_ERR_ARG;
   if (n <= 0 || h <= 0 || w <= 0 || c <= 0 || cstride < coff + c || coff < 0) return SGB_ERR_SHAPE;
-  SGB_CUDA_CHECK(launch_to_chw(n, h, w, c, cstride, coff, static_cast<const __nv_bfloat16*>(x_nhwc), copies,
-                               static_cast<__nv_bfloat16*>(out), (cudaStream_t)stream));
+  SGB_CUDA_CHECK(launch_to_chw(n, h, w, c, cstride, coff, static_cast<const bf16*>(x_nhwc), copies,
+                               static_cast<bf16*>(out), (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+#define NN_DIMS_OK(n, h, w, c) ((n) > 0 && (h) > 0 && (w) > 0 && (c) > 0)
+#define BF(p) static_cast<const bf16*>(p)
+#define BFW(p) static_cast<bf16*>(p)
+
+int sgb_nn_conv_in(int32_t n, int32_t h, int32_t w, int32_t c, const float* in, const float* W, const float* b,
+                   void* out, int32_t cstride, int32_t coff, sgb_stream_t stream) {
+  if (in == nullptr || W == nullptr || b == nullptr || out == nullptr) return SGB_ERR_ARG;
+  if (!NN_DIMS_OK(n, h, w, c) || cstride < coff + c || coff < 0) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_conv_in_fwd(n, h, w, c, in, W, b, BFW(out), cstride, coff, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_conv_in_wgrad(int32_t n, int32_t h, int32_t w, int32_t c, const float* in, const void* dy,
+                         int32_t dy_cstride, float* dW, float* db, sgb_stream_t stream) {
+  if (in == nullptr || dy == nullptr || dW == nullptr || db == nullptr) return SGB_ERR_ARG;
+  if (!NN_DIMS_OK(n, h, w, c) || dy_cstride < c) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_conv_in_wgrad(n, h, w, c, in, BF(dy), dy_cstride, dW, db, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_conv_out(int32_t n, int32_t h, int32_t w, int32_t c, const void* in, int32_t cstride, const float* W,
+                    const float* b, float* out, sgb_stream_t stream) {
+  if (in == nullptr || W == nullptr || b == nullptr || out == nullptr) return SGB_ERR_ARG;
+  if (!NN_DIMS_OK(n, h, w, c) || cstride < c) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_conv_out_fwd(n, h, w, c, BF(in), cstride, W, b, out, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_conv_out_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float* g, const float* W, const void* act,
+                        int32_t act_cstride, void* dx, float* dW, float* db, sgb_stream_t stream) {
+  if (g == nullptr || W == nullptr || act == nullptr || dx == nullptr || dW == nullptr || db == nullptr)
+    return SGB_ERR_ARG;
+  if (!NN_DIMS_OK(n, h, w, c) || act_cstride < c) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_conv_out_bwd(n, h, w, c, g, W, BF(act), act_cstride, BFW(dx), dW, db, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_pool2(int32_t n, int32_t h, int32_t w, int32_t c, const void* in, int32_t cs_in, int32_t coff_in,
+                 void* out, sgb_stream_t stream) {
+  if (in == nullptr || out == nullptr) return SGB_ERR_ARG;
+  if (!NN_DIMS_OK(n, h, w, c) || h % 2 || w % 2 || cs_in < coff_in + c || coff_in < 0) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_pool2(n, h, w, c, BF(in), cs_in, coff_in, BFW(out), (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_up2(int32_t n, int32_t h, int32_t w, int32_t c, const void* in, void* out, int32_t cs_out,
+               int32_t coff_out, sgb_stream_t stream) {
+  if (in == nullptr || out == nullptr) return SGB_ERR_ARG;
+  if (!NN_DIMS_OK(n, h, w, c) || h % 2 || w % 2 || cs_out < coff_out + c || coff_out < 0) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_up2(n, h, w, c, BF(in), BFW(out), cs_out, coff_out, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_up2_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float* g, int32_t cs_g, int32_t coff_g,
+                   const void* act, void* out, sgb_stream_t stream) {
+  if (g == nullptr || act == nullptr || out == nullptr) return SGB_ERR_ARG;
+  if (!NN_DIMS_OK(n, h, w, c) || h % 2 || w % 2 || cs_g < coff_g + c || coff_g < 0) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_up2_bwd(n, h, w, c, g, cs_g, coff_g, BF(act), BFW(out), (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_pool2_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float* gp, const float* gs, int32_t cs_s,
+                     int32_t coff_s, const void* act, int32_t cs_a, int32_t coff_a, void* out, sgb_stream_t stream) {
+  if (gp == nullptr || act == nullptr || out == nullptr) return SGB_ERR_ARG;
+  if (!NN_DIMS_OK(n, h, w, c) || h % 2 || w % 2 || cs_a < coff_a + c || (gs != nullptr && cs_s < coff_s + c))
+    return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_pool2_bwd(n, h, w, c, gp, gs, cs_s, coff_s, BF(act), cs_a, coff_a, BFW(out),
+                                  (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_bias_grad(int64_t npix, int32_t c, const void* dy, float* db, sgb_stream_t stream) {
+  if (dy == nullptr || db == nullptr) return SGB_ERR_ARG;
+  if (npix <= 0 || c <= 0) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_bias_grad(npix, c, BF(dy), db, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_pack_weights(int32_t cout, int32_t cin, const float* W, void* wt, void* wflip, sgb_stream_t stream) {
+  if (W == nullptr || wt == nullptr) return SGB_ERR_ARG;
+  if (cout <= 0 || cin <= 0) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_pack_weights(cout, cin, W, BFW(wt), BFW(wflip), (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_adam(int64_t n, float* p, const float* g, float* m, float* v, float lr, float b1, float b2, float eps,
+                int32_t step, float wd, sgb_stream_t stream) {
+  if (p == nullptr || g == nullptr || m == nullptr || v == nullptr) return SGB_ERR_ARG;
+  if (n <= 0 || step < 1) return SGB_ERR_ARG;
+  SGB_CUDA_CHECK(launch_adam(n, p, g, m, v, lr, b1, b2, eps, step, wd, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_nn_mse(int64_t n, const float* pred, const float* target, float* grad, float* loss, sgb_stream_t stream) {
+  if (pred == nullptr || target == nullptr || grad == nullptr || loss == nullptr) return SGB_ERR_ARG;
+  if (n <= 0) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_mse(n, pred, target, grad, loss, (cudaStream_t)stream));
   return SGB_OK;
 }
 

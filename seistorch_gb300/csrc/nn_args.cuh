@@ -25,7 +25,7 @@ struct GemmArgs {
   const __nv_bfloat16* mask;
   int mask_cstride;
   __nv_bfloat16* out_bf16;
-  float* out_f32;  // CONV: optional fp32 copy; WGRAD: dW [9][Cout][Cin] (accumulated)
+  float* out_f32;  // CONV: optional fp32 copy; WGRAD: dW [Cout][Cin][3][3] (accumulated)
   int out_cstride, out_coff;
   int* status;
 };

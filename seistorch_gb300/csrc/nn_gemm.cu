@@ -24,7 +24,8 @@
 //   WGRAD : weight gradient of one tap (blockIdx.z % 9) and 128 output
 //           channels (blockIdx.z / 9): A = dY in CHW (rows = output channels), B = the input in CHW shifted by the tap's x
 //           offset (one of three pre-shifted copies) and read at the tap's y
-//           offset; K = pixels, split over blockIdx.x; FP32 atomics into dW.
+//           offset; K = pixels, split over blockIdx.x; FP32 atomics into
+//           dW[cout][cin][3][3].
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -260,17 +261,17 @@ __global__ void __launch_bounds__(128, 1) nn_gemm_kernel(const __grid_constant__
         }
       }
     } else {
-      // dW[tap][co][ci] += D[co][ci]
+      // dW[co][ci][tap] += D[co][ci]   (the [cout][cin][3][3] layout)
 #pragma unroll 1
       for (int c = 0; c < BN; c += 16) {
         float v[16];
         tmem_ld16(taddr + c, v);
         const int co = m0 + row;
         if (co >= g.Cout) continue;
-        float* o = g.out_f32 + ((long long)tap * g.Cout + co) * g.Cin + n0 + c;
+        float* o = g.out_f32 + ((long long)co * g.Cin + n0 + c) * 9 + tap;
 #pragma unroll
         for (int j = 0; j < 16; ++j)
-          if (n0 + c + j < g.Cin) atomicAdd(o + j, v[j]);
+          if (n0 + c + j < g.Cin) atomicAdd(o + 9 * j, v[j]);
       }
     }
   }

@@ -1,5 +1,10 @@
 // Memory-bound helper kernels of the learned preconditioner (layouts,
-// pooling, upsampling, small convolutions, optimiser): plain SIMT code.
+// pooling, upsampling, the 2-channel input and 1-channel output
+// convolutions, weight packing, optimiser, loss): plain SIMT code.  The
+// heavy 3x3 convolutions run on the tensor cores (nn_gemm.cu).
+//
+// Activations are bf16 NHWC; a tensor may be a channel slice [coff, coff+c)
+// of a wider one with cstride channels per pixel.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -9,14 +14,24 @@ namespace sgb {
 namespace nn {
 namespace {
 
-// out[k][n][c][y][x] = in[n][y][x - 1 + k][coff + c] (k over copies; with one
-// copy k = 1, the plain transpose).  One thread per (n, c, y, x).
-__global__ void to_chw_kernel(int n, int h, int w, int c, int cstride, int coff, const __nv_bfloat16* in,
-                              int copies, __nv_bfloat16* out) {
+using bf16 = __nv_bfloat16;
+
+__device__ __forceinline__ float ld(const bf16* p) { return __bfloat162float(*p); }
+__device__ __forceinline__ bf16 st(float v) { return __float2bfloat16_rn(v); }
+
+int blocks_for(long long n) {
+  long long b = (n + 255) / 256;
+  return (int)(b > 152 * 32 ? 152 * 32 : (b < 1 ? 1 : b));
+}
+
+#define GRID_STRIDE(i, total) \
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (total); i += (long long)gridDim.x * blockDim.x)
+
+// out[k][n][c][y][x] = in[n][y][x - 1 + k][coff + c] (one copy: k = 1).
+__global__ void to_chw_kernel(int n, int h, int w, int c, int cstride, int coff, const bf16* in, int copies,
+                              bf16* out) {
   const long long total = (long long)n * c * h * w;
-  const long long plane = total;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
+  GRID_STRIDE(i, total) {
     const int x = (int)(i % w);
     long long r = i / w;
     const int y = (int)(r % h);
@@ -24,26 +39,353 @@ __global__ void to_chw_kernel(int n, int h, int w, int c, int cstride, int coff,
     const int ch = (int)(r % c);
     const int b = (int)(r / c);
     for (int k = 0; k < copies; ++k) {
-      const int shift = copies == 1 ? 0 : k - 1;
-      const int xs = x + shift;
-      __nv_bfloat16 v = __float2bfloat16_rn(0.f);
+      const int xs = x + (copies == 1 ? 0 : k - 1);
+      bf16 v = st(0.f);
       if (xs >= 0 && xs < w) v = in[(((long long)b * h + y) * w + xs) * cstride + coff + ch];
-      out[k * plane + i] = v;
+      out[k * total + i] = v;
     }
   }
 }
 
-int blocks_for(long long n) {
-  long long b = (n + 255) / 256;
-  return (int)(b > 152 * 32 ? 152 * 32 : (b < 1 ? 1 : b));
+// Input convolution: 2 fp32 channels [n][2][h][w] -> c bf16 channels (ReLU).
+__global__ void conv_in_fwd_kernel(int n, int h, int w, int c, const float* in, const float* W, const float* b,
+                                   bf16* out, int cstride, int coff) {
+  const long long total = (long long)n * h * w;
+  GRID_STRIDE(i, total) {
+    const int x = (int)(i % w);
+    const int y = (int)((i / w) % h);
+    const int bb = (int)(i / ((long long)w * h));
+    float v[18];
+    for (int ci = 0; ci < 2; ++ci)
+      for (int ky = 0; ky < 3; ++ky)
+        for (int kx = 0; kx < 3; ++kx) {
+          const int yy = y - 1 + ky, xx = x - 1 + kx;
+          v[ci * 9 + ky * 3 + kx] =
+              (yy >= 0 && yy < h && xx >= 0 && xx < w) ? in[(((long long)bb * 2 + ci) * h + yy) * w + xx] : 0.f;
+        }
+    for (int co = 0; co < c; ++co) {
+      float a = b[co];
+      for (int k = 0; k < 18; ++k) a = fmaf(W[co * 18 + k], v[k], a);
+      out[i * cstride + coff + co] = st(a > 0.f ? a : 0.f);
+    }
+  }
+}
+
+// Weight / bias gradient of the input convolution: block (co, split).
+__global__ void conv_in_wgrad_kernel(int n, int h, int w, int c, const float* in, const bf16* dy, int dy_cstride,
+                                     float* dW, float* db) {
+  const int co = blockIdx.y;
+  const long long total = (long long)n * h * w;
+  float acc[19];
+  for (int k = 0; k < 19; ++k) acc[k] = 0.f;
+  GRID_STRIDE(i, total) {
+    const float g = ld(dy + i * dy_cstride + co);
+    if (g == 0.f) continue;
+    const int x = (int)(i % w);
+    const int y = (int)((i / w) % h);
+    const int bb = (int)(i / ((long long)w * h));
+    for (int ci = 0; ci < 2; ++ci)
+      for (int ky = 0; ky < 3; ++ky)
+        for (int kx = 0; kx < 3; ++kx) {
+          const int yy = y - 1 + ky, xx = x - 1 + kx;
+          if (yy >= 0 && yy < h && xx >= 0 && xx < w)
+            acc[ci * 9 + ky * 3 + kx] += g * in[(((long long)bb * 2 + ci) * h + yy) * w + xx];
+        }
+    acc[18] += g;
+  }
+  for (int k = 0; k < 19; ++k) {
+    float v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) {
+      if (k < 18)
+        atomicAdd(dW + co * 18 + k, v);
+      else
+        atomicAdd(db + co, v);
+    }
+  }
+}
+
+// Output convolution: c bf16 channels -> 1 fp32 channel (linear).
+__global__ void conv_out_fwd_kernel(int n, int h, int w, int c, const bf16* in, int cstride, const float* W,
+                                    const float* b, float* out) {
+  const long long total = (long long)n * h * w;
+  GRID_STRIDE(i, total) {
+    const int x = (int)(i % w);
+    const int y = (int)((i / w) % h);
+    const int bb = (int)(i / ((long long)w * h));
+    float a = b[0];
+    for (int ky = 0; ky < 3; ++ky)
+      for (int kx = 0; kx < 3; ++kx) {
+        const int yy = y - 1 + ky, xx = x - 1 + kx;
+        if (yy < 0 || yy >= h || xx < 0 || xx >= w) continue;
+        const bf16* p = in + (((long long)bb * h + yy) * w + xx) * cstride;
+        for (int ci = 0; ci < c; ++ci) a = fmaf(W[ci * 9 + ky * 3 + kx], ld(p + ci), a);
+      }
+    out[i] = a;
+  }
+}
+
+// Data gradient of the output convolution, times [act > 0] (the ReLU of the
+// layer that produced its input): dx[p][ci] = sum_tap W[ci][tap] g[p - off].
+__global__ void conv_out_dgrad_kernel(int n, int h, int w, int c, const float* g, const float* W, const bf16* act,
+                                      int act_cstride, bf16* dx) {
+  const long long total = (long long)n * h * w;
+  GRID_STRIDE(i, total) {
+    const int x = (int)(i % w);
+    const int y = (int)((i / w) % h);
+    const int bb = (int)(i / ((long long)w * h));
+    float gv[9];
+    for (int ky = 0; ky < 3; ++ky)
+      for (int kx = 0; kx < 3; ++kx) {
+        // output pixel (y + 1 - ky, x + 1 - kx) reads this pixel through tap (ky, kx)
+        const int yy = y + 1 - ky, xx = x + 1 - kx;
+        gv[ky * 3 + kx] = (yy >= 0 && yy < h && xx >= 0 && xx < w) ? g[((long long)bb * h + yy) * w + xx] : 0.f;
+      }
+    for (int ci = 0; ci < c; ++ci) {
+      float a = 0.f;
+      for (int k = 0; k < 9; ++k) a = fmaf(W[ci * 9 + k], gv[k], a);
+      const float m = ld(act + i * act_cstride + ci);
+      dx[i * c + ci] = st(m > 0.f ? a : 0.f);
+    }
+  }
+}
+
+// Weight / bias gradient of the output convolution: block (ci, split).
+__global__ void conv_out_wgrad_kernel(int n, int h, int w, int c, const float* g, const bf16* in, int cstride,
+                                      float* dW, float* db) {
+  const int ci = blockIdx.y;
+  const long long total = (long long)n * h * w;
+  float acc[10];
+  for (int k = 0; k < 10; ++k) acc[k] = 0.f;
+  GRID_STRIDE(i, total) {
+    const float gv = g[i];
+    const int x = (int)(i % w);
+    const int y = (int)((i / w) % h);
+    const int bb = (int)(i / ((long long)w * h));
+    for (int ky = 0; ky < 3; ++ky)
+      for (int kx = 0; kx < 3; ++kx) {
+        const int yy = y - 1 + ky, xx = x - 1 + kx;
+        if (yy >= 0 && yy < h && xx >= 0 && xx < w)
+          acc[ky * 3 + kx] += gv * ld(in + (((long long)bb * h + yy) * w + xx) * cstride + ci);
+      }
+    acc[9] += gv;
+  }
+  for (int k = 0; k < 10; ++k) {
+    float v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) {
+      if (k < 9)
+        atomicAdd(dW + ci * 9 + k, v);
+      else if (ci == 0)
+        atomicAdd(db, v);
+    }
+  }
+}
+
+// 2x2 average pooling; h, w are the input dims.
+__global__ void pool2_kernel(int n, int h, int w, int c, const bf16* in, int cs_in, int coff_in, bf16* out) {
+  const int ho = h / 2, wo = w / 2;
+  const long long total = (long long)n * ho * wo * c;
+  GRID_STRIDE(i, total) {
+    const int ch = (int)(i % c);
+    long long r = i / c;
+    const int x = (int)(r % wo);
+    r /= wo;
+    const int y = (int)(r % ho);
+    const int b = (int)(r / ho);
+    float a = 0.f;
+    for (int dy = 0; dy < 2; ++dy)
+      for (int dx = 0; dx < 2; ++dx)
+        a += ld(in + (((long long)b * h + 2 * y + dy) * w + 2 * x + dx) * cs_in + coff_in + ch);
+    out[i] = st(0.25f * a);
+  }
+}
+
+// Nearest 2x upsampling into a channel slice; h, w are the output dims.
+__global__ void up2_kernel(int n, int h, int w, int c, const bf16* in, bf16* out, int cs_out, int coff_out) {
+  const long long total = (long long)n * h * w * c;
+  GRID_STRIDE(i, total) {
+    const int ch = (int)(i % c);
+    long long r = i / c;
+    const int x = (int)(r % w);
+    r /= w;
+    const int y = (int)(r % h);
+    const int b = (int)(r / h);
+    out[(((long long)b * h + y) * w + x) * cs_out + coff_out + ch] =
+        in[(((long long)b * (h / 2) + y / 2) * (w / 2) + x / 2) * c + ch];
+  }
+}
+
+// Gradient through the upsampling (sum of the 2x2 children of a channel
+// slice of g, fp32) times [act > 0]; h, w are the fine dims.
+__global__ void up2_bwd_kernel(int n, int h, int w, int c, const float* g, int cs_g, int coff_g, const bf16* act,
+                               bf16* out) {
+  const int ho = h / 2, wo = w / 2;
+  const long long total = (long long)n * ho * wo * c;
+  GRID_STRIDE(i, total) {
+    const int ch = (int)(i % c);
+    long long r = i / c;
+    const int x = (int)(r % wo);
+    r /= wo;
+    const int y = (int)(r % ho);
+    const int b = (int)(r / ho);
+    float a = 0.f;
+    for (int dy = 0; dy < 2; ++dy)
+      for (int dx = 0; dx < 2; ++dx) a += g[(((long long)b * h + 2 * y + dy) * w + 2 * x + dx) * cs_g + coff_g + ch];
+    out[i] = st(ld(act + i) > 0.f ? a : 0.f);
+  }
+}
+
+// Gradient at an encoder output: pooling backward (gp / 4 from the coarse
+// level) plus the skip branch (a channel slice of g), times [act > 0];
+// h, w are the fine dims.
+__global__ void pool2_bwd_kernel(int n, int h, int w, int c, const float* gp, const float* gs, int cs_s, int coff_s,
+                                 const bf16* act, int cs_a, int coff_a, bf16* out) {
+  const long long total = (long long)n * h * w * c;
+  GRID_STRIDE(i, total) {
+    const int ch = (int)(i % c);
+    long long r = i / c;
+    const int x = (int)(r % w);
+    r /= w;
+    const int y = (int)(r % h);
+    const int b = (int)(r / h);
+    const long long pix = ((long long)b * h + y) * w + x;
+    float a = 0.25f * gp[(((long long)b * (h / 2) + y / 2) * (w / 2) + x / 2) * c + ch];
+    if (gs != nullptr) a += gs[pix * cs_s + coff_s + ch];
+    out[i] = st(ld(act + pix * cs_a + coff_a + ch) > 0.f ? a : 0.f);
+  }
+}
+
+// db[c] += sum over pixels of dy[p][c]: block (channel group of 32 lanes? no:
+// one thread per (channel, pixel stride)).
+__global__ void bias_grad_kernel(long long npix, int c, const bf16* dy, float* db) {
+  const int ch = blockIdx.y;
+  float a = 0.f;
+  GRID_STRIDE(p, npix) a += ld(dy + p * c + ch);
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(db + ch, a);
+}
+
+// fp32 [cout][cin][3][3] -> bf16 [cout][9][cin] and flipped transpose [cin][9][cout].
+__global__ void pack_weights_kernel(int cout, int cin, const float* W, bf16* wt, bf16* wflip) {
+  const long long total = (long long)cout * cin * 9;
+  GRID_STRIDE(i, total) {
+    const int t = (int)(i % 9);
+    const int ci = (int)((i / 9) % cin);
+    const int co = (int)(i / (9LL * cin));
+    const bf16 v = st(W[i]);
+    wt[((long long)co * 9 + t) * cin + ci] = v;
+    if (wflip != nullptr) wflip[((long long)ci * 9 + (8 - t)) * cout + co] = v;
+  }
+}
+
+__global__ void adam_kernel(long long n, float* p, const float* g, float* m, float* v, float lr, float b1, float b2,
+                            float eps, float c1, float c2, float wd) {
+  GRID_STRIDE(i, n) {
+    const float gi = g[i] + wd * p[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+// loss += sum (pred - target)^2 / count; grad = 2 (pred - target) / count.
+__global__ void mse_kernel(long long n, const float* pred, const float* target, float inv_count, float* grad,
+                           float* loss) {
+  float a = 0.f;
+  GRID_STRIDE(i, n) {
+    const float d = pred[i] - target[i];
+    grad[i] = 2.f * d * inv_count;
+    a += d * d;
+  }
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, a * inv_count);
 }
 
 }  // namespace
 
-cudaError_t launch_to_chw(int n, int h, int w, int c, int cstride, int coff, const __nv_bfloat16* x, int copies,
-                          __nv_bfloat16* out, cudaStream_t s) {
-  const long long total = (long long)n * c * h * w;
-  to_chw_kernel<<<blocks_for(total), 256, 0, s>>>(n, h, w, c, cstride, coff, x, copies, out);
+cudaError_t launch_to_chw(int n, int h, int w, int c, int cstride, int coff, const bf16* x, int copies, bf16* out,
+                          cudaStream_t s) {
+  to_chw_kernel<<<blocks_for((long long)n * c * h * w), 256, 0, s>>>(n, h, w, c, cstride, coff, x, copies, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conv_in_fwd(int n, int h, int w, int c, const float* in, const float* W, const float* b, bf16* out,
+                               int cstride, int coff, cudaStream_t s) {
+  conv_in_fwd_kernel<<<blocks_for((long long)n * h * w), 256, 0, s>>>(n, h, w, c, in, W, b, out, cstride, coff);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conv_in_wgrad(int n, int h, int w, int c, const float* in, const bf16* dy, int dy_cstride,
+                                 float* dW, float* db, cudaStream_t s) {
+  const dim3 grid(64, c);
+  conv_in_wgrad_kernel<<<grid, 256, 0, s>>>(n, h, w, c, in, dy, dy_cstride, dW, db);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conv_out_fwd(int n, int h, int w, int c, const bf16* in, int cstride, const float* W,
+                                const float* b, float* out, cudaStream_t s) {
+  conv_out_fwd_kernel<<<blocks_for((long long)n * h * w), 256, 0, s>>>(n, h, w, c, in, cstride, W, b, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conv_out_bwd(int n, int h, int w, int c, const float* g, const float* W, const bf16* act,
+                                int act_cstride, bf16* dx, float* dW, float* db, cudaStream_t s) {
+  conv_out_dgrad_kernel<<<blocks_for((long long)n * h * w), 256, 0, s>>>(n, h, w, c, g, W, act, act_cstride, dx);
+  const dim3 grid(64, c);
+  conv_out_wgrad_kernel<<<grid, 256, 0, s>>>(n, h, w, c, g, act, act_cstride, dW, db);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pool2(int n, int h, int w, int c, const bf16* in, int cs_in, int coff_in, bf16* out,
+                         cudaStream_t s) {
+  pool2_kernel<<<blocks_for((long long)n * (h / 2) * (w / 2) * c), 256, 0, s>>>(n, h, w, c, in, cs_in, coff_in, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_up2(int n, int h, int w, int c, const bf16* in, bf16* out, int cs_out, int coff_out,
+                       cudaStream_t s) {
+  up2_kernel<<<blocks_for((long long)n * h * w * c), 256, 0, s>>>(n, h, w, c, in, out, cs_out, coff_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_up2_bwd(int n, int h, int w, int c, const float* g, int cs_g, int coff_g, const bf16* act,
+                           bf16* out, cudaStream_t s) {
+  up2_bwd_kernel<<<blocks_for((long long)n * (h / 2) * (w / 2) * c), 256, 0, s>>>(n, h, w, c, g, cs_g, coff_g, act,
+                                                                                   out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pool2_bwd(int n, int h, int w, int c, const float* gp, const float* gs, int cs_s, int coff_s,
+                             const bf16* act, int cs_a, int coff_a, bf16* out, cudaStream_t s) {
+  pool2_bwd_kernel<<<blocks_for((long long)n * h * w * c), 256, 0, s>>>(n, h, w, c, gp, gs, cs_s, coff_s, act, cs_a,
+                                                                         coff_a, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bias_grad(long long npix, int c, const bf16* dy, float* db, cudaStream_t s) {
+  const dim3 grid(64, c);
+  bias_grad_kernel<<<grid, 256, 0, s>>>(npix, c, dy, db);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_weights(int cout, int cin, const float* W, bf16* wt, bf16* wflip, cudaStream_t s) {
+  pack_weights_kernel<<<blocks_for((long long)cout * cin * 9), 256, 0, s>>>(cout, cin, W, wt, wflip);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adam(long long n, float* p, const float* g, float* m, float* v, float lr, float b1, float b2,
+                        float eps, int step, float wd, cudaStream_t s) {
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  adam_kernel<<<blocks_for(n), 256, 0, s>>>(n, p, g, m, v, lr, b1, b2, eps, c1, c2, wd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mse(long long n, const float* pred, const float* target, float* grad, float* loss,
+                       cudaStream_t s) {
+  mse_kernel<<<blocks_for(n), 256, 0, s>>>(n, pred, target, 1.f / (float)n, grad, loss);
   return cudaGetLastError();
 }
 

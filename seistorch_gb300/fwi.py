@@ -1,0 +1,192 @@
+"""Full-waveform inversion driver: the plain illumination-preconditioned
+gradient method and the learned-preconditioner method, both on the native
+solver.
+
+Plain (the reference's preconditioning, process.py:115-118 + a normalised
+steepest-descent step, optimizer.py:124-142): d = -g / (P + eps max P),
+scaled to a maximum update of ``alpha`` m/s, accepted only if the data
+misfit decreases (halving ``alpha`` otherwise).
+
+Learned: the network maps [g / max|g|, P / max P] to a model update; the
+update is accepted only if the true data misfit decreases (at full or half
+length), else the plain step is taken -- the misfit stays the judge of the
+network's error and the plain gradient its fallback.
+
+Training pairs come from the solver itself: random layered + anomaly
+models, the smoothed model as the starting point, and the L2 gradient and
+source illumination at that starting point; the target is the model error
+(true - start) / 1000 m/s.
+"""
+import time
+
+import numpy as np
+import torch
+
+from . import engine
+from .pml import generate_pml_coefficients_2d
+from .utils import ricker_wave
+
+TARGET_SCALE = 1000.0  # m/s per unit of network output
+
+
+def random_model(rng, nz=256, nx=512, vmin=1500.0, vmax=4500.0):
+    """Seeded layered + anomaly velocity model (m/s), nz x nx."""
+    zz, xx = np.mgrid[0:nz, 0:nx].astype(np.float64)
+    nl = int(rng.integers(3, 8))
+    base = np.sort(rng.uniform(0.08, 0.95, nl - 1)) * nz
+    vel = np.sort(rng.uniform(vmin, vmax, nl))
+    vel[0] = rng.uniform(vmin, vmin + 500.0)
+    depth_shift = (rng.uniform(-0.08, 0.08) * (xx - nx / 2)
+                   + rng.uniform(0, 12) * np.sin(2 * np.pi * xx / nx * rng.uniform(0.5, 3) + rng.uniform(0, 6)))
+    layer = np.zeros((nz, nx), np.int64)
+    for k, d in enumerate(base):
+        layer += (zz > d + depth_shift).astype(np.int64)
+    v = vel[layer]
+    for _ in range(int(rng.integers(1, 4))):
+        cz, cx = rng.uniform(0.2, 0.9) * nz, rng.uniform(0.1, 0.9) * nx
+        r = rng.uniform(8, 35)
+        v += rng.choice([-1.0, 1.0]) * rng.uniform(200, 600) * np.exp(-((zz - cz) ** 2 + (xx - cx) ** 2) / (2 * r * r))
+    return np.clip(v, vmin, vmax)
+
+
+def smooth(v, sigma=20.0):
+    from scipy.ndimage import gaussian_filter
+    return gaussian_filter(v, sigma, mode="nearest")
+
+
+class Survey:
+    """Acquisition + propagator for inversions on an nz x nx interior grid."""
+
+    def __init__(self, nz=256, nx=512, shots=32, nt=3000, dt=0.001, h=10.0, fm=8.0, width=50, order=4,
+                 device=None):
+        self.dev = torch.device(device or "cuda")
+        self.nzi, self.nxi, self.w = nz, nx, width
+        self.nz, self.nx = nz + 2 * width, nx + 2 * width
+        self.nt, self.dt, self.h = nt, dt, h
+        self.prop = engine.AcousticPropagator(self.nz, self.nx, dt, h, order, "pml", width, False, self.dev)
+        xs = np.linspace(0, nx - 1, shots).round().astype(int)
+        src = [[(width + 2, width + int(x))] for x in xs]
+        rec = [([width + 2] * nx, list(range(width, width + nx)))] * shots
+        wav = ricker_wave(fm, dt, nt, delay=int(1.2 / fm / dt), dtype="numpy")
+        self.acq = engine.Acquisition(self.nz, self.nx, src, rec, wav, self.dev)
+        self.d = generate_pml_coefficients_2d((self.nz, self.nx), width).to(self.dev, torch.float32)
+        self.ckpt = engine.default_ckpt_every(nt)
+
+    def pad(self, v):
+        """Interior model (numpy or tensor) -> padded device tensor."""
+        v = torch.as_tensor(v, dtype=torch.float32, device=self.dev)
+        return torch.nn.functional.pad(v[None, None], (self.w,) * 4, mode="replicate")[0, 0].contiguous()
+
+    def records(self, vp_pad):
+        with torch.no_grad():
+            rec, _ = engine.acoustic_loop(vp_pad, self.prop, self.d, self.acq)
+        return rec
+
+    def misfit(self, vp_pad, obs):
+        return float(((self.records(vp_pad) - obs) ** 2).sum())
+
+    def gradient(self, vp_pad, obs):
+        """(misfit, gradient (interior), illumination (interior))."""
+        vp = vp_pad.clone().requires_grad_(True)
+        rec, illum = engine.acoustic_loop(vp, self.prop, self.d, self.acq, True, self.ckpt)
+        loss = ((rec - obs) ** 2).sum()
+        loss.backward()
+        w = self.w
+        return float(loss.detach()), vp.grad[w:-w, w:-w].detach(), illum[w:-w, w:-w].detach()
+
+
+def features(g, P):
+    """Network input [g / max|g|, P / max P] of shape (2, nz, nx)."""
+    gn = g / g.abs().max().clamp_min(1e-30)
+    pn = P / P.max().clamp_min(1e-30)
+    return torch.stack([gn, pn]).to(torch.float32)
+
+
+def plain_direction(g, P, eps=1e-3):
+    d = -g / (P + eps * P.max())
+    return d / d.abs().max().clamp_min(1e-30)
+
+
+def make_pairs(n, survey, seed=0, log=None):
+    """n training pairs (features (n, 2, nz, nx), targets (n, nz, nx)) from
+    random models, computed by the solver on the device."""
+    rng = np.random.default_rng(seed)
+    X = torch.empty(n, 2, survey.nzi, survey.nxi, device=survey.dev)
+    Y = torch.empty(n, survey.nzi, survey.nxi, device=survey.dev)
+    t0 = time.perf_counter()
+    for i in range(n):
+        vt = random_model(rng, survey.nzi, survey.nxi)
+        v0 = smooth(vt)
+        obs = survey.records(survey.pad(vt))
+        _, g, P = survey.gradient(survey.pad(v0), obs)
+        X[i] = features(g, P)
+        Y[i] = torch.as_tensor((vt - v0) / TARGET_SCALE, dtype=torch.float32, device=survey.dev)
+        if log and (i + 1) % 100 == 0:
+            log(f"pairs {i + 1}/{n} ({time.perf_counter() - t0:.1f} s)")
+    return X, Y
+
+
+def train(net, X, Y, epochs=10, batch=8, lr=1e-3, seed=0, log=None):
+    """Adam on the mean squared error over shuffled mini-batches; returns the
+    per-epoch mean loss."""
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    n = X.shape[0]
+    hist = []
+    for ep in range(epochs):
+        perm = torch.randperm(n, generator=g)
+        tot = torch.zeros((), device=X.device)
+        nb = 0
+        lr_ep = lr * (0.5 ** (ep // max(1, epochs // 3)))
+        for k in range(0, n - batch + 1, batch):
+            idx = perm[k:k + batch].to(X.device)
+            tot += net.train_batch(X[idx], Y[idx], lr_ep)[0]
+            nb += 1
+        hist.append(float(tot) / max(nb, 1))
+        if log:
+            log(f"epoch {ep + 1}/{epochs}: loss {hist[-1]:.5f}")
+    return hist
+
+
+def invert(survey, obs, v0, iters=20, net=None, alpha=100.0, vmin=1500.0, vmax=4500.0, log=None):
+    """FWI from interior model v0.  Returns dict(misfit=[...], time=[...],
+    learned_steps=k, model=final interior model).  misfit[i] / time[i]: data
+    misfit and elapsed wall time after i iterations (i = 0: start)."""
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    v = torch.as_tensor(v0, dtype=torch.float32, device=survey.dev).clone()
+    hist_m, hist_t = [], []
+    learned_steps = 0
+    J, g, P = survey.gradient(survey.pad(v), obs)
+    hist_m.append(J)
+    hist_t.append(time.perf_counter() - t0)
+    for it in range(iters):
+        accepted = False
+        if net is not None:
+            dv = net.predict(features(g, P)[None])[0] * TARGET_SCALE
+            for beta in (1.0, 0.5):
+                cand = (v + beta * dv).clamp(vmin, vmax)
+                Jc = survey.misfit(survey.pad(cand), obs)
+                if Jc < J:
+                    v, accepted = cand, True
+                    learned_steps += 1
+                    break
+        if not accepted:
+            d = plain_direction(g, P)
+            a = alpha
+            for _ in range(4):
+                cand = (v + a * d).clamp(vmin, vmax)
+                Jc = survey.misfit(survey.pad(cand), obs)
+                if Jc < J:
+                    v, accepted = cand, True
+                    alpha = a * 1.5 if a == alpha else a
+                    break
+                a *= 0.5
+            if not accepted:
+                alpha *= 0.25
+        J, g, P = survey.gradient(survey.pad(v), obs)
+        hist_m.append(J)
+        torch.cuda.synchronize()
+        hist_t.append(time.perf_counter() - t0)
+        if log:
+            log(f"iter {it + 1}: misfit {J:.4e} ({hist_t[-1]:.1f} s)")
+    return {"misfit": hist_m, "time": hist_t, "learned_steps": learned_steps, "model": v}

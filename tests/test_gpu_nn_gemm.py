@@ -93,12 +93,12 @@ def test_weight_gradient_matches_torch(N, n, h, w, cin, cout):
     wt = torch.zeros(cout, cin, 3, 3, device=dev, requires_grad=True)
     dy = torch.randn(n, cout, h, w, device=dev).bfloat16().float()
     F.conv2d(x, wt, padding=1).backward(dy)
-    want = wt.grad.permute(2, 3, 0, 1).reshape(9, cout, cin)
+    want = wt.grad.reshape(cout, cin, 9)
     x_nhwc = x.permute(0, 2, 3, 1).contiguous().bfloat16()
     xs = torch.empty(3, n, cin, h, w, device=dev, dtype=torch.bfloat16)
     N.call("sgb_nn_to_chw", n, h, w, cin, cin, 0, N.ptr(x_nhwc), 3, N.ptr(xs), N.stream_handle())
     dy_chw = dy.contiguous().bfloat16()
-    dw = torch.zeros(9, cout, cin, device=dev)
+    dw = torch.zeros(cout, cin, 9, device=dev)
     p = N.NnWgrad(n, h, w, cin, cout, N.ptr(dy_chw), N.PTR3(*[xs[k].data_ptr() for k in range(3)]), N.ptr(dw))
     N.call("sgb_nn_conv3x3_wgrad", ctypes.byref(p), N.stream_handle())
     torch.cuda.synchronize()
