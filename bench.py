@@ -188,10 +188,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="acoustic_gradient",
-                    choices=["acoustic_gradient", "elastic_gradient", "uneven_forward"],
+                    choices=["acoustic_gradient", "elastic_gradient", "uneven_forward", "learned_fwi"],
                     help="acoustic_gradient (default, the headline line); elastic_gradient: 300x800 + 50 PML "
                          "elastic forward+adjoint; uneven_forward: 4 grid sizes x 64 shots in one launch per step")
+    ap.add_argument("--pairs", type=int, default=2000, help="learned_fwi: training pairs")
+    ap.add_argument("--epochs", type=int, default=12, help="learned_fwi: training epochs")
+    ap.add_argument("--iters", type=int, default=20, help="learned_fwi: FWI iterations")
+    ap.add_argument("--save-net", default="", help="learned_fwi: write the trained parameters (.npz)")
     args = ap.parse_args()
+    if args.workload == "learned_fwi":
+        return bench_learned(args)
     if args.workload == "elastic_gradient":
         return bench_elastic(args)
     if args.workload == "uneven_forward":
@@ -572,6 +578,100 @@ def bench_uneven(args):
                          "bytes_per_point": BYTES_FWD, "points_per_step_max": npts_step},
             "gpu_launches": args.steps * max(acq.nt for _, _, _, acq in groups), "clocks": clocks.summary()}
     batch.close()
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------- learned FWI (C5) ---
+# Network: 4-level U-Net, 32 base channels (~1.16 M parameters), bf16
+# weights / fp32 accumulation on tcgen05, inputs raw gradient +
+# illumination on 256 x 512.  Pairs: seeded random layered + anomaly models
+# (1500-4500 m/s), gradient at the smoothed model from 8 shots x 1500 steps.
+# FWI: 20 iterations, 32 shots, 3000 steps, 8 Hz, on a held-out model;
+# plain illumination-preconditioned gradient vs the learned update (misfit-
+# judged, plain fallback).  value = wall time for the learned run to reach
+# the plain run's final misfit / the plain run's wall time.
+
+
+def conv_flops(B, H, W):
+    """FLOPs of one forward pass of the network (multiply-add = 2)."""
+    from seistorch_gb300.learned import LAYERS
+    res = {"e1a": 0, "e1b": 0, "e2a": 1, "e2b": 1, "e3a": 2, "e3b": 2, "b4": 3, "d3": 2, "d2": 1, "d1": 0,
+           "out": 0}
+    return sum(2.0 * B * (H >> res[n]) * (W >> res[n]) * ci * co * 9 for n, ci, co, _ in LAYERS)
+
+
+def bench_learned(args):
+    import torch
+    from seistorch_gb300 import _native, fwi
+    from seistorch_gb300.learned import PrecondNet, n_params
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned preconditioner; its "
+                          "arm is timed on the acoustic gradient workload"}))
+        return 0
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _native.load(build_if_missing=False)
+    log = lambda m: print(m, file=sys.stderr, flush=True)
+    t0 = time.perf_counter()
+    train_sv = fwi.Survey(256, 512, shots=8, nt=1500, fm=8.0, device=dev)
+    X, Y = fwi.make_pairs(args.pairs, train_sv, seed=0, log=log)
+    torch.cuda.synchronize()
+    t_pairs = time.perf_counter() - t0
+    net = PrecondNet(dev, seed=0)
+    # tensor-core throughput of the network (forward + backward, batch 8)
+    xb, yb = X[:8].contiguous(), Y[:8].contiguous()
+    for _ in range(3):
+        net.train_batch(xb, yb, 0.0)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    e0, e1 = ev(), ev()
+    e0.record()
+    for _ in range(10):
+        net.forward(xb)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / 10
+    net = PrecondNet(dev, seed=0)
+    t1 = time.perf_counter()
+    hist = fwi.train(net, X, Y, epochs=args.epochs, batch=8, lr=1e-3, log=log)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t1
+    if args.save_net:
+        np.savez(args.save_net, **net.state_dict())
+    # held-out inversion
+    sv = fwi.Survey(256, 512, shots=32, nt=3000, fm=8.0, device=dev)
+    rng = np.random.default_rng(12345)
+    vt = fwi.random_model(rng, 256, 512)
+    v0 = fwi.smooth(vt)
+    obs = sv.records(sv.pad(vt))
+    plain = fwi.invert(sv, obs, v0, iters=args.iters, log=lambda m: log("plain " + m))
+    learned = fwi.invert(sv, obs, v0, iters=args.iters, net=net, log=lambda m: log("learned " + m))
+    target = plain["misfit"][-1]
+    t_plain = plain["time"][-1]
+    reach = next((t for m, t in zip(learned["misfit"], learned["time"]) if m <= target), None)
+    ratio = reach / t_plain if reach is not None else None
+    model_err = lambda r: float(torch.linalg.norm(r["model"] - torch.as_tensor(vt, device=dev, dtype=torch.float32))
+                                / np.linalg.norm(vt - v0))
+    peak = None
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            peak = json.load(f).get("bf16_tflops")
+    tflops = conv_flops(8, 256, 512) / (fwd_ms * 1e-3) / 1e12
+    line = {"metric": "FWI time-to-misfit, learned vs plain", "value": ratio, "unit": "x plain wall time",
+            "higher_is_better": False, "n_gpus": 1, "steps": 1, "warmup": 0, "vs_baseline": None,
+            "dtype": "bf16 weights / fp32 accumulate (network), f32 (solver)", "data": "synthetic",
+            "config": {"workload": "learned_preconditioner_fwi_256x512_32shots_nt3000", "pairs": args.pairs,
+                       "pair_survey": "8 shots x 1500 steps", "epochs": args.epochs, "iters": args.iters,
+                       "params": n_params()},
+            "plain": {"final_misfit": target, "wall_s": t_plain, "misfit": plain["misfit"],
+                      "time": plain["time"], "model_error": model_err(plain)},
+            "learned": {"misfit": learned["misfit"], "time": learned["time"], "learned_steps": learned["learned_steps"],
+                        "reach_s": reach, "model_error": model_err(learned)},
+            "training": {"pairs_s": t_pairs, "train_s": t_train, "loss": hist},
+            "roofline": {"kernel": "nn_gemm_kernel (network forward, batch 8, 256x512)", "bound": "tensor",
+                         "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (tflops / peak) if peak else None, "forward_ms": fwd_ms}}
     print(json.dumps(line))
     return 0
 

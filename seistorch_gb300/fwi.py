@@ -8,13 +8,13 @@ scaled to a maximum update of ``alpha`` m/s, accepted only if the data
 misfit decreases (halving ``alpha`` otherwise).
 
 Learned: the network maps [g / max|g|, P / max P] to a model update; the
-update is accepted only if the true data misfit decreases (at full or half
-length), else the plain step is taken -- the misfit stays the judge of the
+update is accepted only if the true data misfit decreases (at full, half or
+quarter length), else the plain step is taken -- the misfit stays the judge of the
 network's error and the plain gradient its fallback.
 
 Training pairs come from the solver itself: random layered + anomaly
-models, the smoothed model as the starting point, and the L2 gradient and
-source illumination at that starting point; the target is the model error
+models, a starting point between the smoothed model and the truth, and the
+L2 gradient and source illumination there; the target is the model error
 (true - start) / 1000 m/s.
 """
 import time
@@ -116,7 +116,11 @@ def make_pairs(n, survey, seed=0, log=None):
     t0 = time.perf_counter()
     for i in range(n):
         vt = random_model(rng, survey.nzi, survey.nxi)
+        # a starting model part-way between the smoothed model and the truth,
+        # as later inversion iterates are
+        tau = rng.uniform(0.0, 0.75) if i % 2 else 0.0
         v0 = smooth(vt)
+        v0 = v0 + tau * (vt - v0)
         obs = survey.records(survey.pad(vt))
         _, g, P = survey.gradient(survey.pad(v0), obs)
         X[i] = features(g, P)
@@ -163,7 +167,7 @@ def invert(survey, obs, v0, iters=20, net=None, alpha=100.0, vmin=1500.0, vmax=4
         accepted = False
         if net is not None:
             dv = net.predict(features(g, P)[None])[0] * TARGET_SCALE
-            for beta in (1.0, 0.5):
+            for beta in (1.0, 0.5, 0.25):
                 cand = (v + beta * dv).clamp(vmin, vmax)
                 Jc = survey.misfit(survey.pad(cand), obs)
                 if Jc < J:
