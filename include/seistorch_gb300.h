@@ -149,10 +149,13 @@ int sgb_acoustic_forward(const sgb_grid *grid, const sgb_acoustic_model *model,
                          const sgb_bs_store *bs, int32_t *cur_out, int32_t *prev_out,
                          sgb_stream_t stream);
 
-/* Adjoint of sgb_acoustic_forward (PML): boundary-saving reconstruction of
- * the forward wavefield in the interior box + adjoint time stepping + vp
- * gradient, in one fused kernel per step.  Replaces the autograd path of
- * checkpoint_new.py:146-217 with an exact discrete adjoint.
+/* Adjoint of sgb_acoustic_forward (PML or HABC): boundary-saving
+ * reconstruction of the forward wavefield in the interior box + adjoint time
+ * stepping + vp gradient, in one fused kernel per step (PML: TMA tile
+ * pipeline; HABC: a per-cell kernel that also applies the transposed
+ * one-way boundary blend, acoustic_habc.py:79-204; model->vp and
+ * model->damp = the HABC weights are required).  Replaces the autograd path
+ * of checkpoint_new.py:146-217 with an exact discrete adjoint.
  *   ubuf[0..2]: [nshots][nz][pitch]; on entry ubuf[ucur] = U_nt and
  *               ubuf[uprev] = U_{nt-1} (as left by sgb_acoustic_forward);
  *   lbuf[0..2]: [nshots][nz][pitch] adjoint scratch (zeroed here);

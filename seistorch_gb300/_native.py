@@ -21,7 +21,7 @@ LIB_NAME = "libseistorch_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 SOURCES = ["acoustic.cu", "acoustic_stream.cu", "acoustic_stream_fwd.cu", "acoustic_stream_bwd.cu",
            "elastic.cu", "capi.cu", "capi_elastic.cu", "capi_batch.cu", "noalloc.cu",
-           "nn_gemm.cu", "nn_ops.cu", "capi_nn.cu"]
+           "nn_gemm.cu", "nn_ops.cu", "capi_nn.cu", "habc_bwd.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

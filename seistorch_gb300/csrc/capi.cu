@@ -70,6 +70,10 @@ int fwd_tile_rows();
 int bwd_tile_rows();
 int stencil_box_width(int R);
 int set_stream_config(int fwd, int bwd, int zc);
+cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
+                            const Ring& ring, const float* la1, const float* la2, float* lout, const float* uj,
+                            const float* ujm1, float* uout, float* grad, const float* ring_in, int t_src,
+                            const float* resid, cudaStream_t s);
 
 }  // namespace sgb
 
@@ -194,8 +198,8 @@ int sgb_acoustic_step_vjp(const sgb_grid* grid, const sgb_acoustic_model* model,
                           sgb_stream_t stream) {
   if (int e = check_grid(grid)) return e;
   if (int e = check_model(grid, model)) return e;
-  if (model->boundary != 0) return SGB_ERR_UNSUPPORTED;
   if (model->vp == nullptr) return SGB_ERR_ARG;
+  if (model->boundary == 1 && model->damp == nullptr) return SGB_ERR_ARG;
   if (u == nullptr || gy == nullptr || gu == nullptr || gum == nullptr || gvp_acc == nullptr) return SGB_ERR_ARG;
   if (!aligned16(u) || !aligned16(gy) || !aligned16(gu) || !aligned16(gum) || (gh1 && !aligned16(gh1)))
     return SGB_ERR_ALIGN;
@@ -324,8 +328,8 @@ int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model,
   if (int e = check_grid(grid)) return e;
   if (int e = check_model(grid, model)) return e;
   if (int e = check_acq(grid, acq)) return e;
-  if (model->boundary != 0) return SGB_ERR_UNSUPPORTED;
   if (model->vp == nullptr) return SGB_ERR_ARG;
+  if (model->boundary == 1 && model->damp == nullptr) return SGB_ERR_ARG;
   if (bs == nullptr || bs->ring_store == nullptr || ubuf == nullptr || lbuf == nullptr || grad_shot == nullptr ||
       grad_vp == nullptr)
     return SGB_ERR_ARG;
@@ -347,6 +351,39 @@ int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model,
   const int nt = acq->nt;
   const int K = bs->ckpt_every;
   const int nslots = K > 0 ? nt / K : 0;
+  if (model->boundary == 1) {
+    // HABC: per-cell gather kernel (habc_bwd.cu), same buffer rotation
+    if ((acq->nsrc > 0 && acq->src_ptr == nullptr)) return SGB_ERR_ARG;
+    int uj = ucur, ujm1 = uprev, ufree = 3 - ucur - uprev;
+    int l1 = 0, l2 = 1, lfree = 2;
+    for (int j = nt; j >= 2; --j) {
+      const int n = j - 1;
+      const bool ck = K > 0 && n % K == 0 && n / K >= 1 && n / K <= nslots;
+      if (ck && n < nt) {
+        const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
+        SGB_CUDA_CHECK(cudaMemcpyAsync(ubuf[ujm1], slot, field * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      }
+      const float* ring_in = j >= 3 ? bs->ring_store + (long long)(j - 3) * grid->nshots * ring.size : nullptr;
+      const float* resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
+      SGB_CUDA_CHECK(launch_habc_bwd(*grid, *model, *acq, ring, lbuf[l1], lbuf[l2], lbuf[lfree], ubuf[uj],
+                                     ubuf[ujm1], j >= 3 ? ubuf[ufree] : nullptr, grad_shot, ring_in, j - 1, resid, s));
+      if (ck && j >= 3) {
+        const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
+        SGB_CUDA_CHECK(
+            cudaMemcpyAsync(ubuf[ufree], slot + field, field * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      }
+      const int old_uj = uj;
+      uj = ujm1;
+      ujm1 = ufree;
+      ufree = old_uj;
+      const int old_l2 = l2;
+      l2 = l1;
+      l1 = lfree;
+      lfree = old_l2;
+    }
+    SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, model->vp, ring, grad_vp, s));
+    return SGB_OK;
+  }
   // tensor maps: haloed stencil boxes (136 x (TZ+2R)) and point boxes
   // (128 x TZ) of every rotating buffer; lbuf carries nu = k * Lambda
   const int tzr = bwd_tile_rows();

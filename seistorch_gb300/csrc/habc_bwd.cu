@@ -1,0 +1,284 @@
+// Boundary-saving adjoint of the acoustic HABC loop (acoustic_habc.py:79-221).
+//
+// The HABC step is linear in (U_n, U_{n-1}):
+//   y       = 2 U_n - U_{n-1} + k L(U_n)                      (every cell)
+//   out[p]  = (1 - b_p sum_s W_s(p)) y[p] + b_p sum_s W_s(p) one_s(p)
+// where W_s(p) in {0, 1/2, 1} is side s's share of cell p after the mask
+// precedence (top < bottom < left < right) and the 0.5/0.5 corner diagonals
+// (acoustic_habc.py:167-202), and one_s(p) is the one-way extrapolation of
+// side s along its inward normal d at depth k (acoustic_habc.py:79-101):
+//   one = (2-lam-mu) U_n[p] + (lam+2mu) U_n[p+d] - mu U_n[p2]
+//         + (lam-1) U_{n-1}[p] - lam U_{n-1}[p+d],
+//   lam = 2 vp dt / h, mu = vp^2 dt^2 / h^2, p2 = p + 2d, or the line's edge
+//   cell when k = hw - 1 (the reference's roll of the 51-deep slab).
+// The reverse step gathers the transpose for every cell q:
+//   La_j[q] = 2 wi(q) La1(q) + L(k wi La1)(q) - wi(q) La2(q)
+//             + sum_s [one-way transposes of La1 and La2 along side s]
+//             + receiver residuals,         wi = 1 - b sum_s W_s,
+// with La1 = La_{j+1}, La2 = La_{j+2}.  Inside the undamped interior box
+// the forward is the plain update, so the wavefield is reconstructed as in
+// the PML adjoint (U_{j-2} = 2 U_{j-1} - (U_j - S w) + k L(U_{j-1})) and
+// dJ/dvp += La_j (2k / vp) L(U_{j-1}) there; the ring of order/2 cells
+// around the box comes from the forward's store.
+#include "sgb_common.cuh"
+#include "acoustic_args.cuh"
+
+namespace sgb {
+namespace {
+
+struct HabcW {
+  float wi, wt, wb, wl, wr;  // interior share and the four sides' shares times b
+};
+
+// Side shares of cell (z, x): the same predicates as the forward kernel.
+__device__ __forceinline__ HabcW habc_weights(int z, int x, int nz, int nx, int hw, bool mult, float b) {
+  HabcW w{1.f, 0.f, 0.f, 0.f, 0.f};
+  const int dT = z, dB = nz - 1 - z, dL = x, dR = nx - 1 - x;
+  if (!(dT < hw || dB < hw || dL < hw || dR < hw)) return w;
+  const bool top = !mult && dT < hw && dT <= dL && dT <= dR;
+  const bool bot = dB < hw && dB <= dL && dB <= dR;
+  const bool lft = dL < hw && ((mult && z < hw) || ((z >= hw || dL <= z) && (dB >= hw || dL <= dB)));
+  const bool rgt = dR < hw && ((mult && z < hw) || ((z >= hw || dR <= z) && (dB >= hw || dR <= dB)));
+  const bool tl = !mult && z < hw && x == z;
+  const bool tr = !mult && z < hw && x == nx - hw + z;
+  const bool bl = z >= nz - hw && x == z - (nz - hw);
+  const bool br = z >= nz - hw && x == nx - hw + z - (nz - hw);
+  float T = 0.f, B = 0.f, Lf = 0.f, Rt = 0.f;
+  // later assignments win, as in the forward
+  if (top) { T = 1.f; B = Lf = Rt = 0.f; }
+  if (bot) { B = 1.f; T = Lf = Rt = 0.f; }
+  if (lft) { Lf = 1.f; T = B = Rt = 0.f; }
+  if (rgt) { Rt = 1.f; T = B = Lf = 0.f; }
+  if (tl) { T = 0.5f; Lf = 0.5f; B = Rt = 0.f; }
+  if (tr) { T = 0.5f; Rt = 0.5f; B = Lf = 0.f; }
+  if (bl) { B = 0.5f; Lf = 0.5f; T = Rt = 0.f; }
+  if (br) { B = 0.5f; Rt = 0.5f; T = Lf = 0.f; }
+  const float sum = T + B + Lf + Rt;
+  w.wi = 1.f - b * sum;
+  w.wt = b * T;
+  w.wb = b * B;
+  w.wl = b * Lf;
+  w.wr = b * Rt;
+  return w;
+}
+
+struct HabcBwdArgs {
+  int nz, nx, pitch, nshots, hw, multiple, R;
+  long long sstride;
+  const float* __restrict__ la1;   // La_{j+1}
+  const float* __restrict__ la2;   // La_{j+2}
+  float* __restrict__ lout;        // La_j
+  const float* __restrict__ uj;    // U_j
+  const float* __restrict__ ujm1;  // U_{j-1}
+  float* __restrict__ uout;        // U_{j-2}, or null
+  float* __restrict__ grad;        // [nshots][nz][pitch] += La_j k L(U_{j-1}) inside the box
+  const float* __restrict__ k;     // vp^2 dt^2 / h^2
+  const float* __restrict__ vp;
+  const float* __restrict__ hb;    // blend weight b
+  float lamf, muf;                 // 2 dt / h, dt^2 / h^2
+  FdWeights w;
+  Ring ring;
+  const float* __restrict__ ring_in;  // ring of U_{j-2} [nshots][ring.size], or null (zeros)
+  // sources of step j-1 (removed from U_j) and residuals of records j-1
+  const int* __restrict__ src_ptr;
+  const int* __restrict__ src_z;
+  const int* __restrict__ src_x;
+  const int* __restrict__ src_wrow;
+  const float* __restrict__ wavelet;
+  int nt, t_src;
+  const int* __restrict__ rec_row_ptr;
+  const int* __restrict__ rec_x;
+  const int* __restrict__ rec_col;
+  int nch;
+  const float* __restrict__ resid;
+};
+
+__device__ __forceinline__ float ldz(const float* p, int z, int x, int nz, int nx, int pitch) {
+  return (z >= 0 && z < nz && x >= 0 && x < nx) ? __ldg(p + (long long)z * pitch + x) : 0.f;
+}
+
+// One-way transpose of side s at cell q = (z, x): contributions of the
+// strip cells p = q, q - d, q - 2d (and the wrap to the line's edge cell).
+// depth(q) along s is dq; (sz, sx) is the inward step d.
+__device__ __forceinline__ float oneway_t(const HabcBwdArgs& a, const float* l1, const float* l2, int z, int x,
+                                          int dq, int sz, int sx, int side) {
+  const int hw = a.hw;
+  if (dq > hw) return 0.f;
+  const bool mult = a.multiple != 0;
+  float acc = 0.f;
+  auto share = [&](int pz, int px) -> float {
+    const long long o = (long long)pz * a.pitch + px;
+    const HabcW w = habc_weights(pz, px, a.nz, a.nx, hw, mult, __ldg(a.hb + o));
+    return side == 0 ? w.wt : side == 1 ? w.wb : side == 2 ? w.wl : w.wr;
+  };
+  auto coefs = [&](int pz, int px, float& lam, float& mu) {
+    const float c = __ldg(a.vp + (long long)pz * a.pitch + px);
+    lam = c * a.lamf;
+    mu = c * c * a.muf;
+  };
+  // p = q (depth dq)
+  if (dq < hw) {
+    const float ws = share(z, x);
+    if (ws != 0.f) {
+      float lam, mu;
+      coefs(z, x, lam, mu);
+      const long long o = (long long)z * a.pitch + x;
+      acc += ws * ((2.f - lam - mu) * l1[o] + (lam - 1.f) * l2[o]);
+    }
+  }
+  // p = q - d (depth dq - 1): U[p + d] and P[p + d] terms
+  if (dq >= 1 && dq - 1 < hw) {
+    const int pz = z - sz, px = x - sx;
+    const float ws = share(pz, px);
+    if (ws != 0.f) {
+      float lam, mu;
+      coefs(pz, px, lam, mu);
+      const long long o = (long long)pz * a.pitch + px;
+      acc += ws * ((lam + 2.f * mu) * l1[o] - lam * l2[o]);
+    }
+  }
+  // p = q - 2d (depth dq - 2, whose p2 is q when dq - 2 + 2 <= hw)
+  if (dq >= 2 && dq <= hw) {
+    const int pz = z - 2 * sz, px = x - 2 * sx;
+    const float ws = share(pz, px);
+    if (ws != 0.f) {
+      float lam, mu;
+      coefs(pz, px, lam, mu);
+      acc -= ws * mu * l1[(long long)pz * a.pitch + px];
+    }
+  }
+  // wrap: the depth hw-1 cell of this line reads the edge cell (depth 0)
+  if (dq == 0) {
+    const int pz = z + (hw - 1) * sz, px = x + (hw - 1) * sx;
+    if (pz >= 0 && pz < a.nz && px >= 0 && px < a.nx) {
+      const float ws = share(pz, px);
+      if (ws != 0.f) {
+        float lam, mu;
+        coefs(pz, px, lam, mu);
+        acc -= ws * mu * l1[(long long)pz * a.pitch + px];
+      }
+    }
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(256) habc_bwd_kernel(const HabcBwdArgs a) {
+  const long long plane = (long long)a.nz * a.nx;
+  const long long total = plane * a.nshots;
+  const bool mult = a.multiple != 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(i / plane);
+    const long long r = i - (long long)b * plane;
+    const int z = (int)(r / a.nx), x = (int)(r % a.nx);
+    const long long fb = (long long)b * a.sstride;
+    const long long o = (long long)z * a.pitch + x;
+    const float* l1 = a.la1 + fb;
+    const float* l2 = a.la2 + fb;
+    const float kq = __ldg(a.k + o);
+    // interior part: 2 wi La1 + L(k wi La1) - wi La2
+    auto kwl = [&](int zz, int xx) -> float {
+      if (zz < 0 || zz >= a.nz || xx < 0 || xx >= a.nx) return 0.f;
+      const long long oo = (long long)zz * a.pitch + xx;
+      const HabcW w = habc_weights(zz, xx, a.nz, a.nx, a.hw, mult, __ldg(a.hb + oo));
+      return __ldg(a.k + oo) * w.wi * l1[oo];
+    };
+    const HabcW wq = habc_weights(z, x, a.nz, a.nx, a.hw, mult, __ldg(a.hb + o));
+    float lap = a.w.c[0] * kq * wq.wi * l1[o];
+    for (int j = 1; j <= a.R; ++j)
+      lap += a.w.c[j] * (kwl(z - j, x) + kwl(z + j, x) + kwl(z, x - j) + kwl(z, x + j));
+    float v = 2.f * wq.wi * l1[o] + lap - wq.wi * l2[o];
+    // one-way parts of the four sides
+    v += oneway_t(a, l1, l2, z, x, z, 1, 0, 0);
+    v += oneway_t(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
+    v += oneway_t(a, l1, l2, z, x, x, 0, 1, 2);
+    v += oneway_t(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
+    // residuals of the records of step j-1 (they sample U_j)
+    if (a.resid != nullptr) {
+      const int* rp = a.rec_row_ptr + (long long)b * a.nz;
+      int lo = rp[z], hi = rp[z + 1];  // receivers of the row, sorted by column
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a.rec_x[mid] < x) lo = mid + 1; else hi = mid;
+      }
+      for (int q = lo; q < rp[z + 1] && a.rec_x[q] == x; ++q) v += a.resid[(long long)a.rec_col[q] * a.nch];
+    }
+    a.lout[fb + o] = v;
+    // gradient and reconstruction inside the undamped box
+    const bool inbox = a.ring.inside(z, x);
+    if (inbox || a.uout != nullptr) {
+      const float* u1 = a.ujm1 + fb;
+      float L = a.w.c[0] * u1[o];
+      for (int j = 1; j <= a.R; ++j)
+        L += a.w.c[j] * (ldz(u1, z - j, x, a.nz, a.nx, a.pitch) + ldz(u1, z + j, x, a.nz, a.nx, a.pitch) +
+                         ldz(u1, z, x - j, a.nz, a.nx, a.pitch) + ldz(u1, z, x + j, a.nz, a.nx, a.pitch));
+      if (inbox) a.grad[fb + o] += v * kq * L;  // times 2 / vp in the shot reduction
+      if (a.uout != nullptr) {
+        float u = 0.f;
+        if (inbox) {
+          float ujv = a.uj[fb + o];
+          if (a.src_ptr != nullptr) {
+            for (int q = a.src_ptr[b]; q < a.src_ptr[b + 1]; ++q)
+              if (a.src_z[q] == z && a.src_x[q] == x) ujv -= a.wavelet[(long long)a.src_wrow[q] * a.nt + a.t_src];
+          }
+          u = 2.f * u1[o] - ujv + kq * L;
+        } else {
+          const int ri = a.ring.index(z, x);
+          if (ri >= 0 && a.ring_in != nullptr) u = a.ring_in[(long long)b * a.ring.size + ri];
+        }
+        a.uout[fb + o] = u;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
+                            const Ring& ring, const float* la1, const float* la2, float* lout, const float* uj,
+                            const float* ujm1, float* uout, float* grad, const float* ring_in, int t_src,
+                            const float* resid, cudaStream_t s) {
+  HabcBwdArgs a;
+  a.nz = g.nz;
+  a.nx = g.nx;
+  a.pitch = g.pitch;
+  a.nshots = g.nshots;
+  a.hw = m.habc_width;
+  a.multiple = m.multiple;
+  a.R = m.order / 2;
+  a.sstride = (long long)g.nz * g.pitch;
+  a.la1 = la1;
+  a.la2 = la2;
+  a.lout = lout;
+  a.uj = uj;
+  a.ujm1 = ujm1;
+  a.uout = uout;
+  a.grad = grad;
+  a.k = m.coef + (long long)g.nz * g.pitch;
+  a.vp = m.vp;
+  a.hb = m.damp;
+  a.lamf = 2.f * g.dt / g.h;
+  a.muf = (g.dt * g.dt) / (g.h * g.h);
+  a.w = fd_weights(m.order);
+  a.ring = ring;
+  a.ring_in = ring_in;
+  a.src_ptr = q.nsrc > 0 ? q.src_ptr : nullptr;
+  a.src_z = q.src_z;
+  a.src_x = q.src_x;
+  a.src_wrow = q.src_wrow;
+  a.wavelet = q.wavelet;
+  a.nt = q.nt;
+  a.t_src = t_src;
+  a.rec_row_ptr = q.rec_row_ptr;
+  a.rec_x = q.rec_x;
+  a.rec_col = q.rec_col;
+  a.nch = q.nch;
+  a.resid = resid;
+  const long long total = (long long)g.nz * g.nx * g.nshots;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  habc_bwd_kernel<<<(unsigned)blocks, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace sgb

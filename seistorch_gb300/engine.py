@@ -231,8 +231,6 @@ class AcousticPropagator:
         state = AcousticState()
         bs_struct = None
         if save_for_adjoint:
-            if self.boundary != BOUNDARY_PML:
-                raise NotImplementedError("the boundary-saving adjoint covers the PML acoustic equation")
             iz0, iz1, ix0, ix1 = interior_box(self.nz, self.nx, self.bwidth, self.multiple)
             if iz1 <= iz0 or ix1 <= ix0:
                 raise ValueError("grid too small for its boundary width")

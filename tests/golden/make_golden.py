@@ -150,6 +150,13 @@ def cases():
                                              grad=["vp"], obs_models=None)
     C["grad_acoustic_pml_o8_zeroobs"] = dict(equation="acoustic", models_int=a, order=8, nt=150,
                                              grad=["vp"], obs_models=None)
+    C["grad_acoustic_habc_o2_zeroobs"] = dict(equation="acoustic_habc", models_int=ah, order=2, width=50,
+                                              habc=True, nt=200, grad=["vp"], obs_models=None)
+    C["grad_acoustic_habc_o4_zeroobs"] = dict(equation="acoustic_habc", models_int=ah, order=4, width=50,
+                                              habc=True, nt=200, grad=["vp"], obs_models=None)
+    C["grad_acoustic_habc_o2_multiple_zeroobs"] = dict(equation="acoustic_habc", models_int=ah, order=2,
+                                                       width=50, habc=True, multiple=True, nt=200, grad=["vp"],
+                                                       obs_models=None)
     C["grad_elastic_zeroobs"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,
                                      nt=200, grad=["vp", "vs", "rho"], obs_models=None)
     C["grad_elastic"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,

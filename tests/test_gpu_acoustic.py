@@ -193,3 +193,24 @@ def test_forward_config1_size_vs_fp64_oracle(dev):
     err = rel_l2(got, want)
     print(f"config-1 records rel L2 vs fp64 oracle: {err:.3e}")
     assert err < 1e-5
+
+
+@pytest.mark.parametrize("name", ["grad_acoustic_habc_o2_zeroobs", "grad_acoustic_habc_o4_zeroobs",
+                                  "grad_acoustic_habc_o2_multiple_zeroobs"])
+@pytest.mark.parametrize("ckpt", [0, 25])
+def test_habc_gradient_matches_reference_autograd(dev, name, ckpt):
+    """HABC (acoustic_habc.py): the boundary-saving adjoint with the exact
+    transposed one-way blend vs the reference's autograd gradient, inside
+    the undamped box (rows from 0 with ``multiple``); 0 outside."""
+    g = load(name)
+    vp, rec, per_shot = _forward(g, dev, requires_grad=True, ckpt=ckpt)
+    loss = (per_shot ** 2).sum()
+    loss.backward()
+    assert abs(loss.item() - float(g["loss"])) < 1e-5 * float(g["loss"])
+    w = g["width"]
+    box = (slice(0 if g["multiple"] else w, -w), slice(w, -w))
+    got = vp.grad.cpu().numpy()
+    assert rel_l2(got[box], g["grad_vp"][box]) < 1e-4
+    mask = np.ones_like(got, bool)
+    mask[box] = False
+    assert np.all(got[mask] == 0)
