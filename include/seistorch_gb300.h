@@ -110,8 +110,9 @@ int sgb_device_status(int *out, int reset);
 
 /* Select the tile-pipeline variant used by later PML calls (host-only,
  * process-wide): fwd_cfg in [0, 6) and bwd_cfg in [0, 4) index the compiled
- * (rows per tile, warps per CTA, pipeline stages) variants; `reserved` must
- * be 0.  The autotuner (seistorch_gb300.tuning) times the variants per grid. */
+ * (rows per tile, warps per CTA, pipeline stages) variants;
+ * `reserved` must be 0.  The autotuner (seistorch_gb300.tuning) times the
+ * variants per grid. */
 int sgb_set_stream_config(int32_t fwd_cfg, int32_t bwd_cfg, int32_t reserved);
 
 /* Floats per shot per step of the boundary ring (host-only helper). */

@@ -36,11 +36,12 @@ int make_tmap_f32(CUtensorMap* map, const float* base, int rank, const uint64_t*
   return r == CUDA_SUCCESS ? 0 : -2;
 }
 
-// Tensor maps of a [nshots][nz][pitch] field with a given box width.
-int field_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int nshots, int boxw, int rb) {
+// Tensor maps of a [nshots][nz][pitch] field with a box of boxw columns,
+// rb rows and bs shots.
+int field_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int nshots, int boxw, int rb, int bs) {
   const uint64_t dims[3] = {(uint64_t)nx, (uint64_t)nz, (uint64_t)nshots};
   const uint64_t st[2] = {(uint64_t)pitch * 4, (uint64_t)nz * pitch * 4};
-  const uint32_t box[3] = {(uint32_t)boxw, (uint32_t)rb, 1};
+  const uint32_t box[3] = {(uint32_t)boxw, (uint32_t)rb, (uint32_t)bs};
   return make_tmap_f32(m, p, 3, dims, st, box);
 }
 int coef_map(CUtensorMap* m, const float* coef, int nz, int nx, int pitch, int rb) {

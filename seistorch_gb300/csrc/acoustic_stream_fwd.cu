@@ -8,14 +8,18 @@ namespace sgb {
 
 // PT: the previous field travels through the TMA stage (prefetched S-1
 // tiles ahead) instead of a global load issued before the stage wait.
-template <int R, int TZ, int S, bool PT>
+// SB: shots per tile; one TMA box carries all SB shots (shot is the box's
+// third dimension), the coefficient rows and the tile's barrier are shared.
+template <int R, int TZ, int S, bool PT, int SB = 1>
 struct FwdTileLayout {
   static constexpr int UW = Row<R>::W;
   static constexpr int UROWS = TZ + 2 * R;
-  static constexpr int UF = round32(UROWS * UW);
-  static constexpr int STAGE = UF + (PT ? TZ * TX : 0);
+  static constexpr int USHOT = UROWS * UW;  // floats of one shot's stencil box
+  static constexpr int UF = round32(SB * USHOT);
+  static constexpr int PSHOT = TZ * TX;
+  static constexpr int STAGE = UF + (PT ? SB * PSHOT : 0);
   static constexpr size_t BYTES = (size_t)S * STAGE * 4 + S * 8;
-  static constexpr uint32_t TX_BYTES = (UROWS * UW + (PT ? TZ * TX : 0)) * 4;
+  static constexpr uint32_t TX_BYTES = (SB * USHOT + (PT ? SB * PSHOT : 0)) * 4;
 };
 
 // Tile providers: the single-grid kernel takes its tensor maps and argument
@@ -23,11 +27,12 @@ struct FwdTileLayout {
 // bank); the batch kernel covers every tile of up to MAXG grids (an uneven
 // batch: each group has its own shape, shots, buffers and step), tiles
 // numbered group after group from tile0[g].
+template <int SB>
 struct FwdOne {
   const CUtensorMap* tu;
   const CUtensorMap* tum;
   AcStreamArgs a;
-  __device__ __forceinline__ int ntiles() const { return a.nshots * a.ntx * a.nzc; }
+  __device__ __forceinline__ int ntiles() const { return (a.nshots + SB - 1) / SB * a.ntx * a.nzc; }
   __device__ __forceinline__ int group(int) const { return 0; }
   __device__ __forceinline__ int first(int) const { return 0; }
   __device__ __forceinline__ const AcStreamArgs& args(int) const { return a; }
@@ -52,9 +57,10 @@ struct FwdMany {
 
 // per group: map_u = U_n [nshots][nz][nx], box {W, TZ+2R, 1};
 //            map_um = U_{n-1}, box {128, TZ, 1} (used when PT)
-template <int R, int TZ, int NWP, int S, bool PT, class P>
+template <int R, int TZ, int NWP, int S, bool PT, int SB, class P>
 __device__ __forceinline__ void fwd_tiles(const P& prov) {
-  using Lay = FwdTileLayout<R, TZ, S, PT>;
+  static_assert(SB == 1 || PT, "several shots per tile need the previous field in the stage");
+  using Lay = FwdTileLayout<R, TZ, S, PT, SB>;
   constexpr int RPW = TZ / NWP;
   constexpr int UW = Lay::UW, LO = Row<R>::LO;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -68,11 +74,12 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
   auto issue = [&](int t, int stage) {
     const int gi = prov.group(t);
     const AcStreamArgs& a = prov.args(gi);
-    const Tile g = tile_geom(t - prov.first(gi), a.nshots, a.ntx, TZ);
+    const Tile g = tile_geom(t - prov.first(gi), (a.nshots + SB - 1) / SB, a.ntx, TZ);
     fence_proxy_async_smem();
     mbar_arrive_expect_tx(&bars[stage], Lay::TX_BYTES);
-    tma_load_3d(smem + stage * Lay::STAGE, prov.map_u(gi), g.x0 - LO, g.z0 - R, g.b, &bars[stage]);
-    if (PT) tma_load_3d(smem + stage * Lay::STAGE + Lay::UF, prov.map_um(gi), g.x0, g.z0, g.b, &bars[stage]);
+    tma_load_3d(smem + stage * Lay::STAGE, prov.map_u(gi), g.x0 - LO, g.z0 - R, g.b * SB, &bars[stage]);
+    if (PT)
+      tma_load_3d(smem + stage * Lay::STAGE + Lay::UF, prov.map_um(gi), g.x0, g.z0, g.b * SB, &bars[stage]);
   };
   if (tid == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
@@ -87,86 +94,101 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
     const int stage = k % S;
     const int gi = prov.group(t);
     const AcStreamArgs& a = prov.args(gi);
-    const Tile g = tile_geom(t - prov.first(gi), a.nshots, a.ntx, TZ);
+    const Tile g = tile_geom(t - prov.first(gi), (a.nshots + SB - 1) / SB, a.ntx, TZ);
     const int x = g.x0 + 4 * lane;
     const bool xin = x < a.nx;
     const int zw = g.z0 + wid * RPW;  // first row of this warp
-    // point operands of this warp's rows, issued before the stage wait
+    const int b0 = g.b * SB;          // first shot of the tile
+    // point operands of this warp's rows, issued before the stage wait (the
+    // coefficient rows serve every shot of the tile)
     float4 vm[RPW], vg[RPW], vk[RPW];
-    const long long fbase = (long long)g.b * a.sstride;
 #pragma unroll
     for (int i = 0; i < RPW; ++i) {
       const int z = zw + i;
       if (xin && z < a.nz) {
         const long long mo = (long long)z * a.pitch + x;
-        if (!PT) vm[i] = ldg4(a.um + fbase + mo);
+        if (!PT) vm[i] = ldg4(a.um + (long long)b0 * a.sstride + mo);
         vg[i] = ldg4(a.g + mo);
         vk[i] = ldg4(a.k + mo);
       } else {
         vm[i] = vg[i] = vk[i] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
-    WarpSrc src{0u, -1, 0, 0.f};
-    if (a.src_ptr != nullptr) {
-      const int2 zr = __ldg(reinterpret_cast<const int2*>(a.src_zr) + g.b);
-      if (zr.x < zw + RPW && zr.y > zw)
-        src = warp_sources(lane, g.b, zw, RPW, g.x0, a.src_ptr, a.src_z, a.src_x, a.src_wrow, a.wavelet, a.nt,
-                           a.t, a.status);
-    }
-    bool has_rec = false;
+    unsigned rec_shots = 0;  // bit sb: shot b0 + sb has receivers in this band
     if (a.records != nullptr) {
-      const int2 zr = __ldg(reinterpret_cast<const int2*>(a.rec_zr) + g.b);
-      has_rec = zr.x < g.z0 + TZ && zr.y > g.z0;
+#pragma unroll
+      for (int sb = 0; sb < SB; ++sb) {
+        if (b0 + sb >= a.nshots) break;
+        const int2 zr = __ldg(reinterpret_cast<const int2*>(a.rec_zr) + b0 + sb);
+        if (zr.x < g.z0 + TZ && zr.y > g.z0) rec_shots |= 1u << sb;
+      }
     }
     if (!mbar_wait(&bars[stage], (k / S) & 1, a.status)) s_abort = 1;
     const float* st = smem + stage * Lay::STAGE;
     const bool ring_tile = a.ring_out != nullptr && a.ring.touches(g.z0, TZ, g.x0, TX);
     const int lr0 = wid * RPW;
-    if (PT) {
 #pragma unroll
-      for (int i = 0; i < RPW; ++i) vm[i] = lds4(st + Lay::UF + (lr0 + i) * TX + 4 * lane);
-    }
-    float4 win[2 * R + 1];
+    for (int sb = 0; sb < SB; ++sb) {
+      const int b = b0 + sb;
+      if (b >= a.nshots) break;
+      const long long fbase = (long long)b * a.sstride;
+      const float* su = st + sb * Lay::USHOT;
+      if (PT) {
 #pragma unroll
-    for (int j = 0; j < 2 * R; ++j) win[j] = lds4(st + (lr0 + j) * UW + LO + 4 * lane);
-    float* outp = a.un + fbase + (long long)zw * a.pitch + x;
+        for (int i = 0; i < RPW; ++i) vm[i] = lds4(st + Lay::UF + sb * Lay::PSHOT + (lr0 + i) * TX + 4 * lane);
+      }
+      WarpSrc src{0u, -1, 0, 0.f};
+      if (a.src_ptr != nullptr) {
+        const int2 zr = __ldg(reinterpret_cast<const int2*>(a.src_zr) + b);
+        if (zr.x < zw + RPW && zr.y > zw)
+          src = warp_sources(lane, b, zw, RPW, g.x0, a.src_ptr, a.src_z, a.src_x, a.src_wrow, a.wavelet, a.nt,
+                             a.t, a.status);
+      }
+      float4 win[2 * R + 1];
 #pragma unroll
-    for (int i = 0; i < RPW; ++i) {
-      const int lr = lr0 + i;
-      const int z = zw + i;
-      win[2 * R] = lds4(st + (lr + 2 * R) * UW + LO + 4 * lane);
-      const float4 L = lap_row<R>(win, st + (lr + R) * UW, lane, a.w);
-      const float4 c = win[R];
-      float4 y;
-      y.x = fmaf(vk[i].x, L.x, fmaf(vg[i].x, c.x - vm[i].x, vm[i].x));
-      y.y = fmaf(vk[i].y, L.y, fmaf(vg[i].y, c.y - vm[i].y, vm[i].y));
-      y.z = fmaf(vk[i].z, L.z, fmaf(vg[i].z, c.z - vm[i].z, vm[i].z));
-      y.w = fmaf(vk[i].w, L.w, fmaf(vg[i].w, c.w - vm[i].w, vm[i].w));
-      if (src.mask) apply_sources(src, i, lane, 1.f, y);
-      if (z < a.nz && xin) {
-        *reinterpret_cast<float4*>(outp) = y;
-        if (ring_tile) {
+      for (int j = 0; j < 2 * R; ++j) win[j] = lds4(su + (lr0 + j) * UW + LO + 4 * lane);
+      float* outp = a.un + fbase + (long long)zw * a.pitch + x;
 #pragma unroll
-          for (int m = 0; m < 4; ++m) {
-            const int ri = (x + m < a.nx) ? a.ring.index(z, x + m) : -1;
-            if (ri >= 0) a.ring_out[(long long)g.b * a.ring.size + ri] = comp(y, m);
+      for (int i = 0; i < RPW; ++i) {
+        const int lr = lr0 + i;
+        const int z = zw + i;
+        win[2 * R] = lds4(su + (lr + 2 * R) * UW + LO + 4 * lane);
+        const float4 L = lap_row<R>(win, su + (lr + R) * UW, lane, a.w);
+        const float4 c = win[R];
+        float4 y;
+        y.x = fmaf(vk[i].x, L.x, fmaf(vg[i].x, c.x - vm[i].x, vm[i].x));
+        y.y = fmaf(vk[i].y, L.y, fmaf(vg[i].y, c.y - vm[i].y, vm[i].y));
+        y.z = fmaf(vk[i].z, L.z, fmaf(vg[i].z, c.z - vm[i].z, vm[i].z));
+        y.w = fmaf(vk[i].w, L.w, fmaf(vg[i].w, c.w - vm[i].w, vm[i].w));
+        if (src.mask) apply_sources(src, i, lane, 1.f, y);
+        if (z < a.nz && xin) {
+          *reinterpret_cast<float4*>(outp) = y;
+          if (ring_tile) {
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+              const int ri = (x + m < a.nx) ? a.ring.index(z, x + m) : -1;
+              if (ri >= 0) a.ring_out[(long long)b * a.ring.size + ri] = comp(y, m);
+            }
+          }
+          if (a.illum != nullptr) {
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+              if (x + m < a.nx) atomicAdd(a.illum + (long long)z * a.pitch + x + m, comp(y, m) * comp(y, m));
           }
         }
-        if (a.illum != nullptr) {
+        outp += a.pitch;
 #pragma unroll
-          for (int m = 0; m < 4; ++m)
-            if (x + m < a.nx) atomicAdd(a.illum + (long long)z * a.pitch + x + m, comp(y, m) * comp(y, m));
-        }
+        for (int j = 0; j < 2 * R; ++j) win[j] = win[j + 1];
       }
-      outp += a.pitch;
-#pragma unroll
-      for (int j = 0; j < 2 * R; ++j) win[j] = win[j + 1];
     }
     // stage free; this tile's outputs visible to the CTA; abort is uniform
     if (__syncthreads_or(s_abort)) break;
     if (tid == 0 && t + S * G < ntiles) issue(t + S * G, stage);
-    if (has_rec) {
-      const int* rp = a.rec_row_ptr + (long long)g.b * a.nz;
+    for (int sb = 0; sb < SB; ++sb) {
+      if (!(rec_shots & (1u << sb))) continue;
+      const int b = b0 + sb;
+      const long long fbase = (long long)b * a.sstride;
+      const int* rp = a.rec_row_ptr + (long long)b * a.nz;
       for (int lr = wid; lr < TZ && g.z0 + lr < a.nz; lr += NWP) {
         const int z = g.z0 + lr;
         const int p1 = rp[z + 1];
@@ -184,42 +206,44 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
       if ((int)blockIdx.x + q * G < ntiles) mbar_wait(&bars[q % S], (q / S) & 1, nullptr);
 }
 
-template <int R, int TZ, int NWP, int S, bool PT>
+template <int R, int TZ, int NWP, int S, bool PT, int SB>
 __global__ void __launch_bounds__(32 * NWP) acoustic_fwd_tile_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                                      const __grid_constant__ CUtensorMap tm_um,
                                                                      const AcStreamArgs a) {
-  fwd_tiles<R, TZ, NWP, S, PT>(FwdOne{&tm_u, &tm_um, a});
+  fwd_tiles<R, TZ, NWP, S, PT, SB>(FwdOne<SB>{&tm_u, &tm_um, a});
 }
 
 template <int R, int TZ, int NWP, int S, bool PT, int MAXG>
 __global__ void __launch_bounds__(32 * NWP) acoustic_fwd_batch_kernel(const __grid_constant__ AcFwdBatch<MAXG> B) {
-  fwd_tiles<R, TZ, NWP, S, PT>(FwdMany<MAXG>{B});
+  fwd_tiles<R, TZ, NWP, S, PT, 1>(FwdMany<MAXG>{B});
 }
 
 // ------------------------------------------------------------- launch ---
 
 struct FwdCfg {
-  int tz, nwp, s;
+  int tz, nwp, s, sb;
 };
-static const FwdCfg FWD_TILE_CFGS[] = {{16, 4, 3}, {16, 4, 3}, {8, 4, 4}, {32, 8, 2}, {16, 4, 2}, {8, 4, 3}};
+static const FwdCfg FWD_TILE_CFGS[] = {{16, 4, 3, 1}, {16, 4, 3, 1}, {8, 4, 4, 1},
+                                       {32, 8, 2, 1}, {16, 4, 2, 1}, {8, 4, 3, 1}};
 
 // Launches the variant on batch b; with s == nullptr and prepare_only it
 // only sets the kernel's shared-memory attribute (done once per variant, and
 // before any stream capture).
-template <int R, int TZ, int NWP, int S, bool PT, int MAXG>
+template <int R, int TZ, int NWP, int S, bool PT, int MAXG, int SB = 1>
 static cudaError_t fwd_tile_t(const AcFwdBatch<MAXG>& b, cudaStream_t s, bool prepare_only) {
-  using Lay = FwdTileLayout<R, TZ, S, PT>;
+  using Lay = FwdTileLayout<R, TZ, S, PT, MAXG == 1 ? SB : 1>;
   const size_t smem = Lay::BYTES + 128;  // + alignment slack
   static int blocks = 0;
   if constexpr (MAXG == 1) {
-    auto kern = acoustic_fwd_tile_kernel<R, TZ, NWP, S, PT>;
+    auto kern = acoustic_fwd_tile_kernel<R, TZ, NWP, S, PT, SB>;
     if (blocks == 0) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
       blocks = resident_blocks(kern, 32 * NWP, smem);
     }
     if (prepare_only) return cudaSuccess;
-    const int tiles = b.tile0[b.ngroups];
+    const AcStreamArgs& a = b.g[0];
+    const int tiles = (a.nshots + SB - 1) / SB * a.ntx * a.nzc;
     if (tiles <= 0) return cudaSuccess;
     kern<<<(unsigned)(tiles < blocks ? tiles : blocks), 32 * NWP, smem, s>>>(b.tm_u[0], b.tm_um[0], b.g[0]);
   } else {
@@ -262,6 +286,7 @@ static cudaError_t fwd_dispatch(int R, const AcFwdBatch<MAXG>& b, cudaStream_t s
 }
 
 int fwd_tile_rows() { return FWD_TILE_CFGS[g_fwd_cfg].tz; }
+int fwd_tile_shots() { return FWD_TILE_CFGS[g_fwd_cfg].sb; }
 int stencil_box_width(int R) { return (R % 2 == 0) ? TX + 8 : TX + 16; }
 
 cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s) {

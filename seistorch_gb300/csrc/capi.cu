@@ -63,10 +63,12 @@ int pick_tz(int nz, int nx, int nshots, int tz_max);
 cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s);
 cudaError_t launch_acoustic_bwd_stream(int R, const CUtensorMap* maps, const AcBwdStreamArgs& a,
                                        cudaStream_t s);
-int field_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int nshots, int boxw, int rb);
+int field_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int nshots, int boxw, int rb,
+              int bs = 1);
 int coef_map(CUtensorMap* m, const float* coef, int nz, int nx, int pitch, int rb);
 int plane_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int boxw, int rb);
 int fwd_tile_rows();
+int fwd_tile_shots();
 int bwd_tile_rows();
 int stencil_box_width(int R);
 int set_stream_config(int fwd, int bwd, int zc);
@@ -263,10 +265,11 @@ int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, 
   std::memset(&sa, 0, sizeof(sa));
   if (!habc) {
     const int tzr = fwd_tile_rows();
+    const int tsb = fwd_tile_shots();
     const int bw = stencil_box_width(R);
     for (int i = 0; i < 3; ++i)
-      if (field_map(&mu[i], buf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R) ||
-          field_map(&mum[i], buf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr))
+      if (field_map(&mu[i], buf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R, tsb) ||
+          field_map(&mum[i], buf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr, tsb))
         return SGB_ERR_CUDA;
     sa.nz = a.nz; sa.nx = a.nx; sa.pitch = a.pitch; sa.nshots = a.nshots; sa.ntx = a.ntx;
     sa.zc = tzr;

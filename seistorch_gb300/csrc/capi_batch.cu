@@ -11,7 +11,8 @@
 
 namespace sgb {
 FdWeights fd_weights(int order);
-int field_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int nshots, int boxw, int rb);
+int field_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int nshots, int boxw, int rb,
+              int bs = 1);
 int fwd_tile_rows();
 int stencil_box_width(int R);
 cudaError_t launch_acoustic_fwd_batch(int R, const AcFwdBatch<MAX_BATCH_GROUPS>& b, cudaStream_t s);

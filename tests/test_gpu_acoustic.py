@@ -214,3 +214,22 @@ def test_habc_gradient_matches_reference_autograd(dev, name, ckpt):
     mask = np.ones_like(got, bool)
     mask[box] = False
     assert np.all(got[mask] == 0)
+
+
+def test_every_forward_variant_gives_the_same_records(dev):
+    """All compiled tile-pipeline variants (rows per tile, warps, stages,
+    previous field via TMA) compute the same arithmetic: identical records,
+    within 1e-5 of the reference."""
+    from seistorch_gb300 import tuning
+    g = load("acoustic_pml_o8")
+    outs = []
+    try:
+        for cfg in range(len(tuning.FWD_VARIANTS)):
+            tuning.select(cfg, 0)
+            _, _, rec = _forward(g, dev)
+            outs.append(rec.detach().cpu().numpy())
+    finally:
+        tuning.select(*tuning.DEFAULT)
+    for o in outs:
+        assert np.array_equal(o, outs[0])
+    assert rel_l2(outs[0], g["records"]) < 1e-5
