@@ -188,7 +188,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="acoustic_gradient",
-                    choices=["acoustic_gradient", "elastic_gradient", "uneven_forward", "learned_fwi"],
+                    choices=["acoustic_gradient", "elastic_gradient", "uneven_forward", "learned_fwi", "learned_net"],
                     help="acoustic_gradient (default, the headline line); elastic_gradient: 300x800 + 50 PML "
                          "elastic forward+adjoint; uneven_forward: 4 grid sizes x 64 shots in one launch per step")
     ap.add_argument("--pairs", type=int, default=2000, help="learned_fwi: training pairs")
@@ -198,6 +198,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "learned_fwi":
         return bench_learned(args)
+    if args.workload == "learned_net":
+        return bench_net(args)
     if args.workload == "elastic_gradient":
         return bench_elastic(args)
     if args.workload == "uneven_forward":
@@ -599,6 +601,51 @@ def conv_flops(B, H, W):
     res = {"e1a": 0, "e1b": 0, "e2a": 1, "e2b": 1, "e3a": 2, "e3b": 2, "b4": 3, "d3": 2, "d2": 1, "d1": 0,
            "out": 0}
     return sum(2.0 * B * (H >> res[n]) * (W >> res[n]) * ci * co * 9 for n, ci, co, _ in LAYERS)
+
+
+def bench_net(args):
+    """Tensor-core throughput of the preconditioner network alone: forward and
+    one training step (forward + backward + Adam) on a batch of 8 random
+    2 x 256 x 512 inputs."""
+    import torch
+    from seistorch_gb300 import _native
+    from seistorch_gb300.learned import PrecondNet
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _native.load(build_if_missing=False)
+    torch.manual_seed(0)
+    x = torch.randn(8, 2, 256, 512, device=dev)
+    y = torch.randn(8, 256, 512, device=dev) * 0.1
+    net = PrecondNet(dev, seed=0)
+    for _ in range(args.warmup):
+        net.train_batch(x, y, 1e-4)
+    torch.cuda.synchronize()
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    a, b, c = ev(), ev(), ev()
+    a.record()
+    for _ in range(args.steps):
+        net.forward(x)
+    b.record()
+    for _ in range(args.steps):
+        net.train_batch(x, y, 1e-4)
+    c.record()
+    torch.cuda.synchronize()
+    fwd = a.elapsed_time(b) / args.steps
+    step = b.elapsed_time(c) / args.steps
+    fl = conv_flops(8, 256, 512)
+    peak = None
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            peak = json.load(f).get("bf16_tflops")
+    t_f = fl / (fwd * 1e-3) / 1e12
+    print(json.dumps({"metric": "network TFLOP/s (forward)", "value": t_f, "unit": "TFLOP/s", "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "bf16/fp32acc",
+                      "data": "synthetic", "config": {"workload": "precond_unet_b8_256x512"},
+                      "forward_ms": fwd, "train_step_ms": step, "train_tflops": 3 * fl / (step * 1e-3) / 1e12,
+                      "roofline": {"bound": "tensor", "achieved": t_f, "peak": peak, "unit": "TFLOP/s",
+                                   "frac": t_f / peak if peak else None}}))
+    return 0
 
 
 def bench_learned(args):
