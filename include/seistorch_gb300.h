@@ -315,6 +315,36 @@ int sgb_elastic_gradient(const sgb_grid *grid, const sgb_elastic_model *model, c
                          const float *vp, const float *vs, const float *rho, const sgb_bs_store *bs, int32_t box,
                          float *const grad_out[3], sgb_stream_t stream);
 
+/* ------------------------------------------- misfit and post-processing --- */
+
+/* L2 misfit of MSELoss(reduction='sum') summed over shots (loss.py:409-421):
+ * *loss (device double, accumulated) += sum (syn - obs)^2 and, if resid is
+ * not NULL, resid = 2 (syn - obs), the adjoint source. */
+int sgb_l2_misfit(int64_t n, const float *syn, const float *obs, float *resid, double *loss,
+                  sgb_stream_t stream);
+
+/* out = grad (* mask) / (illum + eps) on [nz][pitch] planes (illum and mask
+ * may be NULL): the gradient cut of process.py:43-47 and the illumination
+ * preconditioning of process.py:115-118 (eps = 0 is the reference's plain
+ * division); padding columns are written as 0. */
+int sgb_grad_precondition(int32_t nz, int32_t nx, int32_t pitch, const float *grad, const float *illum,
+                          float eps, const float *mask, float *out, sgb_stream_t stream);
+
+/* `counts` passes of separable Gaussian smoothing, along z then x, in place
+ * on grad (tmp: scratch of the same [nz][pitch] shape).  weights_* hold
+ * 2 radius + 1 normalised taps; the boundary is numpy's 'reflect' padding
+ * (signal.py:247-319, process.py:66-113). */
+int sgb_grad_smooth(int32_t nz, int32_t nx, int32_t pitch, const float *weights_z, int32_t radius_z,
+                    const float *weights_x, int32_t radius_x, int32_t counts, float *grad, float *tmp,
+                    sgb_stream_t stream);
+
+/* Steepest-descent step (optimizer.py:124-142): d = grad, clamped to
+ * [lo, hi] when clamp != 0 (the reference's 2 % / 98 % quantiles, computed
+ * by the caller), then param -= lr * d / max|d|.  scratch: one device
+ * uint32. */
+int sgb_sd_step(int64_t n, float *param, const float *grad, float lr, int32_t clamp, float lo, float hi,
+                uint32_t *scratch, sgb_stream_t stream);
+
 /* --------------------------------------------- learned preconditioner --- */
 /* BF16-weight / FP32-accumulate kernels of the convolutional gradient
  * preconditioner (no counterpart in the reference, which preconditions by

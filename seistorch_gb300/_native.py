@@ -21,7 +21,7 @@ LIB_NAME = "libseistorch_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 SOURCES = ["acoustic.cu", "acoustic_stream.cu", "acoustic_stream_fwd.cu", "acoustic_stream_bwd.cu",
            "elastic.cu", "capi.cu", "capi_elastic.cu", "capi_batch.cu", "noalloc.cu",
-           "nn_gemm.cu", "nn_ops.cu", "capi_nn.cu", "habc_bwd.cu"]
+           "nn_gemm.cu", "nn_ops.cu", "capi_nn.cu", "habc_bwd.cu", "postproc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -175,6 +175,11 @@ SIGNATURES = {
     "sgb_nn_adam": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_f32, c_f32, c_f32, c_f32, c_i32,
                                    c_f32, c_ptr]),
     "sgb_nn_mse": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr]),
+    "sgb_l2_misfit": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr]),
+    "sgb_grad_precondition": (ctypes.c_int, [c_i32, c_i32, c_i32, c_ptr, c_ptr, c_f32, c_ptr, c_ptr, c_ptr]),
+    "sgb_grad_smooth": (ctypes.c_int, [c_i32, c_i32, c_i32, c_ptr, c_i32, c_ptr, c_i32, c_i32, c_ptr, c_ptr,
+                                       c_ptr]),
+    "sgb_sd_step": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_f32, c_i32, c_f32, c_f32, c_ptr, c_ptr]),
     "sgb_elastic_coefficients": (ctypes.c_int, [ctypes.POINTER(Grid), c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                                                 c_ptr]),
     "sgb_elastic_step": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ElasticModel), PTR5, PTR5,

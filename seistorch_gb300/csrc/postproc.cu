@@ -1,0 +1,147 @@
+// Device kernels around the hot path for the plain FWI baseline: the L2
+// misfit with its adjoint source (loss.py:409-421), illumination
+// preconditioning and gradient masking (process.py:43-47, 115-118),
+// separable Gaussian smoothing (signal.py:247-319, process.py:66-113) and
+// the normalised steepest-descent update (optimizer.py:124-142).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sgb_common.cuh"
+#include "capi_util.cuh"
+
+namespace sgb {
+namespace {
+
+int blocks_for(long long n) {
+  long long b = (n + 255) / 256;
+  return (int)(b > 152 * 16 ? 152 * 16 : (b < 1 ? 1 : b));
+}
+
+// resid = 2 (syn - obs); *loss += sum (syn - obs)^2 (double).
+__global__ void l2_kernel(long long n, const float* syn, const float* obs, float* resid, double* loss) {
+  double a = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float d = syn[i] - obs[i];
+    if (resid != nullptr) resid[i] = 2.f * d;
+    a += (double)d * (double)d;
+  }
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, a);
+}
+
+__global__ void precond_kernel(int nz, int nx, int pitch, const float* g, const float* illum, float eps,
+                               const float* mask, float* out) {
+  const long long n = (long long)nz * pitch;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if ((int)(i % pitch) >= nx) {
+      out[i] = 0.f;
+      continue;
+    }
+    float v = g[i];
+    if (mask != nullptr) v *= mask[i];
+    if (illum != nullptr) v /= (illum[i] + eps);
+    out[i] = v;
+  }
+}
+
+// numpy 'reflect' index (mirror without repeating the edge).
+__device__ __forceinline__ int reflect(int j, int n) {
+  if (n == 1) return 0;
+  const int period = 2 * (n - 1);
+  j %= period;
+  if (j < 0) j += period;
+  return j < n ? j : period - j;
+}
+
+// One axis of the smoothing: out[i] = sum_{d=-r..r} w[d + r] in[reflect(i + d)].
+__global__ void smooth_axis_kernel(int nz, int nx, int pitch, int axis, const float* w, int r, const float* in,
+                                   float* out) {
+  const long long n = (long long)nz * nx;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int z = (int)(i / nx), x = (int)(i % nx);
+    float a = 0.f;
+    if (axis == 0) {
+      for (int d = -r; d <= r; ++d) a = fmaf(w[d + r], in[(long long)reflect(z + d, nz) * pitch + x], a);
+    } else {
+      for (int d = -r; d <= r; ++d) a = fmaf(w[d + r], in[(long long)z * pitch + reflect(x + d, nx)], a);
+    }
+    out[(long long)z * pitch + x] = a;
+  }
+}
+
+// max |clamp(g, lo, hi)| as the bits of a non-negative float.
+__global__ void maxabs_kernel(long long n, const float* g, int clamp, float lo, float hi, unsigned* out) {
+  float m = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float v = g[i];
+    if (clamp) v = fminf(fmaxf(v, lo), hi);
+    m = fmaxf(m, fabsf(v));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+__global__ void sd_kernel(long long n, float* p, const float* g, int clamp, float lo, float hi, float lr,
+                          const unsigned* maxbits) {
+  const float mx = __uint_as_float(*maxbits);
+  const float alpha = mx > 0.f ? lr / mx : 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float v = g[i];
+    if (clamp) v = fminf(fmaxf(v, lo), hi);
+    p[i] -= alpha * v;
+  }
+}
+
+}  // namespace
+}  // namespace sgb
+
+using namespace sgb;
+
+extern "C" {
+
+int sgb_l2_misfit(int64_t n, const float* syn, const float* obs, float* resid, double* loss, sgb_stream_t stream) {
+  if (syn == nullptr || obs == nullptr || loss == nullptr) return SGB_ERR_ARG;
+  if (n <= 0) return SGB_ERR_SHAPE;
+  l2_kernel<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(n, syn, obs, resid, loss);
+  SGB_CUDA_CHECK(cudaGetLastError());
+  return SGB_OK;
+}
+
+int sgb_grad_precondition(int32_t nz, int32_t nx, int32_t pitch, const float* grad, const float* illum, float eps,
+                          const float* mask, float* out, sgb_stream_t stream) {
+  if (grad == nullptr || out == nullptr) return SGB_ERR_ARG;
+  if (nz <= 0 || nx <= 0 || pitch < nx) return SGB_ERR_SHAPE;
+  precond_kernel<<<blocks_for((long long)nz * pitch), 256, 0, (cudaStream_t)stream>>>(nz, nx, pitch, grad, illum,
+                                                                                       eps, mask, out);
+  SGB_CUDA_CHECK(cudaGetLastError());
+  return SGB_OK;
+}
+
+int sgb_grad_smooth(int32_t nz, int32_t nx, int32_t pitch, const float* weights_z, int32_t radius_z,
+                    const float* weights_x, int32_t radius_x, int32_t counts, float* grad, float* tmp,
+                    sgb_stream_t stream) {
+  if (grad == nullptr || tmp == nullptr || weights_z == nullptr || weights_x == nullptr) return SGB_ERR_ARG;
+  if (nz <= 0 || nx <= 0 || pitch < nx || counts < 0 || radius_z < 0 || radius_x < 0) return SGB_ERR_SHAPE;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = blocks_for((long long)nz * nx);
+  for (int c = 0; c < counts; ++c) {
+    smooth_axis_kernel<<<nb, 256, 0, s>>>(nz, nx, pitch, 0, weights_z, radius_z, grad, tmp);
+    smooth_axis_kernel<<<nb, 256, 0, s>>>(nz, nx, pitch, 1, weights_x, radius_x, tmp, grad);
+  }
+  SGB_CUDA_CHECK(cudaGetLastError());
+  return SGB_OK;
+}
+
+int sgb_sd_step(int64_t n, float* param, const float* grad, float lr, int32_t clamp, float lo, float hi,
+                uint32_t* scratch, sgb_stream_t stream) {
+  if (param == nullptr || grad == nullptr || scratch == nullptr) return SGB_ERR_ARG;
+  if (n <= 0) return SGB_ERR_SHAPE;
+  cudaStream_t s = (cudaStream_t)stream;
+  SGB_CUDA_CHECK(cudaMemsetAsync(scratch, 0, sizeof(uint32_t), s));
+  maxabs_kernel<<<blocks_for(n), 256, 0, s>>>(n, grad, clamp, lo, hi, scratch);
+  sd_kernel<<<blocks_for(n), 256, 0, s>>>(n, param, grad, clamp, lo, hi, lr, scratch);
+  SGB_CUDA_CHECK(cudaGetLastError());
+  return SGB_OK;
+}
+
+}  // extern "C"

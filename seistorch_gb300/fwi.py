@@ -24,6 +24,7 @@ import torch
 
 from . import engine
 from .pml import generate_pml_coefficients_2d
+from .postprocess import L2
 from .utils import ricker_wave
 
 TARGET_SCALE = 1000.0  # m/s per unit of network output
@@ -83,13 +84,14 @@ class Survey:
         return rec
 
     def misfit(self, vp_pad, obs):
-        return float(((self.records(vp_pad) - obs) ** 2).sum())
+        with torch.no_grad():
+            return float(L2()(self.records(vp_pad), obs))
 
     def gradient(self, vp_pad, obs):
         """(misfit, gradient (interior), illumination (interior))."""
         vp = vp_pad.clone().requires_grad_(True)
         rec, illum = engine.acoustic_loop(vp, self.prop, self.d, self.acq, True, self.ckpt)
-        loss = ((rec - obs) ** 2).sum()
+        loss = L2()(rec, obs)
         loss.backward()
         w = self.w
         return float(loss.detach()), vp.grad[w:-w, w:-w].detach(), illum[w:-w, w:-w].detach()

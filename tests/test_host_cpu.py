@@ -211,3 +211,24 @@ def test_elastic_calls_validate_before_touching_the_gpu(lib):
     cur = ctypes.c_int32(0)
     assert lib.sgb_elastic_forward(ctypes.byref(g), ctypes.byref(m), ctypes.byref(q), ctypes.byref(io),
                                    N.PTR10(*([16] * 10)), None, None, ctypes.byref(cur), None) == 1
+
+
+def test_pickled_geometry_and_shot_files_round_trip(tmp_path):
+    """Geometry in the reference's pickle layout (io.py:352-364) feeds
+    setup_acquisition; shot gathers round-trip through the shot file."""
+    from seistorch_gb300.io import SeisIO
+    io = SeisIO()
+    src = [[10, 2], [30, 2]]
+    rec = [[list(range(0, 40)), [2] * 40]] * 2
+    sp, rp = str(tmp_path / "src.pkl"), str(tmp_path / "rec.pkl")
+    io.write_pkl(sp, src)
+    io.write_pkl(rp, rec)
+    cfg = {"geom": {"sources": sp, "receivers": rp}}
+    s2, r2 = io.read_geom(cfg)
+    assert s2 == src and r2 == rec
+    with pytest.raises(FileNotFoundError):
+        io.read_geom({"geom": {"sources": sp + "x", "receivers": rp}})
+    shots = [np.random.default_rng(i).standard_normal((20, 40, 1)).astype(np.float32) for i in range(2)]
+    path = io.write_shots(str(tmp_path / "obs.hdf5"), shots)
+    for i in range(2):
+        assert np.array_equal(io.read_shot(path, i), shots[i])
