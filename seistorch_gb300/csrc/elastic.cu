@@ -105,10 +105,6 @@ struct RowIO {
     if (L.ld && z >= 0 && z < nz) return __ldg(reinterpret_cast<const float4*>(p + (long long)z * pitch + L.xl));
     return f4(0.f);
   }
-  __device__ __forceinline__ float4 ldw(const float* p, int z, const ElLane& L) const {  // read-write data
-    if (L.ld && z >= 0 && z < nz) return *reinterpret_cast<const float4*>(p + (long long)z * pitch + L.xl);
-    return f4(0.f);
-  }
   __device__ __forceinline__ void st(float* p, int z, const ElLane& L, const float4& v) const {
     if (L.own) *reinterpret_cast<float4*>(p + (long long)z * pitch + L.xl) = v;
   }
@@ -214,10 +210,18 @@ __device__ __forceinline__ bool lane_ring_row(const Ring& R, int z, const ElLane
 
 // ------------------------------------------------------------ forward ---
 
+// Rows a forward iteration reads, prefetched one iteration ahead: for step
+// row z, vx / vz / txz and the five coefficient rows of z + 1, txx / tzz of z.
+constexpr int FWD_PRE_ROWS = 10;
+
 template <int TZ>
 __global__ void __launch_bounds__(128) elastic_fwd_kernel(const ElFwdArgs a) {
   __shared__ __align__(16) float sbuf_all[4][128];
+  // per warp, two slots of the prefetched rows; each lane copies and reads
+  // back only its own 16 bytes, so the slots need no warp synchronisation
+  __shared__ __align__(16) float pre_all[4][2][FWD_PRE_ROWS][128];
   float* sbuf = sbuf_all[threadIdx.x >> 5];
+  float* pre = &pre_all[threadIdx.x >> 5][0][0][0];
   const int gw = blockIdx.x * 4 + (threadIdx.x >> 5);
   if (gw >= a.nshots * a.nstrip * a.nband) return;  // whole warps; no block barrier below
   const int b = gw % a.nshots;
@@ -260,12 +264,38 @@ __global__ void __launch_bounds__(128) elastic_fwd_kernel(const ElFwdArgs a) {
     txz_c = fma4(io.ld(a.c.ma, z0, L), G, q_c * io.ld(txz, z0, L));
   }
 
+  auto cp_row = [&](float* dst, const float* src, int zz) {
+    const bool ok = L.ld && zz >= 0 && zz < nz;
+    cp_async16(dst + 4 * L.lane, ok ? src + (long long)zz * a.pitch + L.xl : src, ok ? 16 : 0);
+  };
+  auto fetch = [&](int slot, int z) {
+    float* d = pre + slot * FWD_PRE_ROWS * 128;
+    cp_row(d + 0 * 128, vx, z + 1);
+    cp_row(d + 1 * 128, vz, z + 1);
+    cp_row(d + 2 * 128, txz, z + 1);
+    cp_row(d + 3 * 128, a.c.q, z + 1);
+    cp_row(d + 4 * 128, a.c.pa, z + 1);
+    cp_row(d + 5 * 128, a.c.la, z + 1);
+    cp_row(d + 6 * 128, a.c.ma, z + 1);
+    cp_row(d + 7 * 128, a.c.bv, z + 1);
+    cp_row(d + 8 * 128, txx, z);
+    cp_row(d + 9 * 128, tzz, z);
+    cp_async_commit();
+  };
+  fetch(0, z0);
   for (int z = z0; z < z1; ++z) {
     const int zn = z + 1;
-    const float4 vx_n = io.ld(vx, zn, L), vz_n = io.ld(vz, zn, L), txz_in = io.ld(txz, zn, L);
-    const float4 txx_in = io.ld(txx, z, L), tzz_in = io.ld(tzz, z, L);
-    const float4 q_n = io.ld(a.c.q, zn, L), pa_n = io.ld(a.c.pa, zn, L), la_n = io.ld(a.c.la, zn, L);
-    const float4 ma_n = io.ld(a.c.ma, zn, L), bv_n = io.ld(a.c.bv, zn, L);
+    const int slot = (z - z0) & 1;
+    if (zn < z1)
+      fetch(slot ^ 1, zn);
+    else
+      cp_async_commit();  // an empty group keeps the wait count uniform
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    const float* r = pre + slot * FWD_PRE_ROWS * 128 + 4 * L.lane;
+    const float4 vx_n = lds4(r + 0 * 128), vz_n = lds4(r + 1 * 128), txz_in = lds4(r + 2 * 128);
+    const float4 txx_in = lds4(r + 8 * 128), tzz_in = lds4(r + 9 * 128);
+    const float4 q_n = lds4(r + 3 * 128), pa_n = lds4(r + 4 * 128), la_n = lds4(r + 5 * 128);
+    const float4 ma_n = lds4(r + 6 * 128), bv_n = lds4(r + 7 * 128);
     // stresses of row z (A-8, A-9) and txz' of row z + 1 (A-10)
     const float4 E = dxm(vx_c, L);
     const float4 F = z < nz - 1 ? vz_n - vz_c : f4(0.f);
@@ -337,10 +367,18 @@ __global__ void __launch_bounds__(128) elastic_fwd_kernel(const ElFwdArgs a) {
 // A warp walks rows r = z0-1 .. z1: at row r it completes everything that
 // needs rows <= r and finishes row r-1 (the Dz+ vz_i, Dz- hxz terms).
 
+// Rows a reverse iteration r reads, prefetched one iteration ahead (index in
+// the slot): s0 s1 (v_in in mode 1) s2 s3 a0 a2 a3 a4 of r; the three
+// gradient rows of r; s4 a1 of r + 1.  The coefficient rows (shared by all
+// shots, L2-resident) are read with early __ldg instead.
+constexpr int BWD_PRE_ROWS = 13;
+
 template <int TZ, int MODE>
 __global__ void __launch_bounds__(128) elastic_bwd_kernel(const ElBwdArgs a) {
   __shared__ __align__(16) float sbuf_all[4][128];
+  extern __shared__ __align__(16) float bwd_pre[];  // [4 warps][2 slots][BWD_PRE_ROWS][128]
   float* sbuf = sbuf_all[threadIdx.x >> 5];
+  float* pre = bwd_pre + (threadIdx.x >> 5) * 2 * BWD_PRE_ROWS * 128;
   const int gw = blockIdx.x * 4 + (threadIdx.x >> 5);
   if (gw >= a.nshots * a.nstrip * a.nband) return;
   const int b = gw % a.nshots;
@@ -373,20 +411,42 @@ __global__ void __launch_bounds__(128) elastic_bwd_kernel(const ElBwdArgs a) {
   ElPoints pr = a.p;
   pr.rec_row_ptr = rp;
 
-  // state (s'') row loader: subtract this step's sources
-  auto lds = [&](int f, int z) {
-    float4 v = io.ld(S[f], z, L);
+  // corrections on loading: this step's sources leave the state (s''), the
+  // receiver residuals of the channels on field f enter the adjoint
+  auto fix_s = [&](float4 v, int f, int z) {
     if (MODE == 0 && (a.p.src_fields & (1 << f)) && z >= 0 && z < nz) add_sources(src, z, -1.f, v, sbuf, L);
     return v;
   };
-  // adjoint row loader: add the receiver residuals of the channels on field f
-  auto lda = [&](int f, int z) {
-    float4 v = io.ld(A[f], z, L);
+  auto fix_a = [&](float4 v, int f, int z) {
     if (MODE == 0 && has_rec && z >= 0 && z < nz) {
       for (int ch = 0; ch < a.p.nch; ++ch)
         if (a.p.rec_fields[ch] == f) add_residual(pr, a.resid, z, ch, v, sbuf, L);
     }
     return v;
+  };
+  auto lds = [&](int f, int z) { return fix_s(io.ld(S[f], z, L), f, z); };
+  auto lda = [&](int f, int z) { return fix_a(io.ld(A[f], z, L), f, z); };
+  auto cp_row = [&](float* dst, const float* src, int zz) {
+    const bool ok = L.ld && zz >= 0 && zz < nz;
+    cp_async16(dst + 4 * L.lane, ok ? src + (long long)zz * a.pitch + L.xl : src, ok ? 16 : 0);
+  };
+  auto fetch = [&](int slot, int r) {
+    float* d = pre + slot * BWD_PRE_ROWS * 128;
+    cp_row(d + 0 * 128, MODE == 0 ? S[0] : a.v_in[0] + fb, r);
+    cp_row(d + 1 * 128, MODE == 0 ? S[1] : a.v_in[1] + fb, r);
+    cp_row(d + 2 * 128, S[2], r);
+    cp_row(d + 3 * 128, S[3], r);
+    cp_row(d + 4 * 128, A[0], r);
+    cp_row(d + 5 * 128, A[2], r);
+    cp_row(d + 6 * 128, A[3], r);
+    cp_row(d + 7 * 128, A[4], r);
+    const bool wrr = r >= z0 && r < z1;  // gradient rows are only read where this warp writes them
+    cp_row(d + 8 * 128, a.grad[0] + fb, wrr ? r : -1);
+    cp_row(d + 9 * 128, a.grad[1] + fb, wrr ? r : -1);
+    cp_row(d + 10 * 128, a.grad[2] + fb, wrr ? r : -1);
+    cp_row(d + 11 * 128, S[4], r + 1);
+    cp_row(d + 12 * 128, A[1], r + 1);
+    cp_async_commit();
   };
   auto ringv = [&](int f, int z, unsigned m) {  // ring values of s_i for the components in m
     float4 v = f4(0.f);
@@ -418,21 +478,30 @@ __global__ void __launch_bounds__(128) elastic_bwd_kernel(const ElBwdArgs a) {
   float4 avz_r = lda(1, z0 - 1);
   float4 gz_r = io.ld(a.c.bv, z0 - 1, L) * avz_r;
 
+  fetch(0, z0 - 1);
   for (int r = z0 - 1; r <= z1; ++r) {
     const bool inrow = r >= 0 && r < nz;
     const bool wr = r >= z0 && r < z1;
     const bool fin = r - 1 >= z0 && r - 1 < z1;
     const unsigned box = (MODE == 1 || (r >= a.ring.iz0 && r < a.ring.iz1)) ? boxc : 0u;
-    // row r
-    const float4 txx = lds(2, r), tzz = lds(3, r);
+    const int slot = (r - (z0 - 1)) & 1;
+    if (r + 1 <= z1)
+      fetch(slot ^ 1, r + 1);
+    else
+      cp_async_commit();  // an empty group keeps the wait count uniform
     const float4 q = io.ld(a.c.q, r, L), pa = io.ld(a.c.pa, r, L), la = io.ld(a.c.la, r, L);
-    const float4 ma = io.ld(a.c.ma, r, L), bv = io.ld(a.c.bv, r, L);
-    const float4 avx = lda(0, r);
-    const float4 atxx = lda(2, r), atzz = lda(3, r), atxz = lda(4, r);
+    const float4 ma = io.ld(a.c.ma, r, L), bv = io.ld(a.c.bv, r, L), bv_n = io.ld(a.c.bv, r + 1, L);
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    const float* pr_ = pre + slot * BWD_PRE_ROWS * 128 + 4 * L.lane;
+    // row r
+    const float4 txx = fix_s(lds4(pr_ + 2 * 128), 2, r), tzz = fix_s(lds4(pr_ + 3 * 128), 3, r);
+    const float4 avx = fix_a(lds4(pr_ + 4 * 128), 0, r);
+    const float4 atxx = fix_a(lds4(pr_ + 5 * 128), 2, r), atzz = fix_a(lds4(pr_ + 6 * 128), 3, r);
+    const float4 atxz = fix_a(lds4(pr_ + 7 * 128), 4, r);
     // row r + 1 parts
-    const float4 txz_n = lds(4, r + 1);
-    const float4 avz_n = lda(1, r + 1);
-    const float4 gz_n = io.ld(a.c.bv, r + 1, L) * avz_n;
+    const float4 txz_n = fix_s(lds4(pr_ + 11 * 128), 4, r + 1);
+    const float4 avz_n = fix_a(lds4(pr_ + 12 * 128), 1, r + 1);
+    const float4 gz_n = bv_n * avz_n;
     const float4 gx = bv * avx;
     // velocity part: Dv(s'') and v_i
     const float4 dvx = dxp(txx, L) + (r <= nz - 2 ? txz_n - txz_r : f4(0.f));
@@ -441,12 +510,12 @@ __global__ void __launch_bounds__(128) elastic_bwd_kernel(const ElBwdArgs a) {
     unsigned rmask = 0u;
     if (MODE == 0) {
       rmask = inrow ? ring_mask(r) : 0u;
-      const float4 vxs = lds(0, r), vzs = lds(1, r);
+      const float4 vxs = fix_s(lds4(pr_ + 0 * 128), 0, r), vzs = fix_s(lds4(pr_ + 1 * 128), 1, r);
       vxi = pick(box, vxs - bv * dvx, ringv(0, r, rmask));
       vzi = pick(box, vzs - bv * dvz, ringv(1, r, rmask));
     } else {
-      vxi = io.ld(a.v_in[0] + fb, r, L);
-      vzi = io.ld(a.v_in[1] + fb, r, L);
+      vxi = lds4(pr_ + 0 * 128);
+      vzi = lds4(pr_ + 1 * 128);
     }
     const float4 gb_inc = sel(box, fma4(avx, dvx, avz_r * dvz));
     // stress adjoint after the velocity transpose
@@ -474,9 +543,9 @@ __global__ void __launch_bounds__(128) elastic_bwd_kernel(const ElBwdArgs a) {
     const float4 G = dxp(vzi, L) + (r >= 1 ? vxi - vxi_p : f4(0.f));
     if (wr) {
       const float4 Sx = sel(box, atxx_m + atzz_m);
-      float4 glam = io.ldw(a.grad[0] + fb, r, L);
-      float4 gmu = io.ldw(a.grad[1] + fb, r, L);
-      const float4 gbv = io.ldw(a.grad[2] + fb, r, L) + gb_inc;
+      float4 glam = lds4(pr_ + 8 * 128);
+      float4 gmu = lds4(pr_ + 9 * 128);
+      const float4 gbv = lds4(pr_ + 10 * 128) + gb_inc;
       glam = fma4(Sx, E, glam);
       gmu = gmu + sel(box, fma4(2.f * atxx_m, E, atxz_m * G));
       if (MODE == 0) {
@@ -595,10 +664,20 @@ cudaError_t launch_elastic_fwd(const ElFwdArgs& a, cudaStream_t s) {
 
 cudaError_t launch_elastic_bwd(const ElBwdArgs& a, int mode, cudaStream_t s) {
   const long long warps = (long long)a.nshots * a.nstrip * a.nband;
+  constexpr size_t smem = 4 * 2 * BWD_PRE_ROWS * 128 * sizeof(float);
+  static bool set = false;
+  if (!set) {
+    cudaError_t e = cudaFuncSetAttribute(elastic_bwd_kernel<EL_TZ, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(elastic_bwd_kernel<EL_TZ, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    set = true;
+  }
   if (mode == 0)
-    elastic_bwd_kernel<EL_TZ, 0><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(a);
+    elastic_bwd_kernel<EL_TZ, 0><<<(unsigned)((warps + 3) / 4), 128, smem, s>>>(a);
   else
-    elastic_bwd_kernel<EL_TZ, 1><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(a);
+    elastic_bwd_kernel<EL_TZ, 1><<<(unsigned)((warps + 3) / 4), 128, smem, s>>>(a);
   return cudaGetLastError();
 }
 
