@@ -345,6 +345,15 @@ int sgb_grad_smooth(int32_t nz, int32_t nx, int32_t pitch, const float *weights_
 int sgb_sd_step(int64_t n, float *param, const float *grad, float lr, int32_t clamp, float lo, float hi,
                 uint32_t *scratch, sgb_stream_t stream);
 
+/* Zero-phase IIR filtering of records (scipy.signal.filtfilt with its
+ * default odd padding, as SeisSignal.filter applies it to each shot,
+ * signal.py:39-101): records [nt][ntraces] (trace fastest); b, a (a[0] = 1),
+ * zi (lfilter_zi, ncoef - 1 values) are ncoef <= 17 device doubles; padlen
+ * = 3 max(len a, len b), padlen < nt; work: [nt + 2 padlen][ntraces]
+ * doubles.  out may alias in. */
+int sgb_filtfilt(int32_t nt, int32_t ntraces, int32_t ncoef, const double *b, const double *a, const double *zi,
+                 int32_t padlen, const float *in, float *out, double *work, sgb_stream_t stream);
+
 /* --------------------------------------------- learned preconditioner --- */
 /* BF16-weight / FP32-accumulate kernels of the convolutional gradient
  * preconditioner (no counterpart in the reference, which preconditions by

@@ -179,6 +179,7 @@ SIGNATURES = {
     "sgb_grad_precondition": (ctypes.c_int, [c_i32, c_i32, c_i32, c_ptr, c_ptr, c_f32, c_ptr, c_ptr, c_ptr]),
     "sgb_grad_smooth": (ctypes.c_int, [c_i32, c_i32, c_i32, c_ptr, c_i32, c_ptr, c_i32, c_i32, c_ptr, c_ptr,
                                        c_ptr]),
+    "sgb_filtfilt": (ctypes.c_int, [c_i32, c_i32, c_i32, c_ptr, c_ptr, c_ptr, c_i32, c_ptr, c_ptr, c_ptr, c_ptr]),
     "sgb_sd_step": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_f32, c_i32, c_f32, c_f32, c_ptr, c_ptr]),
     "sgb_elastic_coefficients": (ctypes.c_int, [ctypes.POINTER(Grid), c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                                                 c_ptr]),

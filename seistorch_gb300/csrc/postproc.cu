@@ -92,6 +92,45 @@ __global__ void sd_kernel(long long n, float* p, const float* g, int clamp, floa
   }
 }
 
+// Zero-phase IIR filter of every trace (scipy.signal.filtfilt's default
+// method as SeisSignal._filter_ calls it, signal.py:39-40): odd extension
+// by padlen samples at both ends, a forward direct-form-II-transposed pass
+// started from zi * first sample, a backward pass started from zi * its
+// first sample, extension removed.  Records [nt][ntr] (trace fastest); one
+// thread per trace; float64 state.  work: [nt + 2 padlen][ntr] doubles.
+__global__ void filtfilt_kernel(int nt, int ntr, int nc, const double* b, const double* a, const double* zi,
+                                int padlen, const float* in, float* out, double* work) {
+  const int tr = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tr >= ntr) return;
+  const int ne = nt + 2 * padlen;
+  auto x_ext = [&](int i) -> double {  // odd extension
+    if (i < padlen) return 2.0 * in[tr] - in[(long long)(padlen - i) * ntr + tr];
+    if (i >= padlen + nt) {
+      const int k = i - (padlen + nt);  // 0.. padlen-1
+      return 2.0 * in[(long long)(nt - 1) * ntr + tr] - in[(long long)(nt - 2 - k) * ntr + tr];
+    }
+    return in[(long long)(i - padlen) * ntr + tr];
+  };
+  double z[16];
+  const int m = nc - 1;  // state length
+  double x0 = x_ext(0);
+  for (int j = 0; j < m; ++j) z[j] = zi[j] * x0;
+  for (int i = 0; i < ne; ++i) {
+    const double x = x_ext(i);
+    const double y = b[0] * x + (m > 0 ? z[0] : 0.0);
+    for (int j = 0; j < m; ++j) z[j] = b[j + 1] * x - a[j + 1] * y + (j + 1 < m ? z[j + 1] : 0.0);
+    work[(long long)i * ntr + tr] = y;
+  }
+  x0 = work[(long long)(ne - 1) * ntr + tr];
+  for (int j = 0; j < m; ++j) z[j] = zi[j] * x0;
+  for (int i = ne - 1; i >= 0; --i) {
+    const double x = work[(long long)i * ntr + tr];
+    const double y = b[0] * x + (m > 0 ? z[0] : 0.0);
+    for (int j = 0; j < m; ++j) z[j] = b[j + 1] * x - a[j + 1] * y + (j + 1 < m ? z[j + 1] : 0.0);
+    if (i >= padlen && i < padlen + nt) out[(long long)(i - padlen) * ntr + tr] = (float)y;
+  }
+}
+
 }  // namespace
 }  // namespace sgb
 
@@ -140,6 +179,17 @@ int sgb_sd_step(int64_t n, float* param, const float* grad, float lr, int32_t cl
   SGB_CUDA_CHECK(cudaMemsetAsync(scratch, 0, sizeof(uint32_t), s));
   maxabs_kernel<<<blocks_for(n), 256, 0, s>>>(n, grad, clamp, lo, hi, scratch);
   sd_kernel<<<blocks_for(n), 256, 0, s>>>(n, param, grad, clamp, lo, hi, lr, scratch);
+  SGB_CUDA_CHECK(cudaGetLastError());
+  return SGB_OK;
+}
+
+int sgb_filtfilt(int32_t nt, int32_t ntraces, int32_t ncoef, const double* b, const double* a, const double* zi,
+                 int32_t padlen, const float* in, float* out, double* work, sgb_stream_t stream) {
+  if (b == nullptr || a == nullptr || zi == nullptr || in == nullptr || out == nullptr || work == nullptr)
+    return SGB_ERR_ARG;
+  if (nt < 2 || ntraces <= 0 || ncoef < 1 || ncoef > 17 || padlen < 0 || padlen > nt - 1) return SGB_ERR_SHAPE;
+  filtfilt_kernel<<<(ntraces + 127) / 128, 128, 0, (cudaStream_t)stream>>>(nt, ntraces, ncoef, b, a, zi, padlen,
+                                                                            in, out, work);
   SGB_CUDA_CHECK(cudaGetLastError());
   return SGB_OK;
 }

@@ -1,5 +1,7 @@
 """Misfit and gradient post-processing on the device, with seistorch's names.
 
+``filter_records`` (SeisSignal.filter, signal.py:39-101): Butterworth
+low-/band-pass applied forward and backward (zero phase) to every trace.
 ``L2`` (loss.py:409-421): sum over shots of MSELoss(reduction='sum'); its
 backward is the adjoint source 2 (syn - obs) from the same kernel pass.
 ``precondition`` / ``cut_gradient`` (process.py:43-47, 115-118),
@@ -125,3 +127,43 @@ class Steepestdescent(torch.optim.Optimizer):
                        int(group["grad_clamp"]), ctypes.c_float(lo), ctypes.c_float(hi), N.ptr(s),
                        N.stream_handle())
         return loss
+
+
+def filter_mode(freqs):
+    """SeisSignal.decide_filter_type: a number or [f] -> lowpass, [f1, f2] -> bandpass."""
+    if freqs == "all":
+        return "all"
+    if isinstance(freqs, (int, float)):
+        return "lowpass"
+    if isinstance(freqs, (list, tuple)):
+        return "lowpass" if len(freqs) == 1 else "bandpass"
+    raise ValueError(f"cannot filter with frequencies {freqs!r}")
+
+
+def filter_records(records, dt, freqs, order=4):
+    """Zero-phase Butterworth filter of records (nt, ntraces[, nch]) along time
+    on the device; the filter is designed with scipy.signal.butter as the
+    reference does (Wn = 2 f dt)."""
+    from scipy import signal as sps
+    mode = filter_mode(freqs)
+    if mode == "all":
+        return records
+    f = [freqs] if isinstance(freqs, (int, float)) else list(freqs)
+    wn = [2.0 * fr * dt for fr in f]
+    b, a = sps.butter(order, wn[0] if len(wn) == 1 else wn, btype=mode)
+    zi = sps.lfilter_zi(b, a)
+    padlen = 3 * max(len(a), len(b))
+    require_cuda(records, "filter_records")
+    shape = records.shape
+    x = records.reshape(shape[0], -1).contiguous().to(torch.float32)
+    nt, ntr = x.shape
+    if padlen >= nt:
+        raise ValueError("records too short for the filter's padding")
+    dev = records.device
+    host = lambda v: torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).to(dev)
+    bt, at, zt = host(b / a[0]), host(a / a[0]), host(zi)
+    out = torch.empty_like(x)
+    work = torch.empty(nt + 2 * padlen, ntr, dtype=torch.float64, device=dev)
+    N.call("sgb_filtfilt", nt, ntr, len(b), N.ptr(bt), N.ptr(at), N.ptr(zt), padlen, N.ptr(x), N.ptr(out),
+           N.ptr(work), N.stream_handle())
+    return out.reshape(shape)

@@ -71,3 +71,26 @@ def test_steepest_descent_step():
     d = p.grad.clamp(q[0], q[1])
     want = p0 - 10.0 * d / d.abs().max()
     assert torch.allclose(p.detach(), want, rtol=1e-6, atol=1e-5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("freqs", [5.0, [3.0, 12.0]])
+def test_record_filter_matches_scipy_filtfilt(freqs):
+    """SeisSignal.filter's scipy backend is scipy.signal.filtfilt(b, a, d,
+    axis=0) with a Butterworth design; the device filter matches it to 1e-5
+    (both recur in float64; the band-pass design's poles near the unit
+    circle amplify the different summation order to ~1e-6)."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    from scipy import signal as sps
+    from seistorch_gb300 import _native, postprocess
+    _native.load(build_if_missing=False)
+    rng = np.random.default_rng(0)
+    d = rng.standard_normal((500, 37, 2)).astype(np.float32)
+    dt = 0.002
+    mode = postprocess.filter_mode(freqs)
+    f = [freqs] if isinstance(freqs, float) else freqs
+    b, a = sps.butter(4, [2 * x * dt for x in f] if len(f) > 1 else 2 * f[0] * dt, btype=mode)
+    want = sps.filtfilt(b, a, d, axis=0).astype(np.float32)
+    got = postprocess.filter_records(torch.tensor(d, device="cuda"), dt, freqs, 4).cpu().numpy()
+    assert rel_l2(got, want) < 1e-5
