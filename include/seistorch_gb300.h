@@ -409,6 +409,8 @@ int sgb_nn_to_chw(int32_t n, int32_t h, int32_t w, int32_t c, int32_t cstride, i
  * pool2_bwd: gp / 4 (coarse, c channels) + an optional slice gs, times
  * [act > 0].  pack_weights: fp32 [cout][cin][3][3] -> bf16 [cout][9][cin]
  * and (if wflip) the flipped transpose [cin][9][cout] for data gradients.
+ * bias_grad: db[c] += sum of a channel-major bf16 gradient [n][c][hw].
+ * Channel counts, strides and offsets of these helpers are multiples of 8.
  * adam: one step (bias-corrected, step >= 1, decoupled weight decay wd).
  * mse: grad = 2 (pred - target) / n and *loss += mean squared error. */
 int sgb_nn_conv_in(int32_t n, int32_t h, int32_t w, int32_t c, const float *in, const float *W, const float *b,
@@ -427,7 +429,7 @@ int sgb_nn_up2_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float *g, i
                    const void *act, void *out, sgb_stream_t stream);
 int sgb_nn_pool2_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float *gp, const float *gs, int32_t cs_s,
                      int32_t coff_s, const void *act, int32_t cs_a, int32_t coff_a, void *out, sgb_stream_t stream);
-int sgb_nn_bias_grad(int64_t npix, int32_t c, const void *dy, float *db, sgb_stream_t stream);
+int sgb_nn_bias_grad(int32_t n, int64_t hw, int32_t c, const void *dy_chw, float *db, sgb_stream_t stream);
 int sgb_nn_pack_weights(int32_t cout, int32_t cin, const float *W, void *wt, void *wflip, sgb_stream_t stream);
 int sgb_nn_adam(int64_t n, float *p, const float *g, float *m, float *v, float lr, float b1, float b2, float eps,
                 int32_t step, float wd, sgb_stream_t stream);

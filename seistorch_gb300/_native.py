@@ -170,7 +170,7 @@ SIGNATURES = {
     "sgb_nn_up2_bwd": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_ptr, c_i32, c_i32, c_ptr, c_ptr, c_ptr]),
     "sgb_nn_pool2_bwd": (ctypes.c_int, [c_i32, c_i32, c_i32, c_i32, c_ptr, c_ptr, c_i32, c_i32, c_ptr, c_i32,
                                         c_i32, c_ptr, c_ptr]),
-    "sgb_nn_bias_grad": (ctypes.c_int, [ctypes.c_int64, c_i32, c_ptr, c_ptr, c_ptr]),
+    "sgb_nn_bias_grad": (ctypes.c_int, [c_i32, ctypes.c_int64, c_i32, c_ptr, c_ptr, c_ptr]),
     "sgb_nn_pack_weights": (ctypes.c_int, [c_i32, c_i32, c_ptr, c_ptr, c_ptr, c_ptr]),
     "sgb_nn_adam": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_f32, c_f32, c_f32, c_f32, c_i32,
                                    c_f32, c_ptr]),

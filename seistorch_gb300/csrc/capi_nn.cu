@@ -30,7 +30,7 @@ cudaError_t launch_up2_bwd(int n, int h, int w, int c, const float* g, int cs_g,
                            bf16* out, cudaStream_t s);
 cudaError_t launch_pool2_bwd(int n, int h, int w, int c, const float* gp, const float* gs, int cs_s, int coff_s,
                              const bf16* act, int cs_a, int coff_a, bf16* out, cudaStream_t s);
-cudaError_t launch_bias_grad(long long npix, int c, const bf16* dy, float* db, cudaStream_t s);
+cudaError_t launch_bias_grad(int n, long long hw, int c, const bf16* dy, float* db, cudaStream_t s);
 cudaError_t launch_pack_weights(int cout, int cin, const float* W, bf16* wt, bf16* wflip, cudaStream_t s);
 cudaError_t launch_adam(long long n, float* p, const float* g, float* m, float* v, float lr, float b1, float b2,
                         float eps, int step, float wd, cudaStream_t s);
@@ -196,6 +196,7 @@ int sgb_nn_to_chw(int32_t n, int32_t h, int32_t w, int32_t c, int32_t cstride, i
                   int32_t copies, void* out, sgb_stream_t stream) {
   if (x_nhwc == nullptr || out == nullptr || (copies != 1 && copies != 3)) return SGB_ERR_ARG;
   if (n <= 0 || h <= 0 || w <= 0 || c <= 0 || cstride < coff + c || coff < 0) return SGB_ERR_SHAPE;
+  if (c % 8 || cstride % 8 || coff % 8) return SGB_ERR_ALIGN;
   SGB_CUDA_CHECK(launch_to_chw(n, h, w, c, cstride, coff, static_cast<const bf16*>(x_nhwc), copies,
                                static_cast<bf16*>(out), (cudaStream_t)stream));
   return SGB_OK;
@@ -209,6 +210,7 @@ int sgb_nn_conv_in(int32_t n, int32_t h, int32_t w, int32_t c, const float* in, 
                    void* out, int32_t cstride, int32_t coff, sgb_stream_t stream) {
   if (in == nullptr || W == nullptr || b == nullptr || out == nullptr) return SGB_ERR_ARG;
   if (!NN_DIMS_OK(n, h, w, c) || cstride < coff + c || coff < 0) return SGB_ERR_SHAPE;
+  if (c % 8 || cstride % 8 || coff % 8) return SGB_ERR_ALIGN;
   SGB_CUDA_CHECK(launch_conv_in_fwd(n, h, w, c, in, W, b, BFW(out), cstride, coff, (cudaStream_t)stream));
   return SGB_OK;
 }
@@ -225,6 +227,7 @@ int sgb_nn_conv_out(int32_t n, int32_t h, int32_t w, int32_t c, const void* in, 
                     const float* b, float* out, sgb_stream_t stream) {
   if (in == nullptr || W == nullptr || b == nullptr || out == nullptr) return SGB_ERR_ARG;
   if (!NN_DIMS_OK(n, h, w, c) || cstride < c) return SGB_ERR_SHAPE;
+  if (c % 8 || cstride % 8) return SGB_ERR_ALIGN;
   SGB_CUDA_CHECK(launch_conv_out_fwd(n, h, w, c, BF(in), cstride, W, b, out, (cudaStream_t)stream));
   return SGB_OK;
 }
@@ -234,6 +237,7 @@ int sgb_nn_conv_out_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float*
   if (g == nullptr || W == nullptr || act == nullptr || dx == nullptr || dW == nullptr || db == nullptr)
     return SGB_ERR_ARG;
   if (!NN_DIMS_OK(n, h, w, c) || act_cstride < c) return SGB_ERR_SHAPE;
+  if (c % 8 || act_cstride % 8) return SGB_ERR_ALIGN;
   SGB_CUDA_CHECK(launch_conv_out_bwd(n, h, w, c, g, W, BF(act), act_cstride, BFW(dx), dW, db, (cudaStream_t)stream));
   return SGB_OK;
 }
@@ -242,6 +246,7 @@ int sgb_nn_pool2(int32_t n, int32_t h, int32_t w, int32_t c, const void* in, int
                  void* out, sgb_stream_t stream) {
   if (in == nullptr || out == nullptr) return SGB_ERR_ARG;
   if (!NN_DIMS_OK(n, h, w, c) || h % 2 || w % 2 || cs_in < coff_in + c || coff_in < 0) return SGB_ERR_SHAPE;
+  if (c % 8 || cs_in % 8 || coff_in % 8) return SGB_ERR_ALIGN;
   SGB_CUDA_CHECK(launch_pool2(n, h, w, c, BF(in), cs_in, coff_in, BFW(out), (cudaStream_t)stream));
   return SGB_OK;
 }
@@ -250,6 +255,7 @@ int sgb_nn_up2(int32_t n, int32_t h, int32_t w, int32_t c, const void* in, void*
                int32_t coff_out, sgb_stream_t stream) {
   if (in == nullptr || out == nullptr) return SGB_ERR_ARG;
   if (!NN_DIMS_OK(n, h, w, c) || h % 2 || w % 2 || cs_out < coff_out + c || coff_out < 0) return SGB_ERR_SHAPE;
+  if (c % 8 || cs_out % 8 || coff_out % 8) return SGB_ERR_ALIGN;
   SGB_CUDA_CHECK(launch_up2(n, h, w, c, BF(in), BFW(out), cs_out, coff_out, (cudaStream_t)stream));
   return SGB_OK;
 }
@@ -258,6 +264,7 @@ int sgb_nn_up2_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float* g, i
                    const void* act, void* out, sgb_stream_t stream) {
   if (g == nullptr || act == nullptr || out == nullptr) return SGB_ERR_ARG;
   if (!NN_DIMS_OK(n, h, w, c) || h % 2 || w % 2 || cs_g < coff_g + c || coff_g < 0) return SGB_ERR_SHAPE;
+  if (c % 8 || cs_g % 8 || coff_g % 8) return SGB_ERR_ALIGN;
   SGB_CUDA_CHECK(launch_up2_bwd(n, h, w, c, g, cs_g, coff_g, BF(act), BFW(out), (cudaStream_t)stream));
   return SGB_OK;
 }
@@ -267,15 +274,16 @@ int sgb_nn_pool2_bwd(int32_t n, int32_t h, int32_t w, int32_t c, const float* gp
   if (gp == nullptr || act == nullptr || out == nullptr) return SGB_ERR_ARG;
   if (!NN_DIMS_OK(n, h, w, c) || h % 2 || w % 2 || cs_a < coff_a + c || (gs != nullptr && cs_s < coff_s + c))
     return SGB_ERR_SHAPE;
+  if (c % 8 || cs_a % 8 || coff_a % 8 || (gs != nullptr && (cs_s % 8 || coff_s % 8))) return SGB_ERR_ALIGN;
   SGB_CUDA_CHECK(launch_pool2_bwd(n, h, w, c, gp, gs, cs_s, coff_s, BF(act), cs_a, coff_a, BFW(out),
                                   (cudaStream_t)stream));
   return SGB_OK;
 }
 
-int sgb_nn_bias_grad(int64_t npix, int32_t c, const void* dy, float* db, sgb_stream_t stream) {
-  if (dy == nullptr || db == nullptr) return SGB_ERR_ARG;
-  if (npix <= 0 || c <= 0) return SGB_ERR_SHAPE;
-  SGB_CUDA_CHECK(launch_bias_grad(npix, c, BF(dy), db, (cudaStream_t)stream));
+int sgb_nn_bias_grad(int32_t n, int64_t hw, int32_t c, const void* dy_chw, float* db, sgb_stream_t stream) {
+  if (dy_chw == nullptr || db == nullptr) return SGB_ERR_ARG;
+  if (n <= 0 || hw <= 0 || c <= 0) return SGB_ERR_SHAPE;
+  SGB_CUDA_CHECK(launch_bias_grad(n, hw, c, BF(dy_chw), db, (cudaStream_t)stream));
   return SGB_OK;
 }
 

@@ -289,7 +289,9 @@ __global__ void __launch_bounds__(128, 1) nn_gemm_kernel(const __grid_constant__
 
 template <int BN, int RB>
 cudaError_t launch_t(const CUtensorMap* maps, const GemmArgs& g, dim3 grid, cudaStream_t s) {
-  constexpr int S = 4;
+  // three stages for the 32 KB stages of BN = 128, RB = 128 so that two CTAs
+  // share an SM (one drains its accumulator while the other multiplies)
+  constexpr int S = (BN == 128 && RB == 128) ? 3 : 4;
   using Lay = GemmLayout<BN, RB, S>;
   auto kern = nn_gemm_kernel<BN, RB, S>;
   static bool set = false;

@@ -4,7 +4,8 @@
 // heavy 3x3 convolutions run on the tensor cores (nn_gemm.cu).
 //
 // Activations are bf16 NHWC; a tensor may be a channel slice [coff, coff+c)
-// of a wider one with cstride channels per pixel.
+// of a wider one with cstride channels per pixel.  Channel counts, strides
+// and offsets are multiples of 8 (16-byte channel vectors).
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -24,26 +25,60 @@ int blocks_for(long long n) {
   return (int)(b > 152 * 32 ? 152 * 32 : (b < 1 ? 1 : b));
 }
 
+// 8 bf16 channels moved as one 16-byte vector (little-endian pairs: the
+// lower half of each 32-bit word is the even channel).
+__device__ __forceinline__ void unpack8(const uint4& u, float (&f)[8]) {
+  const unsigned w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    f[2 * k] = __uint_as_float(w[k] << 16);
+    f[2 * k + 1] = __uint_as_float(w[k] & 0xffff0000u);
+  }
+}
+__device__ __forceinline__ uint4 pack8(const float (&f)[8]) {
+  unsigned w[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const __nv_bfloat162 h2 = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+    w[k] = *reinterpret_cast<const unsigned*>(&h2);
+  }
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+__device__ __forceinline__ uint4 ld8(const bf16* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
+__device__ __forceinline__ void st8(bf16* p, const uint4& v) { *reinterpret_cast<uint4*>(p) = v; }
+
 #define GRID_STRIDE(i, total) \
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (total); i += (long long)gridDim.x * blockDim.x)
 
 // out[k][n][c][y][x] = in[n][y][x - 1 + k][coff + c] (one copy: k = 1).
+// A block moves a tile of 32 columns (plus the one-column halo the shifted
+// copies read) of one image row through shared memory: 16-byte reads of
+// the channel vectors, 64-byte coalesced rows of the channel-major output.
+constexpr int TCHW_X = 32;
 __global__ void to_chw_kernel(int n, int h, int w, int c, int cstride, int coff, const bf16* in, int copies,
                               bf16* out) {
-  const long long total = (long long)n * c * h * w;
-  GRID_STRIDE(i, total) {
-    const int x = (int)(i % w);
-    long long r = i / w;
-    const int y = (int)(r % h);
-    r /= h;
-    const int ch = (int)(r % c);
-    const int b = (int)(r / c);
-    for (int k = 0; k < copies; ++k) {
-      const int xs = x + (copies == 1 ? 0 : k - 1);
-      bf16 v = st(0.f);
-      if (xs >= 0 && xs < w) v = in[(((long long)b * h + y) * w + xs) * cstride + coff + ch];
-      out[k * total + i] = v;
-    }
+  extern __shared__ __align__(16) bf16 tile[];  // [TCHW_X + 2][c]
+  const int row = blockIdx.y;  // b * h + y
+  const int x0 = blockIdx.x * TCHW_X;
+  const int cv = c / 8;
+  for (int q = threadIdx.x; q < (TCHW_X + 2) * cv; q += blockDim.x) {
+    const int px = q / cv, k8 = (q % cv) * 8;
+    const int x = x0 - 1 + px;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (x >= 0 && x < w) v = ld8(in + ((long long)row * w + x) * cstride + coff + k8);
+    st8(tile + px * c + k8, v);
+  }
+  __syncthreads();
+  const long long plane = (long long)n * c * h * w;
+  const int b = row / h, y = row % h;
+  for (int q = threadIdx.x; q < copies * c * TCHW_X; q += blockDim.x) {
+    const int xx = q % TCHW_X;
+    const int ch = (q / TCHW_X) % c;
+    const int k = q / (TCHW_X * c);
+    const int x = x0 + xx;
+    if (x >= w) continue;
+    const int shift = copies == 1 ? 0 : k - 1;
+    out[k * plane + (((long long)b * c + ch) * h + y) * w + x] = tile[(xx + 1 + shift) * c + ch];
   }
 }
 
@@ -63,10 +98,16 @@ __global__ void conv_in_fwd_kernel(int n, int h, int w, int c, const float* in, 
           v[ci * 9 + ky * 3 + kx] =
               (yy >= 0 && yy < h && xx >= 0 && xx < w) ? in[(((long long)bb * 2 + ci) * h + yy) * w + xx] : 0.f;
         }
-    for (int co = 0; co < c; ++co) {
-      float a = b[co];
-      for (int k = 0; k < 18; ++k) a = fmaf(W[co * 18 + k], v[k], a);
-      out[i * cstride + coff + co] = st(a > 0.f ? a : 0.f);
+    for (int c8 = 0; c8 < c; c8 += 8) {
+      float o[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int co = c8 + j;
+        float a = b[co];
+        for (int k = 0; k < 18; ++k) a = fmaf(W[co * 18 + k], v[k], a);
+        o[j] = a > 0.f ? a : 0.f;
+      }
+      st8(out + i * cstride + coff + c8, pack8(o));
     }
   }
 }
@@ -119,7 +160,12 @@ __global__ void conv_out_fwd_kernel(int n, int h, int w, int c, const bf16* in, 
         const int yy = y - 1 + ky, xx = x - 1 + kx;
         if (yy < 0 || yy >= h || xx < 0 || xx >= w) continue;
         const bf16* p = in + (((long long)bb * h + yy) * w + xx) * cstride;
-        for (int ci = 0; ci < c; ++ci) a = fmaf(W[ci * 9 + ky * 3 + kx], ld(p + ci), a);
+        for (int c8 = 0; c8 < c; c8 += 8) {
+          float f[8];
+          unpack8(ld8(p + c8), f);
+#pragma unroll
+          for (int j = 0; j < 8; ++j) a = fmaf(W[(c8 + j) * 9 + ky * 3 + kx], f[j], a);
+        }
       }
     out[i] = a;
   }
@@ -141,11 +187,16 @@ __global__ void conv_out_dgrad_kernel(int n, int h, int w, int c, const float* g
         const int yy = y + 1 - ky, xx = x + 1 - kx;
         gv[ky * 3 + kx] = (yy >= 0 && yy < h && xx >= 0 && xx < w) ? g[((long long)bb * h + yy) * w + xx] : 0.f;
       }
-    for (int ci = 0; ci < c; ++ci) {
-      float a = 0.f;
-      for (int k = 0; k < 9; ++k) a = fmaf(W[ci * 9 + k], gv[k], a);
-      const float m = ld(act + i * act_cstride + ci);
-      dx[i * c + ci] = st(m > 0.f ? a : 0.f);
+    for (int c8 = 0; c8 < c; c8 += 8) {
+      float o[8], m[8];
+      unpack8(ld8(act + i * act_cstride + c8), m);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        float a = 0.f;
+        for (int k = 0; k < 9; ++k) a = fmaf(W[(c8 + j) * 9 + k], gv[k], a);
+        o[j] = m[j] > 0.f ? a : 0.f;
+      }
+      st8(dx + i * c + c8, pack8(o));
     }
   }
 }
@@ -182,86 +233,126 @@ __global__ void conv_out_wgrad_kernel(int n, int h, int w, int c, const float* g
   }
 }
 
-// 2x2 average pooling; h, w are the input dims.
+// 2x2 average pooling; h, w are the input dims; 8 channels per thread.
 __global__ void pool2_kernel(int n, int h, int w, int c, const bf16* in, int cs_in, int coff_in, bf16* out) {
-  const int ho = h / 2, wo = w / 2;
-  const long long total = (long long)n * ho * wo * c;
+  const int ho = h / 2, wo = w / 2, cv = c / 8;
+  const long long total = (long long)n * ho * wo * cv;
   GRID_STRIDE(i, total) {
-    const int ch = (int)(i % c);
-    long long r = i / c;
+    const int c8 = (int)(i % cv) * 8;
+    long long r = i / cv;
     const int x = (int)(r % wo);
     r /= wo;
     const int y = (int)(r % ho);
     const int b = (int)(r / ho);
-    float a = 0.f;
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int dy = 0; dy < 2; ++dy)
-      for (int dx = 0; dx < 2; ++dx)
-        a += ld(in + (((long long)b * h + 2 * y + dy) * w + 2 * x + dx) * cs_in + coff_in + ch);
-    out[i] = st(0.25f * a);
+      for (int dx = 0; dx < 2; ++dx) {
+        float f[8];
+        unpack8(ld8(in + (((long long)b * h + 2 * y + dy) * w + 2 * x + dx) * cs_in + coff_in + c8), f);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[j] += f[j];
+      }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] *= 0.25f;
+    st8(out + (((long long)b * ho + y) * wo + x) * c + c8, pack8(acc));
   }
 }
 
-// Nearest 2x upsampling into a channel slice; h, w are the output dims.
+// Nearest 2x upsampling into a channel slice; h, w are the output dims;
+// 8 channels per thread.
 __global__ void up2_kernel(int n, int h, int w, int c, const bf16* in, bf16* out, int cs_out, int coff_out) {
-  const long long total = (long long)n * h * w * c;
+  const int cv = c / 8;
+  const long long total = (long long)n * h * w * cv;
   GRID_STRIDE(i, total) {
-    const int ch = (int)(i % c);
-    long long r = i / c;
+    const int c8 = (int)(i % cv) * 8;
+    long long r = i / cv;
     const int x = (int)(r % w);
     r /= w;
     const int y = (int)(r % h);
     const int b = (int)(r / h);
-    out[(((long long)b * h + y) * w + x) * cs_out + coff_out + ch] =
-        in[(((long long)b * (h / 2) + y / 2) * (w / 2) + x / 2) * c + ch];
+    st8(out + (((long long)b * h + y) * w + x) * cs_out + coff_out + c8,
+        ld8(in + (((long long)b * (h / 2) + y / 2) * (w / 2) + x / 2) * c + c8));
   }
 }
 
+// 8 fp32 values of an fp32 gradient (two 16-byte loads).
+__device__ __forceinline__ void ld8f(const float* p, float (&f)[8]) {
+  const float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
+  f[0] = a.x; f[1] = a.y; f[2] = a.z; f[3] = a.w; f[4] = b.x; f[5] = b.y; f[6] = b.z; f[7] = b.w;
+}
+
 // Gradient through the upsampling (sum of the 2x2 children of a channel
-// slice of g, fp32) times [act > 0]; h, w are the fine dims.
+// slice of g, fp32) times [act > 0]; h, w are the fine dims; 8 channels per
+// thread.
 __global__ void up2_bwd_kernel(int n, int h, int w, int c, const float* g, int cs_g, int coff_g, const bf16* act,
                                bf16* out) {
-  const int ho = h / 2, wo = w / 2;
-  const long long total = (long long)n * ho * wo * c;
+  const int ho = h / 2, wo = w / 2, cv = c / 8;
+  const long long total = (long long)n * ho * wo * cv;
   GRID_STRIDE(i, total) {
-    const int ch = (int)(i % c);
-    long long r = i / c;
+    const int c8 = (int)(i % cv) * 8;
+    long long r = i / cv;
     const int x = (int)(r % wo);
     r /= wo;
     const int y = (int)(r % ho);
     const int b = (int)(r / ho);
-    float a = 0.f;
+    float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int dy = 0; dy < 2; ++dy)
-      for (int dx = 0; dx < 2; ++dx) a += g[(((long long)b * h + 2 * y + dy) * w + 2 * x + dx) * cs_g + coff_g + ch];
-    out[i] = st(ld(act + i) > 0.f ? a : 0.f);
+      for (int dx = 0; dx < 2; ++dx) {
+        float f[8];
+        ld8f(g + (((long long)b * h + 2 * y + dy) * w + 2 * x + dx) * cs_g + coff_g + c8, f);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] += f[j];
+      }
+    const long long o = (((long long)b * ho + y) * wo + x) * c + c8;
+    float m[8];
+    unpack8(ld8(act + o), m);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = m[j] > 0.f ? a[j] : 0.f;
+    st8(out + o, pack8(a));
   }
 }
 
 // Gradient at an encoder output: pooling backward (gp / 4 from the coarse
 // level) plus the skip branch (a channel slice of g), times [act > 0];
-// h, w are the fine dims.
+// h, w are the fine dims; 8 channels per thread.
 __global__ void pool2_bwd_kernel(int n, int h, int w, int c, const float* gp, const float* gs, int cs_s, int coff_s,
                                  const bf16* act, int cs_a, int coff_a, bf16* out) {
-  const long long total = (long long)n * h * w * c;
+  const int cv = c / 8;
+  const long long total = (long long)n * h * w * cv;
   GRID_STRIDE(i, total) {
-    const int ch = (int)(i % c);
-    long long r = i / c;
+    const int c8 = (int)(i % cv) * 8;
+    long long r = i / cv;
     const int x = (int)(r % w);
     r /= w;
     const int y = (int)(r % h);
     const int b = (int)(r / h);
     const long long pix = ((long long)b * h + y) * w + x;
-    float a = 0.25f * gp[(((long long)b * (h / 2) + y / 2) * (w / 2) + x / 2) * c + ch];
-    if (gs != nullptr) a += gs[pix * cs_s + coff_s + ch];
-    out[i] = st(ld(act + pix * cs_a + coff_a + ch) > 0.f ? a : 0.f);
+    float a[8], f[8], m[8];
+    ld8f(gp + (((long long)b * (h / 2) + y / 2) * (w / 2) + x / 2) * c + c8, a);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] *= 0.25f;
+    if (gs != nullptr) {
+      ld8f(gs + pix * cs_s + coff_s + c8, f);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) a[j] += f[j];
+    }
+    unpack8(ld8(act + pix * cs_a + coff_a + c8), m);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = m[j] > 0.f ? a[j] : 0.f;
+    st8(out + pix * c + c8, pack8(a));
   }
 }
 
-// db[c] += sum over pixels of dy[p][c]: block (channel group of 32 lanes? no:
-// one thread per (channel, pixel stride)).
-__global__ void bias_grad_kernel(long long npix, int c, const bf16* dy, float* db) {
+// db[c] += sum over images and pixels of dy[n][c][p] (channel-major copy);
+// block (split, channel).
+__global__ void bias_grad_kernel(int n, long long hw, int c, const bf16* dy, float* db) {
   const int ch = blockIdx.y;
   float a = 0.f;
-  GRID_STRIDE(p, npix) a += ld(dy + p * c + ch);
+  const long long total = (long long)n * hw;
+  GRID_STRIDE(q, total) {
+    const long long b = q / hw, p = q % hw;
+    a += ld(dy + (b * c + ch) * hw + p);
+  }
   for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(db + ch, a);
 }
@@ -308,7 +399,13 @@ __global__ void mse_kernel(long long n, const float* pred, const float* target, 
 
 cudaError_t launch_to_chw(int n, int h, int w, int c, int cstride, int coff, const bf16* x, int copies, bf16* out,
                           cudaStream_t s) {
-  to_chw_kernel<<<blocks_for((long long)n * c * h * w), 256, 0, s>>>(n, h, w, c, cstride, coff, x, copies, out);
+  const size_t smem = (size_t)(TCHW_X + 2) * c * sizeof(bf16);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(to_chw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const dim3 grid((unsigned)((w + TCHW_X - 1) / TCHW_X), (unsigned)(n * h));
+  to_chw_kernel<<<grid, 256, smem, s>>>(n, h, w, c, cstride, coff, x, copies, out);
   return cudaGetLastError();
 }
 
@@ -341,33 +438,34 @@ cudaError_t launch_conv_out_bwd(int n, int h, int w, int c, const float* g, cons
 
 cudaError_t launch_pool2(int n, int h, int w, int c, const bf16* in, int cs_in, int coff_in, bf16* out,
                          cudaStream_t s) {
-  pool2_kernel<<<blocks_for((long long)n * (h / 2) * (w / 2) * c), 256, 0, s>>>(n, h, w, c, in, cs_in, coff_in, out);
+  pool2_kernel<<<blocks_for((long long)n * (h / 2) * (w / 2) * (c / 8)), 256, 0, s>>>(n, h, w, c, in, cs_in, coff_in,
+                                                                                     out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_up2(int n, int h, int w, int c, const bf16* in, bf16* out, int cs_out, int coff_out,
                        cudaStream_t s) {
-  up2_kernel<<<blocks_for((long long)n * h * w * c), 256, 0, s>>>(n, h, w, c, in, out, cs_out, coff_out);
+  up2_kernel<<<blocks_for((long long)n * h * w * (c / 8)), 256, 0, s>>>(n, h, w, c, in, out, cs_out, coff_out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_up2_bwd(int n, int h, int w, int c, const float* g, int cs_g, int coff_g, const bf16* act,
                            bf16* out, cudaStream_t s) {
-  up2_bwd_kernel<<<blocks_for((long long)n * (h / 2) * (w / 2) * c), 256, 0, s>>>(n, h, w, c, g, cs_g, coff_g, act,
-                                                                                   out);
+  up2_bwd_kernel<<<blocks_for((long long)n * (h / 2) * (w / 2) * (c / 8)), 256, 0, s>>>(n, h, w, c, g, cs_g, coff_g,
+                                                                                         act, out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_pool2_bwd(int n, int h, int w, int c, const float* gp, const float* gs, int cs_s, int coff_s,
                              const bf16* act, int cs_a, int coff_a, bf16* out, cudaStream_t s) {
-  pool2_bwd_kernel<<<blocks_for((long long)n * h * w * c), 256, 0, s>>>(n, h, w, c, gp, gs, cs_s, coff_s, act, cs_a,
-                                                                         coff_a, out);
+  pool2_bwd_kernel<<<blocks_for((long long)n * h * w * (c / 8)), 256, 0, s>>>(n, h, w, c, gp, gs, cs_s, coff_s, act,
+                                                                               cs_a, coff_a, out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_bias_grad(long long npix, int c, const bf16* dy, float* db, cudaStream_t s) {
-  const dim3 grid(64, c);
-  bias_grad_kernel<<<grid, 256, 0, s>>>(npix, c, dy, db);
+cudaError_t launch_bias_grad(int n, long long hw, int c, const bf16* dy, float* db, cudaStream_t s) {
+  const dim3 grid(32, c);
+  bias_grad_kernel<<<grid, 256, 0, s>>>(n, hw, c, dy, db);
   return cudaGetLastError();
 }
 

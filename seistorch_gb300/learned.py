@@ -155,7 +155,7 @@ class PrecondNet:
         p = N.NnWgrad(B, h, w, ci, co, N.ptr(dy_chw),
                       N.PTR3(*[x_chw.data_ptr() + 2 * k * n_x for k in range(3)]), N.ptr(self.gW[name]))
         N.call("sgb_nn_conv3x3_wgrad", ctypes.byref(p), s)
-        N.call("sgb_nn_bias_grad", B * h * w, co, N.ptr(dy), N.ptr(self.gb[name]), s)
+        N.call("sgb_nn_bias_grad", B, h * w, co, N.ptr(dy_chw), N.ptr(self.gb[name]), s)
 
     # -- forward / backward
     def forward(self, x):
