@@ -36,7 +36,6 @@ struct AcStepArgs {
   int nrec, nch;
   float* __restrict__ records;  // records + t*nrec*nch (channel 0)
   float* __restrict__ illum;
-  float* __restrict__ ring_out;  // [nshots][ring.size] of U_{n+1}, or null
   Ring ring;
   int* status;
 };
@@ -81,7 +80,6 @@ struct AcStreamArgs {
   int nrec, nch;
   float* __restrict__ records;
   float* __restrict__ illum;
-  float* __restrict__ ring_out;
   Ring ring;
   int* status;
 };
@@ -115,8 +113,7 @@ struct AcBwdStreamArgs {
   float* __restrict__ grad_shot;  // read through TMA, written here
   FdWeights w;
   int do_recon;
-  const float* __restrict__ ring_in;
-  Ring ring;
+  Ring ring;  // the undamped box: U_{j-2} is reconstructed inside it
   const int* __restrict__ src_ptr;
   const int* __restrict__ src_z;
   const int* __restrict__ src_x;

@@ -12,8 +12,8 @@
 //   * nu_j from nu_{j+1} (haloed) and nu_{j+2};
 //   * the gradient term nu_j L(U_{j-1}) inside the undamped box;
 //   * the reconstruction U_{j-2} = 2 U_{j-1} - (U_j - S w_{j-1}) + k L(U_{j-1})
-//     inside the box (g = 2 there), the saved ring outside it, 0 in the
-//     damped band.
+//     inside the box (g = 2 there), 0 outside it; the host copies the saved
+//     ring back into U_{j-2} after the launch.
 #include "stream_common.cuh"
 
 namespace sgb {
@@ -30,7 +30,7 @@ struct BwdTileLayout {
 };
 
 template <int R, int TZ, int NWP, int S>
-__global__ void __launch_bounds__(32 * NWP) acoustic_bwd_tile_kernel(
+__global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_tile_kernel(
     const __grid_constant__ CUtensorMap tm_u,     // U_{j-1}   box {W, TZ+2R, 1}
     const __grid_constant__ CUtensorMap tm_n,     // nu_{j+1}  box {W, TZ+2R, 1}
     const __grid_constant__ CUtensorMap tm_grad,  // grad_shot box {128, TZ, 1}
@@ -119,7 +119,6 @@ __global__ void __launch_bounds__(32 * NWP) acoustic_bwd_tile_kernel(
     const float* st = smem + stage * Lay::STAGE;
     const float* sn = st + Lay::UF;
     const float* sgr = st + 2 * Lay::UF;
-    const bool ring_tile = a.ring_in != nullptr && a.ring.touches(g.z0, TZ, g.x0, TX);
     const bool cols_all = x >= a.ring.ix0 && x + 3 < a.ring.ix1;
     const bool cols_any = x + 3 >= a.ring.ix0 && x < a.ring.ix1;
     const int lr0 = wid * RPW;
@@ -173,24 +172,14 @@ __global__ void __launch_bounds__(32 * NWP) acoustic_bwd_tile_kernel(
         }
         if (a.do_recon) {
           float4 uo;
-          if (zin && cols_all) {
-            uo.x = fmaf(k4.x, LU.x, fmaf(g4.x, u1.x - un.x, un.x));
-            uo.y = fmaf(k4.y, LU.y, fmaf(g4.y, u1.y - un.y, un.y));
-            uo.z = fmaf(k4.z, LU.z, fmaf(g4.z, u1.z - un.z, un.z));
-            uo.w = fmaf(k4.w, LU.w, fmaf(g4.w, u1.w - un.w, un.w));
-          } else {
+          uo.x = fmaf(k4.x, LU.x, fmaf(g4.x, u1.x - un.x, un.x));
+          uo.y = fmaf(k4.y, LU.y, fmaf(g4.y, u1.y - un.y, un.y));
+          uo.z = fmaf(k4.z, LU.z, fmaf(g4.z, u1.z - un.z, un.z));
+          uo.w = fmaf(k4.w, LU.w, fmaf(g4.w, u1.w - un.w, un.w));
+          if (!(zin && cols_all)) {  // 0 outside the box; the host writes the saved ring after
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-              const int xm = x + m;
-              float v = 0.f;
-              if (a.ring.inside(z, xm)) {
-                v = fmaf(comp(k4, m), comp(LU, m), fmaf(comp(g4, m), comp(u1, m) - comp(un, m), comp(un, m)));
-              } else if (ring_tile && xm < a.nx) {
-                const int ri = a.ring.index(z, xm);
-                if (ri >= 0) v = a.ring_in[(long long)g.b * a.ring.size + ri];
-              }
-              set_comp(uo, m, v);
-            }
+            for (int m = 0; m < 4; ++m)
+              if (!(zin && x + m >= a.ring.ix0 && x + m < a.ring.ix1)) set_comp(uo, m, 0.f);
           }
           *reinterpret_cast<float4*>(a.uout + goff) = uo;
         }

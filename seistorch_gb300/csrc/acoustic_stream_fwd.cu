@@ -1,7 +1,7 @@
 // Forward step of the acoustic PML equation as a TMA tile pipeline (see
 // stream_common.cuh): u+ = g (u - u-) + u- + k L(u) (acoustic.py:73-86),
-// with source injection (source.py:47-57), receiver sampling (probe.py:42-44),
-// the boundary ring for the adjoint and the illumination sum fused in.
+// with source injection (source.py:47-57), receiver sampling (probe.py:42-44)
+// and the illumination sum fused in.
 #include "stream_common.cuh"
 
 namespace sgb {
@@ -125,7 +125,6 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
     }
     if (!mbar_wait(&bars[stage], (k / S) & 1, a.status)) s_abort = 1;
     const float* st = smem + stage * Lay::STAGE;
-    const bool ring_tile = a.ring_out != nullptr && a.ring.touches(g.z0, TZ, g.x0, TX);
     const int lr0 = wid * RPW;
 #pragma unroll
     for (int sb = 0; sb < SB; ++sb) {
@@ -163,13 +162,6 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
         if (src.mask) apply_sources(src, i, lane, 1.f, y);
         if (z < a.nz && xin) {
           *reinterpret_cast<float4*>(outp) = y;
-          if (ring_tile) {
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-              const int ri = (x + m < a.nx) ? a.ring.index(z, x + m) : -1;
-              if (ri >= 0) a.ring_out[(long long)b * a.ring.size + ri] = comp(y, m);
-            }
-          }
           if (a.illum != nullptr) {
 #pragma unroll
             for (int m = 0; m < 4; ++m)

@@ -56,6 +56,8 @@ cudaError_t launch_acoustic_fwd(int R, bool habc, int tz, const AcStepArgs& a, c
 cudaError_t launch_acoustic_vjp(int R, const AcVjpArgs& a, cudaStream_t s);
 cudaError_t launch_acoustic_coef(const sgb_grid& gr, const float* vp, const float* damp, int boundary,
                                  float* g, float* k, cudaStream_t s);
+cudaError_t launch_ring_copy(const sgb_grid& gr, const Ring& ring, float* field, float* slots, bool scatter,
+                             cudaStream_t s);
 cudaError_t launch_acoustic_grad_reduce(const sgb_grid& gr, const float* grad_shot, const float* vp,
                                         const Ring& ring, float* grad_vp, cudaStream_t s);
 int pick_tz(int nz, int nx, int nshots, int tz_max);
@@ -299,7 +301,6 @@ int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, 
     a.un = buf[nxt];
     a.t = t;
     a.records = acq->records ? acq->records + (long long)t * acq->nrec * acq->nch : nullptr;
-    a.ring_out = bs ? bs->ring_store + (long long)t * grid->nshots * a.ring.size : nullptr;
     if (habc) {
       SGB_CUDA_CHECK(launch_acoustic_fwd(R, habc, tz, a, s));
     } else {
@@ -307,10 +308,12 @@ int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, 
       sa.um = buf[prev];
       sa.t = t;
       sa.records = a.records;
-      sa.ring_out = a.ring_out;
       const CUtensorMap maps[2] = {mu[cur], mum[prev]};
       SGB_CUDA_CHECK(launch_acoustic_fwd_stream(R, maps, sa, s));
     }
+    if (bs != nullptr)  // boundary ring of U_{t+1}
+      SGB_CUDA_CHECK(launch_ring_copy(*grid, a.ring, buf[nxt], bs->ring_store + (long long)t * grid->nshots * a.ring.size,
+                                      false, s));
     if (bs != nullptr && bs->ckpt_every > 0 && (t + 1) % bs->ckpt_every == 0) {
       float* slot = bs->ckpt_store + (long long)((t + 1) / bs->ckpt_every - 1) * 2 * field;
       SGB_CUDA_CHECK(cudaMemcpyAsync(slot, buf[nxt], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
@@ -436,11 +439,13 @@ int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model,
     sb.unext = ubuf[uj];
     sb.n2 = lbuf[l2];
     sb.do_recon = j >= 3;
-    sb.ring_in = j >= 3 ? bs->ring_store + (long long)(j - 3) * grid->nshots * ring.size : nullptr;
     sb.t_src = j - 1;
     sb.resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
     const CUtensorMap maps[3] = {uf[ujm1], nf[l1], mgrad};
     SGB_CUDA_CHECK(launch_acoustic_bwd_stream(R, maps, sb, s));
+    if (j >= 3)  // the saved ring of U_{j-2} (the kernel leaves 0 outside the box)
+      SGB_CUDA_CHECK(launch_ring_copy(*grid, ring, ubuf[ufree], bs->ring_store + (long long)(j - 3) * grid->nshots * ring.size,
+                                      true, s));
     if (ck && j >= 3) {
       const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
       SGB_CUDA_CHECK(cudaMemcpyAsync(ubuf[ufree], slot + field, field * sizeof(float), cudaMemcpyDeviceToDevice, s));
