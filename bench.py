@@ -310,9 +310,8 @@ def main():
         "roofline_forward": {"kernel": "acoustic_fwd_tile_kernel", "achieved": fwd_bytes / (fwd_launch_ms * 1e-3) / 1e9,
                              "frac": fwd_bytes / (fwd_launch_ms * 1e-3) / 1e9 / peak, "unit": "GB/s",
                              "launch_ms": fwd_launch_ms},
-        # per step: NT forward + NT ring gathers, NT-1 reverse + NT-2 ring scatters,
-        # coefficients, misfit, gradient reduction
-        "gpu_launches": args.steps * (2 * NT + (NT - 1) + (NT - 2) + 3),
+        # per step: NT forward, NT-1 reverse, coefficients, misfit, gradient reduction
+        "gpu_launches": args.steps * (NT + (NT - 1) + 3),
         "clocks": clocks.summary(),
     }
     if not args.no_e2e:

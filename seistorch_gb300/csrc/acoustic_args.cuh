@@ -81,6 +81,10 @@ struct AcStreamArgs {
   float* __restrict__ records;
   float* __restrict__ illum;
   Ring ring;
+  // boundary ring of the input field U_n (read-only in this launch) into
+  // ring_dst [nshots][ring.size], or null; single-grid launches only
+  const float* __restrict__ ring_src;
+  float* __restrict__ ring_dst;
   int* status;
 };
 
@@ -113,7 +117,8 @@ struct AcBwdStreamArgs {
   float* __restrict__ grad_shot;  // read through TMA, written here
   FdWeights w;
   int do_recon;
-  Ring ring;  // the undamped box: U_{j-2} is reconstructed inside it
+  Ring ring;  // U_{j-2} is reconstructed inside the box; its ring cells come from ring_in
+  const float* __restrict__ ring_in;  // ring of U_{j-2} [nshots][ring.size], or null
   const int* __restrict__ src_ptr;
   const int* __restrict__ src_z;
   const int* __restrict__ src_x;

@@ -12,8 +12,8 @@
 //   * nu_j from nu_{j+1} (haloed) and nu_{j+2};
 //   * the gradient term nu_j L(U_{j-1}) inside the undamped box;
 //   * the reconstruction U_{j-2} = 2 U_{j-1} - (U_j - S w_{j-1}) + k L(U_{j-1})
-//     inside the box (g = 2 there), 0 outside it; the host copies the saved
-//     ring back into U_{j-2} after the launch.
+//     inside the box (g = 2 there), the saved ring around it (each CTA
+//     copies a share after its tiles), 0 in the damped band.
 #include "stream_common.cuh"
 
 namespace sgb {
@@ -176,12 +176,19 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_
           uo.y = fmaf(k4.y, LU.y, fmaf(g4.y, u1.y - un.y, un.y));
           uo.z = fmaf(k4.z, LU.z, fmaf(g4.z, u1.z - un.z, un.z));
           uo.w = fmaf(k4.w, LU.w, fmaf(g4.w, u1.w - un.w, un.w));
-          if (!(zin && cols_all)) {  // 0 outside the box; the host writes the saved ring after
+          if (zin && cols_all) {
+            *reinterpret_cast<float4*>(a.uout + goff) = uo;
+          } else {
+            // 0 outside the box, ring cells left to the ring scatter below
+            const bool zr = z >= a.ring.iz0 - a.ring.rt && z < a.ring.iz1 + a.ring.rb;
 #pragma unroll
-            for (int m = 0; m < 4; ++m)
-              if (!(zin && x + m >= a.ring.ix0 && x + m < a.ring.ix1)) set_comp(uo, m, 0.f);
+            for (int m = 0; m < 4; ++m) {
+              const int xm = x + m;
+              const bool inbox = zin && xm >= a.ring.ix0 && xm < a.ring.ix1;
+              const bool ring = !inbox && zr && xm >= a.ring.ix0 - a.ring.rl && xm < a.ring.ix1 + a.ring.rr;
+              if (!ring) a.uout[goff + m] = inbox ? comp(uo, m) : 0.f;
+            }
           }
-          *reinterpret_cast<float4*>(a.uout + goff) = uo;
         }
       }
 #pragma unroll
@@ -193,9 +200,16 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_
     if (__syncthreads_or(s_abort)) break;  // stage free
     if (tid == 0 && t + S * G < ntiles) issue(t + S * G, stage);
   }
-  if (s_abort && tid == 0)
-    for (int q = k; q < k + S; ++q)
-      if ((int)blockIdx.x + q * G < ntiles) mbar_wait(&bars[q % S], (q / S) & 1, nullptr);
+  if (s_abort) {
+    if (tid == 0)
+      for (int q = k; q < k + S; ++q)
+        if ((int)blockIdx.x + q * G < ntiles) mbar_wait(&bars[q % S], (q / S) & 1, nullptr);
+    return;
+  }
+  // the saved ring of U_{j-2}; the tiles above never write ring cells, and
+  // nothing in this launch reads U_{j-2}
+  if (a.do_recon && a.ring_in != nullptr)
+    ring_copy_share(a.ring, a.nshots, a.pitch, a.sstride, a.uout, const_cast<float*>(a.ring_in), true);
 }
 
 // ------------------------------------------------------------- launch ---

@@ -1,7 +1,7 @@
 // Forward step of the acoustic PML equation as a TMA tile pipeline (see
 // stream_common.cuh): u+ = g (u - u-) + u- + k L(u) (acoustic.py:73-86),
-// with source injection (source.py:47-57), receiver sampling (probe.py:42-44)
-// and the illumination sum fused in.
+// with source injection (source.py:47-57), receiver sampling (probe.py:42-44),
+// the illumination sum and the saving of the input's boundary ring fused in.
 #include "stream_common.cuh"
 
 namespace sgb {
@@ -203,6 +203,10 @@ __global__ void __launch_bounds__(32 * NWP) acoustic_fwd_tile_kernel(const __gri
                                                                      const __grid_constant__ CUtensorMap tm_um,
                                                                      const AcStreamArgs a) {
   fwd_tiles<R, TZ, NWP, S, PT, SB>(FwdOne<SB>{&tm_u, &tm_um, a});
+  // the input field's boundary ring for the adjoint, spread over the CTAs'
+  // tails (the input is read-only in this launch)
+  if (a.ring_dst != nullptr)
+    ring_copy_share(a.ring, a.nshots, a.pitch, a.sstride, const_cast<float*>(a.ring_src), a.ring_dst, false);
 }
 
 template <int R, int TZ, int NWP, int S, bool PT, int MAXG>

@@ -308,10 +308,15 @@ int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, 
       sa.um = buf[prev];
       sa.t = t;
       sa.records = a.records;
+      // the step saves the ring of its input U_t into slot t-1 (the adjoint
+      // reads the rings of U_1 .. U_{nt-2})
+      sa.ring_src = buf[cur];
+      sa.ring_dst = (bs != nullptr && t >= 1) ? bs->ring_store + (long long)(t - 1) * grid->nshots * a.ring.size
+                                              : nullptr;
       const CUtensorMap maps[2] = {mu[cur], mum[prev]};
       SGB_CUDA_CHECK(launch_acoustic_fwd_stream(R, maps, sa, s));
     }
-    if (bs != nullptr)  // boundary ring of U_{t+1}
+    if (habc && bs != nullptr)  // ring of U_{t+1} into slot t
       SGB_CUDA_CHECK(launch_ring_copy(*grid, a.ring, buf[nxt], bs->ring_store + (long long)t * grid->nshots * a.ring.size,
                                       false, s));
     if (bs != nullptr && bs->ckpt_every > 0 && (t + 1) % bs->ckpt_every == 0) {
@@ -442,10 +447,8 @@ int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model,
     sb.t_src = j - 1;
     sb.resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
     const CUtensorMap maps[3] = {uf[ujm1], nf[l1], mgrad};
+    sb.ring_in = j >= 3 ? bs->ring_store + (long long)(j - 3) * grid->nshots * ring.size : nullptr;
     SGB_CUDA_CHECK(launch_acoustic_bwd_stream(R, maps, sb, s));
-    if (j >= 3)  // the saved ring of U_{j-2} (the kernel leaves 0 outside the box)
-      SGB_CUDA_CHECK(launch_ring_copy(*grid, ring, ubuf[ufree], bs->ring_store + (long long)(j - 3) * grid->nshots * ring.size,
-                                      true, s));
     if (ck && j >= 3) {
       const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
       SGB_CUDA_CHECK(cudaMemcpyAsync(ubuf[ufree], slot + field, field * sizeof(float), cudaMemcpyDeviceToDevice, s));

@@ -70,30 +70,6 @@ struct Ring {
     }
     return -1;
   }
-  // Ring slots of one row: column x of row z is slot b0 + x when
-  // l0 <= x < h0, slot b1 + x when l1 <= x < h1, no slot otherwise (the
-  // same numbering as index(), with the row tests taken once per row).
-  struct RowSlots {
-    int b0, l0, h0, b1, l1, h1;
-    __host__ __device__ int slot(int x) const {
-      return (x >= l0 && x < h0) ? b0 + x : ((x >= l1 && x < h1) ? b1 + x : -1);
-    }
-  };
-  __host__ __device__ RowSlots row_slots(int z) const {
-    const int W = width();
-    const int xa = ix0 - rl, xb = ix1 + rr;
-    RowSlots s{0, 0, 0, 0, 0, 0};
-    if (z >= iz0 - rt && z < iz0) {
-      s.b0 = (z - (iz0 - rt)) * W - xa; s.l0 = xa; s.h0 = xb;
-    } else if (z >= iz1 && z < iz1 + rb) {
-      s.b0 = (rt + z - iz1) * W - xa; s.l0 = xa; s.h0 = xb;
-    } else if (z >= iz0 && z < iz1) {
-      const int base = (rt + rb) * W;
-      s.b0 = base + (z - iz0) * rl - xa; s.l0 = xa; s.h0 = ix0;
-      s.b1 = base + (iz1 - iz0) * rl + (z - iz0) * rr - ix1; s.l1 = ix1; s.h1 = xb;
-    }
-    return s;
-  }
   // The cell (z, x) of slot ri in [0, size): the inverse of index().
   __host__ __device__ void cell(int ri, int& z, int& x) const {
     const int W = width();

@@ -121,6 +121,25 @@ __device__ __forceinline__ void apply_sources(const WarpSrc& s, int i, int lane,
   }
 }
 
+// This CTA's share of a boundary-ring copy between a field
+// [nshots][nz][pitch] and its slots [nshots][ring.size] (slot order of
+// Ring::index): scatter = slots -> field, else field -> slots.
+__device__ __forceinline__ void ring_copy_share(const Ring& ring, int nshots, int pitch, long long sstride,
+                                                float* field, float* slots, bool scatter) {
+  const long long n = (long long)nshots * ring.size;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(i / ring.size);
+    int z, x;
+    ring.cell((int)(i - (long long)b * ring.size), z, x);
+    float* f = field + b * sstride + (long long)z * pitch + x;
+    if (scatter)
+      *f = slots[i];
+    else
+      slots[i] = *f;
+  }
+}
+
 template <class Kern>
 static int resident_blocks(Kern kern, int threads, size_t smem) {
   int nb = 0;
