@@ -189,6 +189,44 @@ int sgb_acoustic_backward_noalloc(const sgb_grid *grid, const sgb_acoustic_model
                                   float *const ubuf[3], int32_t ucur, int32_t uprev, float *grad_vp,
                                   sgb_stream_t stream);
 
+/* --------------------------------------------------- Born modelling --- */
+
+/* Born (linearised) modelling of the acoustic HABC equation for
+ * least-squares RTM: the loop of acoustic_lsrtm_habc._time_step
+ * (seistorch/equations2d/acoustic_lsrtm_habc.py:11-30) with its sources on
+ * the background field h1 and its receivers on the scattered field sh1
+ * (examples/lsrtm/acoustic/configs/lsrtm.yml).  Per step:
+ *   p+ = HABC(2p - p- + k L(p)) + sources,
+ *   s+ = HABC(2s - s- + k L(s) + m k L(p)),   records sample s+;
+ * model->boundary must be 1 (HABC), m is the reflectivity plane
+ * [nz][pitch].  pbuf / sbuf: the background and scattered fields' three
+ * rotating buffers (zeroed here; both rotate together, so cur_out /
+ * prev_out name U_nt / U_{nt-1} of both); born_src: scratch
+ * [nshots][nz][pitch].  bs (optional) saves the background's boundary ring
+ * and checkpoints for sgb_born_backward. */
+int sgb_born_forward(const sgb_grid *grid, const sgb_acoustic_model *model, const float *m,
+                     const sgb_acquisition *acq, float *const pbuf[3], float *const sbuf[3],
+                     float *born_src, const sgb_bs_store *bs, int32_t *cur_out, int32_t *prev_out,
+                     sgb_stream_t stream);
+
+/* One step of the same pair of fields without sources or receivers (the
+ * per-step equation-module drop-in, acoustic_lsrtm_habc._time_step):
+ * pnext = HABC step of (p, pm), snext = HABC step of (sc, scm) + m k L(p);
+ * born_src: scratch [nshots][nz][pitch]. */
+int sgb_born_step(const sgb_grid *grid, const sgb_acoustic_model *model, const float *m, const float *p,
+                  const float *pm, const float *sc, const float *scm, float *pnext, float *snext,
+                  float *born_src, sgb_stream_t stream);
+
+/* dJ/dm of sgb_born_forward (the reference's autograd gradient of the
+ * reflectivity, the velocity held fixed as in lsrtm.yml's invlist): the
+ * exact HABC adjoint of the scattered field, driven by dJ/d(records) in
+ * acq->records, against the background field reconstructed from
+ * pbuf[pcur] / pbuf[pprev] and bs; grad_m = sum_t La k L(p) inside the
+ * undamped box, 0 outside it.  lbuf, grad_shot: as in sgb_acoustic_backward. */
+int sgb_born_backward(const sgb_grid *grid, const sgb_acoustic_model *model, const sgb_acquisition *acq,
+                      const sgb_bs_store *bs, float *const pbuf[3], int32_t pcur, int32_t pprev,
+                      float *const lbuf[3], float *grad_shot, float *grad_m, sgb_stream_t stream);
+
 /* ------------------------------------------------------ uneven batch --- */
 
 /* One grid of an uneven batch: its own shape and shots (grid), PML model,

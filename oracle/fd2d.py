@@ -251,6 +251,23 @@ def acoustic_habc_step(vp, h1, h2, dt, h, b, order, multiple=False, dtype=np.flo
     return y, np.asarray(h1, dtype)
 
 
+def born_habc_step(vp, m, h1, h2, sh1, sh2, dt, h, b, order, multiple=False, dtype=np.float64):
+    """Born modelling step (acoustic_lsrtm_habc.py:11-30): background
+    p0 = 2 h1 - h2 + vp^2 lap(h1) dt^2, scattered
+    sh0 = 2 sh1 - sh2 + vp^2 lap(sh1) dt^2 + m vp^2 lap(h1) dt^2, each then
+    blended by the HABC of its own field.  Returns (p0, h1, sh0, sh1)."""
+    vp = np.asarray(vp, dtype)
+    m = np.asarray(m, dtype)
+    dt_ = dtype(dt)
+    vp2_lap_p = vp ** 2 * laplacian(h1, order, h, dtype)
+    p0 = 2 * np.asarray(h1, dtype) - np.asarray(h2, dtype) + vp2_lap_p * dt_ ** 2
+    s0 = (2 * np.asarray(sh1, dtype) - np.asarray(sh2, dtype) + vp ** 2 * laplacian(sh1, order, h, dtype) * dt_ ** 2
+          + m * vp2_lap_p * dt_ ** 2)
+    p0 = habc_apply(p0, h1, h2, vp, b, dt, h, 50, multiple, dtype)
+    s0 = habc_apply(s0, sh1, sh2, vp, b, dt, h, 50, multiple, dtype)
+    return p0, np.asarray(h1, dtype), s0, np.asarray(sh1, dtype)
+
+
 def dfwd(a, axis):
     """a[i] - a[i-1], zero at index 0 (equations2d/utils.py:3-25, forward)."""
     out = a - np.roll(a, 1, axis=axis)
@@ -298,8 +315,9 @@ def elastic_step(vp, vs, rho, vx, vz, txx, tzz, txz, dt, h, d, dtype=np.float64)
 # ----------------------------------------------------------- time loop ---
 
 WAVEFIELDS = {"acoustic": ["h1", "h2"], "acoustic_habc": ["h1", "h2"],
+              "acoustic_lsrtm_habc": ["h1", "h2", "sh1", "sh2"],
               "elastic": ["vx", "vz", "txx", "tzz", "txz"]}
-MODEL_PARAMS = {"acoustic": ["vp"], "acoustic_habc": ["vp"],
+MODEL_PARAMS = {"acoustic": ["vp"], "acoustic_habc": ["vp"], "acoustic_lsrtm_habc": ["vp", "m"],
                 "elastic": ["vp", "vs", "rho"]}
 
 
@@ -341,6 +359,10 @@ def forward(equation, models, d, dt, h, wavelet, sources, receivers, *,
             y, h1 = acoustic_habc_step(models["vp"], fields["h1"], fields["h2"], dt, h, d, order,
                                        multiple, dtype)
             fields["h1"], fields["h2"] = y, h1
+        elif equation == "acoustic_lsrtm_habc":
+            out = born_habc_step(models["vp"], models["m"], fields["h1"], fields["h2"], fields["sh1"],
+                                 fields["sh2"], dt, h, d, order, multiple, dtype)
+            fields = dict(zip(names, out))
         elif equation == "elastic":
             out = elastic_step(models["vp"], models["vs"], models["rho"],
                                *[fields[n] for n in names], dt, h, d, dtype)

@@ -206,6 +206,16 @@ __global__ void __launch_bounds__(NTHREADS) acoustic_fwd_kernel(const AcStepArgs
     y.z = fmaf(vk.z, L.z, fmaf(vg.z, win[R].z - vm.z, vm.z));
     y.w = fmaf(vk.w, L.w, fmaf(vg.w, win[R].w - vm.w, vm.w));
     if (z < a.nz && x < a.nx) {
+      const long long po = (long long)z * a.pitch + x;
+      if (a.born_out != nullptr) {  // m k L(u): the scattered field's source
+        const float4 mm = *reinterpret_cast<const float4*>(a.born_m + po);
+        *reinterpret_cast<float4*>(a.born_out + base + po) =
+            make_float4(mm.x * (vk.x * L.x), mm.y * (vk.y * L.y), mm.z * (vk.z * L.z), mm.w * (vk.w * L.w));
+      }
+      if (a.born_in != nullptr) {
+        const float4 sb = *reinterpret_cast<const float4*>(a.born_in + base + po);
+        y = make_float4(y.x + sb.x, y.y + sb.y, y.z + sb.z, y.w + sb.w);
+      }
       if (HABC) {
 #pragma unroll
         for (int m = 0; m < 4; ++m)
@@ -365,7 +375,7 @@ __global__ void acoustic_grad_reduce_kernel(int nz, int nx, int pitch, int nshot
     if (x < nx && ring.inside(z, x)) {
       // the adjoint is carried as nu = k * Lambda: dJ/dvp = (2/vp) sum nu L(U)
       for (int b = 0; b < nshots; ++b) s += grad_shot[b * sstride + i];
-      s *= 2.f / vp[i];
+      if (vp != nullptr) s *= 2.f / vp[i];  // without vp: the sum itself (dJ/dm of Born)
     }
     grad_vp[i] = s;
   }

@@ -37,6 +37,12 @@ struct AcStepArgs {
   float* __restrict__ records;  // records + t*nrec*nch (channel 0)
   float* __restrict__ illum;
   Ring ring;
+  // Born modelling (acoustic_lsrtm_habc.py:11-30): the background step
+  // writes born_out = born_m k L(u) (per shot); the scattered step adds
+  // born_in to its interior update before the boundary blend.  Null otherwise.
+  const float* __restrict__ born_m;  // [nz][pitch]
+  float* __restrict__ born_out;      // [nshots][nz][pitch]
+  const float* __restrict__ born_in;  // [nshots][nz][pitch]
   int* status;
 };
 

@@ -58,6 +58,9 @@ cudaError_t launch_acoustic_coef(const sgb_grid& gr, const float* vp, const floa
                                  float* g, float* k, cudaStream_t s);
 cudaError_t launch_ring_copy(const sgb_grid& gr, const Ring& ring, float* field, float* slots, bool scatter,
                              cudaStream_t s);
+int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
+                           const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur, int32_t uprev,
+                           float* const lbuf[3], float* grad_shot, float* grad_vp, bool born, cudaStream_t s);
 cudaError_t launch_acoustic_grad_reduce(const sgb_grid& gr, const float* grad_shot, const float* vp,
                                         const Ring& ring, float* grad_vp, cudaStream_t s);
 int pick_tz(int nz, int nx, int nshots, int tz_max);
@@ -333,9 +336,149 @@ int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, 
   return SGB_OK;
 }
 
+int sgb_born_forward(const sgb_grid* grid, const sgb_acoustic_model* model, const float* m,
+                     const sgb_acquisition* acq, float* const pbuf[3], float* const sbuf[3], float* born_src,
+                     const sgb_bs_store* bs, int32_t* cur_out, int32_t* prev_out, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (int e = check_model(grid, model)) return e;
+  if (int e = check_acq(grid, acq)) return e;
+  if (model->boundary != 1) return SGB_ERR_UNSUPPORTED;  // the reference's Born equation is HABC
+  if (model->vp == nullptr || model->damp == nullptr) return SGB_ERR_ARG;
+  if (m == nullptr || born_src == nullptr || pbuf == nullptr || sbuf == nullptr || cur_out == nullptr ||
+      prev_out == nullptr)
+    return SGB_ERR_ARG;
+  if (!aligned16(m) || !aligned16(born_src)) return SGB_ERR_ALIGN;
+  for (int i = 0; i < 3; ++i) {
+    if (pbuf[i] == nullptr || sbuf[i] == nullptr) return SGB_ERR_ARG;
+    if (!aligned16(pbuf[i]) || !aligned16(sbuf[i])) return SGB_ERR_ALIGN;
+  }
+  if (acq->records != nullptr && acq->nch != 1) return SGB_ERR_UNSUPPORTED;
+  cudaStream_t s = (cudaStream_t)stream;
+  // background: sources, no receivers, writes m k L(p); scattered: receivers
+  AcStepArgs ap = base_step_args(grid, model);
+  ap.src_ptr = acq->nsrc > 0 ? acq->src_ptr : nullptr;
+  ap.src_z = acq->src_z;
+  ap.src_x = acq->src_x;
+  ap.src_wrow = acq->src_wrow;
+  ap.wavelet = acq->wavelet;
+  ap.nt = acq->nt;
+  ap.born_m = m;
+  ap.born_out = born_src;
+  AcStepArgs as = base_step_args(grid, model);
+  as.nt = acq->nt;
+  as.rec_row_ptr = acq->rec_row_ptr;
+  as.rec_x = acq->rec_x;
+  as.rec_col = acq->rec_col;
+  as.nrec = acq->nrec;
+  as.nch = acq->nch;
+  as.born_in = born_src;
+  const long long plane = (long long)grid->nz * grid->pitch;
+  const long long field = plane * grid->nshots;
+  Ring ring{};
+  if (bs != nullptr) {  // boundary store of the background field
+    if (bs->ring < 1 || bs->ring_store == nullptr) return SGB_ERR_ARG;
+    if (bs->iz0 < 0 || bs->ix0 < 0 || bs->iz1 > grid->nz || bs->ix1 > grid->nx || bs->iz0 >= bs->iz1 ||
+        bs->ix0 >= bs->ix1)
+      return SGB_ERR_SHAPE;
+    ring = make_ring(*grid, bs->iz0, bs->iz1, bs->ix0, bs->ix1, bs->ring);
+    if (ring.size != bs->ring_size) return SGB_ERR_SHAPE;
+    if (bs->ckpt_every > 0 && bs->ckpt_store == nullptr) return SGB_ERR_ARG;
+  }
+  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 32);
+  const int R = model->order / 2;
+  for (int i = 0; i < 3; ++i) {
+    SGB_CUDA_CHECK(cudaMemsetAsync(pbuf[i], 0, field * sizeof(float), s));
+    SGB_CUDA_CHECK(cudaMemsetAsync(sbuf[i], 0, field * sizeof(float), s));
+  }
+  int cur = 0, prev = 1, nxt = 2;
+  for (int t = 0; t < acq->nt; ++t) {
+    ap.u = pbuf[cur];
+    ap.um = pbuf[prev];
+    ap.un = pbuf[nxt];
+    ap.t = t;
+    SGB_CUDA_CHECK(launch_acoustic_fwd(R, true, tz, ap, s));
+    as.u = sbuf[cur];
+    as.um = sbuf[prev];
+    as.un = sbuf[nxt];
+    as.t = t;
+    as.records = acq->records ? acq->records + (long long)t * acq->nrec * acq->nch : nullptr;
+    SGB_CUDA_CHECK(launch_acoustic_fwd(R, true, tz, as, s));
+    if (bs != nullptr) {
+      SGB_CUDA_CHECK(launch_ring_copy(*grid, ring, pbuf[nxt], bs->ring_store + (long long)t * grid->nshots * ring.size,
+                                      false, s));
+      if (bs->ckpt_every > 0 && (t + 1) % bs->ckpt_every == 0) {
+        float* slot = bs->ckpt_store + (long long)((t + 1) / bs->ckpt_every - 1) * 2 * field;
+        SGB_CUDA_CHECK(cudaMemcpyAsync(slot, pbuf[nxt], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        SGB_CUDA_CHECK(cudaMemcpyAsync(slot + field, pbuf[cur], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      }
+    }
+    prev = cur;
+    cur = nxt;
+    nxt = 3 - prev - cur;
+  }
+  *cur_out = cur;
+  *prev_out = prev;
+  return SGB_OK;
+}
+
+int sgb_born_step(const sgb_grid* grid, const sgb_acoustic_model* model, const float* m, const float* p,
+                  const float* pm, const float* sc, const float* scm, float* pnext, float* snext, float* born_src,
+                  sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (int e = check_model(grid, model)) return e;
+  if (model->boundary != 1) return SGB_ERR_UNSUPPORTED;
+  if (model->vp == nullptr || model->damp == nullptr) return SGB_ERR_ARG;
+  const float* in[6] = {m, p, pm, sc, scm, born_src};
+  for (const float* q : in) {
+    if (q == nullptr) return SGB_ERR_ARG;
+    if (!aligned16(q)) return SGB_ERR_ALIGN;
+  }
+  if (pnext == nullptr || snext == nullptr) return SGB_ERR_ARG;
+  if (!aligned16(pnext) || !aligned16(snext)) return SGB_ERR_ALIGN;
+  if (pnext == p || pnext == pm || snext == sc || snext == scm) return SGB_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 32);
+  AcStepArgs a = base_step_args(grid, model);
+  a.u = p;
+  a.um = pm;
+  a.un = pnext;
+  a.born_m = m;
+  a.born_out = born_src;
+  SGB_CUDA_CHECK(launch_acoustic_fwd(model->order / 2, true, tz, a, s));
+  AcStepArgs b = base_step_args(grid, model);
+  b.u = sc;
+  b.um = scm;
+  b.un = snext;
+  b.born_in = born_src;
+  SGB_CUDA_CHECK(launch_acoustic_fwd(model->order / 2, true, tz, b, s));
+  return SGB_OK;
+}
+
+int sgb_born_backward(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
+                      const sgb_bs_store* bs, float* const pbuf[3], int32_t pcur, int32_t pprev, float* const lbuf[3],
+                      float* grad_shot, float* grad_m, sgb_stream_t stream) {
+  return sgb::acoustic_backward_impl(grid, model, acq, bs, pbuf, pcur, pprev, lbuf, grad_shot, grad_m, true,
+                                     (cudaStream_t)stream);
+}
+
 int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                           const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur, int32_t uprev,
                           float* const lbuf[3], float* grad_shot, float* grad_vp, sgb_stream_t stream) {
+  return sgb::acoustic_backward_impl(grid, model, acq, bs, ubuf, ucur, uprev, lbuf, grad_shot, grad_vp, false,
+                                     (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+namespace sgb {
+
+// The reverse loop of sgb_acoustic_backward; with `born` (HABC only) the
+// adjoint runs the scattered field's recursion against the background's
+// reconstruction and the reduction returns sum La k L(U) (dJ/dm of Born
+// modelling) instead of (2/vp) times it (dJ/dvp).
+int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
+                           const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur, int32_t uprev,
+                           float* const lbuf[3], float* grad_shot, float* grad_vp, bool born, cudaStream_t s) {
   if (int e = check_grid(grid)) return e;
   if (int e = check_model(grid, model)) return e;
   if (int e = check_acq(grid, acq)) return e;
@@ -351,7 +494,8 @@ int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model,
   }
   if (!aligned16(grad_shot)) return SGB_ERR_ALIGN;
   if (acq->records != nullptr && acq->nch != 1) return SGB_ERR_UNSUPPORTED;
-  cudaStream_t s = (cudaStream_t)stream;
+  if (born && model->boundary != 1) return SGB_ERR_UNSUPPORTED;
+  const float* gscale = born ? nullptr : model->vp;
   const long long plane = (long long)grid->nz * grid->pitch;
   const long long field = plane * grid->nshots;
   const Ring ring = make_ring(*grid, bs->iz0, bs->iz1, bs->ix0, bs->ix1, bs->ring);
@@ -392,7 +536,7 @@ int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model,
       l1 = lfree;
       lfree = old_l2;
     }
-    SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, model->vp, ring, grad_vp, s));
+    SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, gscale, ring, grad_vp, s));
     return SGB_OK;
   }
   // tensor maps: haloed stencil boxes (136 x (TZ+2R)) and point boxes
@@ -462,8 +606,8 @@ int sgb_acoustic_backward(const sgb_grid* grid, const sgb_acoustic_model* model,
     l1 = lfree;
     lfree = old_l2;
   }
-  SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, model->vp, ring, grad_vp, s));
+  SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, gscale, ring, grad_vp, s));
   return SGB_OK;
 }
 
-}  // extern "C"
+}  // namespace sgb

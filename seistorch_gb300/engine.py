@@ -231,25 +231,7 @@ class AcousticPropagator:
         state = AcousticState()
         bs_struct = None
         if save_for_adjoint:
-            iz0, iz1, ix0, ix1 = interior_box(self.nz, self.nx, self.bwidth, self.multiple)
-            if iz1 <= iz0 or ix1 <= ix0:
-                raise ValueError("grid too small for its boundary width")
-            dpl = keep[1][:, :self.nx]
-            if torch.count_nonzero(dpl[iz0:iz1, ix0:ix1]).item() != 0:
-                raise ValueError("the damping profile is not zero inside the interior box; "
-                                 "boundary-saving reconstruction needs an undamped interior")
-            r = self.order // 2
-            size = ctypes.c_int32(0)
-            g1 = self.grid(B)
-            N.call("sgb_ring_size", ctypes.byref(g1), iz0, iz1, ix0, ix1, r, ctypes.byref(size))
-            state.ring_store = torch.empty(acq.nt, B, max(size.value, 1), dtype=torch.float32, device=dev)
-            K = int(ckpt_every) if ckpt_every else 0
-            nslots = acq.nt // K if K > 0 else 0
-            state.ckpt_store = (torch.empty(max(nslots, 1), 2, *field, dtype=torch.float32, device=dev)
-                                if K > 0 else None)
-            bs_struct = N.BsStore(iz0, iz1, ix0, ix1, r, size.value, N.ptr(state.ring_store), K,
-                                  N.ptr(state.ckpt_store))
-            state.bs = bs_struct
+            bs_struct = self._boundary_store(state, keep, B, acq.nt, ckpt_every, field, dev)
         cur = ctypes.c_int32(0)
         prev = ctypes.c_int32(0)
         g = self.grid(B)
@@ -262,6 +244,28 @@ class AcousticPropagator:
         state.keep = keep
         state.model = m
         return records[:, :acq.nrec], state, (illum[:, :self.nx] if illum is not None else None)
+
+    def _boundary_store(self, state, keep, B, nt, ckpt_every, field, dev):
+        """Ring store [nt][shots][ring] and checkpoints for the adjoint."""
+        iz0, iz1, ix0, ix1 = interior_box(self.nz, self.nx, self.bwidth, self.multiple)
+        if iz1 <= iz0 or ix1 <= ix0:
+            raise ValueError("grid too small for its boundary width")
+        dpl = keep[1][:, :self.nx]
+        if torch.count_nonzero(dpl[iz0:iz1, ix0:ix1]).item() != 0:
+            raise ValueError("the damping profile is not zero inside the interior box; "
+                             "boundary-saving reconstruction needs an undamped interior")
+        r = self.order // 2
+        size = ctypes.c_int32(0)
+        g1 = self.grid(B)
+        N.call("sgb_ring_size", ctypes.byref(g1), iz0, iz1, ix0, ix1, r, ctypes.byref(size))
+        state.ring_store = torch.empty(nt, B, max(size.value, 1), dtype=torch.float32, device=dev)
+        K = int(ckpt_every) if ckpt_every else 0
+        nslots = nt // K if K > 0 else 0
+        state.ckpt_store = (torch.empty(max(nslots, 1), 2, *field, dtype=torch.float32, device=dev)
+                            if K > 0 else None)
+        state.bs = N.BsStore(iz0, iz1, ix0, ix1, r, size.value, N.ptr(state.ring_store), K,
+                             N.ptr(state.ckpt_store))
+        return state.bs
 
     def backward(self, state, acq, grad_records):
         """dJ/dvp (nz, nx) from dJ/d(records) through the fused adjoint."""
@@ -316,6 +320,105 @@ def acoustic_loop(vp, prop, damp, acq, illumination=False, ckpt_every=0):
 def default_ckpt_every(nt):
     """Checkpoint spacing of the reconstruction: about sqrt(nt), at most 256."""
     return int(min(256, max(16, round(math.sqrt(max(nt, 1))))))
+
+
+class BornPropagator(AcousticPropagator):
+    """Born modelling of the acoustic HABC equation for least-squares RTM
+    (acoustic_lsrtm_habc.py:11-30): a background field p driven by the
+    sources and a scattered field s driven by m k L(p), both under the HABC
+    blend; receivers sample s.  The gradient is dJ/dm (the velocity is held
+    fixed, as in the reference's LSRTM configurations)."""
+
+    def __init__(self, nz, nx, dt, h, order=2, bwidth=50, multiple=False, device=None):
+        super().__init__(nz, nx, dt, h, order, "habc", bwidth, multiple, device)
+
+    def forward_born(self, vp, refl, damp, acq, *, save_for_adjoint=False, ckpt_every=0):
+        require_cuda(vp, "BornPropagator.forward_born")
+        m, keep = self.model(vp, damp)
+        B = acq.nshots
+        dev = vp.device
+        field = (B, self.nz, self.pitch)
+        mp = to_pitched(refl.detach().to(device=dev, dtype=torch.float32), self.pitch).contiguous()
+        pbuf = [torch.empty(field, dtype=torch.float32, device=dev) for _ in range(3)]
+        sbuf = [torch.empty(field, dtype=torch.float32, device=dev) for _ in range(3)]
+        src = torch.empty(field, dtype=torch.float32, device=dev)
+        records = torch.empty(acq.nt, max(acq.nrec, 1), 1, dtype=torch.float32, device=dev)
+        state = AcousticState()
+        bs_struct = None
+        if save_for_adjoint:
+            bs_struct = self._boundary_store(state, keep, B, acq.nt, ckpt_every, field, dev)
+        cur = ctypes.c_int32(0)
+        prev = ctypes.c_int32(0)
+        g = self.grid(B)
+        q = acq.struct(records if acq.nrec else None, 1)
+        N.call("sgb_born_forward", ctypes.byref(g), ctypes.byref(m), N.ptr(mp), ctypes.byref(q),
+               N.PTR3(*[b.data_ptr() for b in pbuf]), N.PTR3(*[b.data_ptr() for b in sbuf]), N.ptr(src),
+               ctypes.byref(bs_struct) if bs_struct is not None else None, ctypes.byref(cur), ctypes.byref(prev),
+               N.stream_handle())
+        state.buf, state.cur, state.prev = pbuf, cur.value, prev.value
+        state.keep = keep
+        state.model = m
+        state.scattered = sbuf
+        return records[:, :acq.nrec], state
+
+    def step_born(self, vp, refl, damp, p, pm, sc, scm):
+        """One step of both fields (no sources or receivers): (p+, s+)."""
+        m, keep = self.model(vp, damp)
+        B = p.shape[0]
+        pit = lambda t: to_pitched(t.to(torch.float32), self.pitch).contiguous()
+        pp, ppm, ps, psm = pit(p), pit(pm), pit(sc), pit(scm)
+        mp = to_pitched(refl.detach().to(device=p.device, dtype=torch.float32), self.pitch).contiguous()
+        pn, sn, src = torch.empty_like(pp), torch.empty_like(pp), torch.empty_like(pp)
+        g = self.grid(B)
+        N.call("sgb_born_step", ctypes.byref(g), ctypes.byref(m), N.ptr(mp), N.ptr(pp), N.ptr(ppm), N.ptr(ps),
+               N.ptr(psm), N.ptr(pn), N.ptr(sn), N.ptr(src), N.stream_handle())
+        return pn[..., :self.nx], sn[..., :self.nx]
+
+    def backward_born(self, state, acq, grad_records):
+        """dJ/dm (nz, nx) from dJ/d(records) of the scattered field."""
+        B = acq.nshots
+        dev = state.buf[0].device
+        resid = torch.zeros(acq.nt, max(acq.nrec, 1), 1, dtype=torch.float32, device=dev)
+        if acq.nrec:
+            resid[:, :acq.nrec] = grad_records.to(torch.float32).reshape(acq.nt, acq.nrec, 1)
+        field = (B, self.nz, self.pitch)
+        lbuf = [torch.empty(field, dtype=torch.float32, device=dev) for _ in range(3)]
+        grad_shot = torch.empty(field, dtype=torch.float32, device=dev)
+        grad = torch.empty(self.nz, self.pitch, dtype=torch.float32, device=dev)
+        g = self.grid(B)
+        q = acq.struct(resid, 1)
+        N.call("sgb_born_backward", ctypes.byref(g), ctypes.byref(state.model), ctypes.byref(q),
+               ctypes.byref(state.bs), N.PTR3(*[b.data_ptr() for b in state.buf]), state.cur, state.prev,
+               N.PTR3(*[b.data_ptr() for b in lbuf]), N.ptr(grad_shot), N.ptr(grad), N.stream_handle())
+        return grad[:, :self.nx]
+
+
+class _BornLoop(torch.autograd.Function):
+    """Whole Born loop as one differentiable op: reflectivity m -> records."""
+
+    @staticmethod
+    def forward(ctx, refl, vp, prop, damp, acq, ckpt_every):
+        need = ctx.needs_input_grad[0]
+        rec, state = prop.forward_born(vp, refl, damp, acq, save_for_adjoint=need, ckpt_every=ckpt_every)
+        ctx.prop, ctx.acq, ctx.state = prop, acq, state
+        return rec
+
+    @staticmethod
+    def backward(ctx, grad_rec):
+        if ctx.state.bs is None:
+            return None, None, None, None, None, None
+        grad_m = ctx.prop.backward_born(ctx.state, ctx.acq, grad_rec.contiguous())
+        ctx.state = None
+        return grad_m, None, None, None, None, None
+
+
+def born_loop(vp, refl, prop, damp, acq, ckpt_every=0):
+    """Scattered-field records (nt, nrec, 1) of Born modelling; differentiable
+    in the reflectivity ``refl`` (the background velocity is not)."""
+    if vp.requires_grad:
+        raise NotImplementedError("Born modelling differentiates the reflectivity m only "
+                                  "(hold vp fixed, as the reference's LSRTM does)")
+    return _BornLoop.apply(refl, vp.detach(), prop, damp, acq, ckpt_every)
 
 
 class UnevenBatch:

@@ -8,16 +8,18 @@ class Parameters:
     def valid_model_paras():
         return {"acoustic": ["vp"],
                 "acoustic_habc": ["vp"],
+                "acoustic_lsrtm_habc": ["vp", "m"],
                 "elastic": ["vp", "vs", "rho"]}
 
     @staticmethod
     def secondorder_equations():
-        return ["acoustic", "acoustic_habc"]
+        return ["acoustic", "acoustic_habc", "acoustic_lsrtm_habc"]
 
 
 class Wavefield:
     _FIELDS = {"acoustic": ["h1", "h2"],
                "acoustic_habc": ["h1", "h2"],
+               "acoustic_lsrtm_habc": ["h1", "h2", "sh1", "sh2"],
                "elastic": ["vx", "vz", "txx", "tzz", "txz"]}
 
     def __init__(self, equation="acoustic"):
@@ -33,6 +35,10 @@ class Wavefield:
     @property
     def acoustic_habc(self):
         return list(self._FIELDS["acoustic_habc"])
+
+    @property
+    def acoustic_lsrtm_habc(self):
+        return list(self._FIELDS["acoustic_lsrtm_habc"])
 
     @property
     def elastic(self):

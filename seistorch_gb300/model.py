@@ -5,6 +5,7 @@ import importlib
 
 from .cell import WaveCell
 from .config import load_config
+from .eqconfigure import Parameters
 from .geom import WaveGeometryFreeForm
 from .rnn import WaveRNN
 from .utils import set_dtype, update_cfg
@@ -33,7 +34,7 @@ def build_model(config_path, device="cuda", mode="forward", source_encoding=Fals
     bwd = getattr(module, "_time_step_backward_multiple" if g.get("multiple") else "_time_step_backward", None)
     if bwd is None:
         raise ImportError(f"equation module {cfg['equation']} has no backward function")
-    fwd.ACOUSTIC2nd = cfg["equation"] in ("acoustic", "acoustic_habc")
+    fwd.ACOUSTIC2nd = cfg["equation"] in Parameters.secondorder_equations()
     cell = WaveCell(geom, fwd, bwd)
     model = WaveRNN(cell, source_encoding)
     return cfg, model

@@ -103,6 +103,16 @@ class WaveRNN(torch.nn.Module):
             rec, illum = engine.acoustic_loop(models[0].to(torch.float32), prop, d, acq,
                                               self.source_illumination, ck)
             self._fields = prop
+        elif eq == "acoustic_lsrtm_habc":
+            if list(geom.source_type) != ["h1"] or list(geom.receiver_type) != ["sh1"]:
+                raise NotImplementedError("Born modelling injects into h1 and records sh1")
+            if not geom.use_habc:
+                raise NotImplementedError("acoustic_lsrtm_habc runs with the HABC boundary")
+            prop = engine.BornPropagator(nz, nx, geom.dt, float(geom.h), geom.spatial_order, geom.bwidth,
+                                         geom.multiple, device)
+            ck = geom.ckpt_every or engine.default_ckpt_every(acq.nt)
+            rec = engine.born_loop(models[0].to(torch.float32), models[1].to(torch.float32), prop, d, acq, ck)
+            self._fields = prop
         elif eq == "elastic":
             from . import elastic_engine
             rec, illum, fields = elastic_engine.elastic_loop(models, geom, d, acq,

@@ -54,8 +54,11 @@ def run_case(ref, equation, models_int, *, order=2, width=20, multiple=False, ns
              grad=None, obs_models=None, source_type=None, receiver_type=None):
     torch.set_default_dtype(dtype)
     eqmod = {"acoustic": ref.acoustic, "acoustic_habc": ref.acoustic_habc,
-             "elastic": ref.elastic}[equation]
-    if equation != "elastic":
+             "acoustic_lsrtm_habc": ref.acoustic_lsrtm_habc, "elastic": ref.elastic}[equation]
+    if equation == "acoustic_lsrtm_habc":
+        # its Laplacian is acoustic_habc._laplacian, which reads acoustic_habc's kernel
+        RL.set_spatial_order(ref.acoustic_habc, order, dtype)
+    elif equation != "elastic":
         RL.set_spatial_order(eqmod, order, dtype)
     names = ref.eqconfigure.Parameters.valid_model_paras()[equation]
     top = 0 if multiple else width
@@ -157,6 +160,17 @@ def cases():
     C["grad_acoustic_habc_o2_multiple_zeroobs"] = dict(equation="acoustic_habc", models_int=ah, order=2,
                                                        width=50, habc=True, multiple=True, nt=200, grad=["vp"],
                                                        obs_models=None)
+    born = {"vp": ah["vp"], "m": layered(16, 24, [0.0, 0.08, -0.05], 3, anomaly=0.04)}
+    born_obs = {"vp": ah["vp"], "m": layered(16, 24, [0.0, 0.06, -0.02], 4, anomaly=0.0)}
+    for order in (2, 4):
+        C[f"born_habc_o{order}"] = dict(equation="acoustic_lsrtm_habc", models_int=born, order=order, width=50,
+                                        habc=True, nt=240, receiver_type=["sh1"])
+    C["born_habc_o2_multiple"] = dict(equation="acoustic_lsrtm_habc", models_int=born, order=2, width=50,
+                                      habc=True, multiple=True, nt=240, receiver_type=["sh1"])
+    C["grad_born_habc_o2_zeroobs"] = dict(equation="acoustic_lsrtm_habc", models_int=born, order=2, width=50,
+                                          habc=True, nt=200, grad=["m"], obs_models=None, receiver_type=["sh1"])
+    C["grad_born_habc_o4"] = dict(equation="acoustic_lsrtm_habc", models_int=born, order=4, width=50,
+                                  habc=True, nt=200, grad=["m"], obs_models=born_obs, receiver_type=["sh1"])
     C["grad_elastic_zeroobs"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,
                                      nt=200, grad=["vp", "vs", "rho"], obs_models=None)
     C["grad_elastic"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,

@@ -11,9 +11,10 @@ tensorboard, prettytable, ...).  Those are absent here, so this loader:
 * registers a bare ``seistorch`` package whose ``__path__`` is the reference
   package directory (so ``__init__`` never runs),
 * registers empty stub modules for the missing third-party names,
-* execs ``equations2d/acoustic.py`` and ``acoustic_habc.py`` from source with
-  their module-level ``device = "cuda"`` (acoustic.py:56,
-  acoustic_habc.py:57) replaced by ``"cpu"`` so the FD kernel can be built
+* execs ``equations2d/acoustic.py``, ``acoustic_habc.py`` and
+  ``acoustic_lsrtm_habc.py`` from source with their module-level
+  ``device = "cuda"`` (acoustic.py:56, acoustic_habc.py:57,
+  acoustic_lsrtm_habc.py:7) replaced by ``"cpu"`` so the FD kernel can be built
   without a GPU, and lets the caller patch ``spatial_order``/``kernel``
   (module globals read at call time, acoustic.py:55-58).
 """
@@ -113,6 +114,8 @@ def load(device="cpu"):
                                 os.path.join(PKG_DIR, "equations2d", "acoustic.py"), device)
     ns.acoustic_habc = _exec_patched("seistorch.equations2d.acoustic_habc",
                                      os.path.join(PKG_DIR, "equations2d", "acoustic_habc.py"), device)
+    ns.acoustic_lsrtm_habc = _exec_patched("seistorch.equations2d.acoustic_lsrtm_habc",
+                                           os.path.join(PKG_DIR, "equations2d", "acoustic_lsrtm_habc.py"), device)
     ns.elastic = importlib.import_module("seistorch.equations2d.elastic")
     ns.pml = importlib.import_module("seistorch.pml")
     ns.habc = importlib.import_module("seistorch.habc")

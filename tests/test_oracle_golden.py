@@ -28,6 +28,22 @@ def test_oracle_forward_matches_reference_fp64(name):
         assert rel_l2(out["fields"][n][0], g["field_" + n]) < 1e-10, n
 
 
+def test_oracle_born_records_are_the_scattered_field():
+    """The Born records (receivers on sh1) vanish with m = 0 and are linear
+    in m: the oracle at 2m gives twice the records."""
+    g = load("born_habc_o2")
+    args = (g["d"], g["dt"], g["h"], g["wavelet"], g["sources"], g["receivers"])
+    kw = dict(order=2, source_type=["h1"], receiver_type=["sh1"], nt=80)
+    zero = {"vp": g["models"]["vp"], "m": np.zeros_like(g["models"]["m"])}
+    r0 = np.stack(fd2d.forward("acoustic_lsrtm_habc", zero, *args, **kw)["records"])
+    assert np.abs(r0).max() == 0.0
+    r1 = np.stack(fd2d.forward("acoustic_lsrtm_habc", g["models"], *args, **kw)["records"])
+    twice = {"vp": g["models"]["vp"], "m": 2.0 * g["models"]["m"]}
+    r2 = np.stack(fd2d.forward("acoustic_lsrtm_habc", twice, *args, **kw)["records"])
+    assert np.abs(r1).max() > 0.0
+    assert rel_l2(r2, 2.0 * r1) < 1e-12
+
+
 @pytest.mark.parametrize("name", ["acoustic_pml_o4", "acoustic_habc_o2", "elastic"])
 def test_oracle_fp32_tracks_reference_fp32(name):
     """The oracle in float32 stays as close to the reference fp32 run as
