@@ -188,9 +188,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="acoustic_gradient",
-                    choices=["acoustic_gradient", "elastic_gradient", "uneven_forward", "learned_fwi", "learned_net"],
+                    choices=["acoustic_gradient", "elastic_gradient", "uneven_forward", "learned_fwi", "learned_net",
+                             "born_gradient"],
                     help="acoustic_gradient (default, the headline line); elastic_gradient: 300x800 + 50 PML "
-                         "elastic forward+adjoint; uneven_forward: 4 grid sizes x 64 shots in one launch per step")
+                         "elastic forward+adjoint; uneven_forward: 4 grid sizes x 64 shots in one launch per step; "
+                         "born_gradient: least-squares RTM gradient (Born modelling, HABC)")
     ap.add_argument("--pairs", type=int, default=2000, help="learned_fwi: training pairs")
     ap.add_argument("--epochs", type=int, default=12, help="learned_fwi: training epochs")
     ap.add_argument("--iters", type=int, default=20, help="learned_fwi: FWI iterations")
@@ -204,6 +206,8 @@ def main():
         return bench_elastic(args)
     if args.workload == "uneven_forward":
         return bench_uneven(args)
+    if args.workload == "born_gradient":
+        return bench_born(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -496,6 +500,120 @@ def bench_elastic(args):
             "roofline_forward": {"kernel": "elastic_fwd_kernel", "achieved": fwd_gbs, "frac": fwd_gbs / peak,
                                  "unit": "GB/s", "launch_ms": fwd_ms / nt},
             "gpu_launches": args.steps * (2 * nt + 2), "clocks": clocks.summary()}
+    print(json.dumps(line))
+    return 0
+
+
+# --------------------------------------------------------------- Born ---
+# Least-squares RTM gradient (acoustic_lsrtm_habc, examples/lsrtm/acoustic):
+# 400 x 1000 interior + 50-cell HABC (500 x 1100), dx = 10 m, dt = 1 ms,
+# 2000 steps, 2nd order (the equation module's spatial_order); smoothed
+# layered background vp 1500-3500 m/s held fixed; true reflectivity
+# m = 2 dv / v0 of the layered model, the gradient taken at half of it;
+# 32 shots on row 2, 10 Hz Ricker, receivers on every interior cell of row 2
+# recording the scattered field.  One step = Born forward (background +
+# scattered fields) + L2 residual + HABC adjoint + dJ/dm.
+BN_NZI, BN_NXI, BN_W, BN_DT, BN_H, BN_NT, BN_FM, BN_SHOTS = 400, 1000, 50, 0.001, 10.0, 2000, 10.0, 32
+BN_BYTES_FWD = 32  # background: read p, p-, write p+, m k L(p); scattered: read s, s-, m k L(p), write s+
+BN_BYTES_REV = 32  # read La1, La2, U_j, U_{j-1}, grad; write La_j, U_{j-2}, grad
+BN_BYTES_COEF = 16  # vp, blend weight, g / k, m planes, shared by the shots
+
+
+def born_models(seed=0):
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    nl = 7
+    tops = np.sort(rng.choice(np.arange(20, BN_NZI - 20), nl - 1, replace=False))
+    vel = np.linspace(1500.0, 3500.0, nl) + rng.uniform(-100, 100, nl)
+    zz, xx = np.mgrid[0:BN_NZI, 0:BN_NXI]
+    depth = zz + (8.0 * np.sin(2 * np.pi * xx / BN_NXI * rng.uniform(1, 3))).astype(int)
+    vp = vel[np.searchsorted(tops, depth, side="right")]
+    v0 = gaussian_filter(vp, sigma=12)
+    m_true = 2.0 * (vp - v0) / v0
+    pad = lambda a: np.pad(a, BN_W, mode="edge")
+    return pad(v0), pad(m_true)
+
+
+def bench_born(args):
+    import torch
+    from seistorch_gb300 import _native, engine
+    from seistorch_gb300.habc import generate_habc_coefficients_2d
+    from seistorch_gb300.postprocess import L2
+    from seistorch_gb300.utils import ricker_wave
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm is timed on the acoustic "
+                          "gradient workload only"}))
+        return 0
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _native.load(build_if_missing=False)
+    nt = args.nt if args.nt != NT else BN_NT
+    shots = args.shots if args.shots != NSHOTS else BN_SHOTS
+    v0, m_true = born_models()
+    nz, nx = v0.shape
+    b = generate_habc_coefficients_2d((nz, nx), BN_W).to(torch.float32)
+    wav = ricker_wave(BN_FM, BN_DT, nt, delay=int(1.2 / BN_FM / BN_DT), dtype="numpy")
+    xs = np.linspace(0, BN_NXI - 1, shots).round().astype(int)
+    src = [[(BN_W + 2, BN_W + int(x))] for x in xs]
+    rec = [([BN_W + 2] * BN_NXI, list(range(BN_W, BN_W + BN_NXI)))] * shots
+    prop = engine.BornPropagator(nz, nx, BN_DT, BN_H, 2, BN_W, False, dev)
+    acq = engine.Acquisition(nz, nx, src, rec, wav, dev)
+    t = lambda a, rg=False: torch.tensor(a, dtype=torch.float32, device=dev, requires_grad=rg)
+    vp, bb = t(v0), b.to(dev)
+    ck = engine.default_ckpt_every(nt)
+    with torch.no_grad():
+        obs = engine.born_loop(vp, t(m_true), prop, bb, acq).contiguous()
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def step(timing=None):
+        m = t(0.5 * m_true, True)
+        e0, e1, e2 = ev(), ev(), ev()
+        e0.record(stream)
+        r = engine.born_loop(vp, m, prop, bb, acq, ck)
+        e1.record(stream)
+        loss = L2()(r, obs)
+        loss.backward()
+        e2.record(stream)
+        if timing is not None:
+            timing.append((e0, e1, e2))
+        return loss
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    timing = []
+    with ClockSampler(0) as clocks:
+        t0, t1 = ev(), ev()
+        t0.record(stream)
+        for _ in range(args.steps):
+            step(timing)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    fwd_ms = float(np.median([a.elapsed_time(c) for a, c, _ in timing]))
+    rev_ms = float(np.median([c.elapsed_time(e) for _, c, e in timing]))
+    npts = nz * nx
+    rev_bytes = shots * npts * BN_BYTES_REV + npts * BN_BYTES_COEF
+    fwd_bytes = shots * npts * BN_BYTES_FWD + npts * BN_BYTES_COEF
+    peak, kind = measured_peaks()
+    rev_gbs = rev_bytes / (rev_ms / (nt - 1) * 1e-3) / 1e9
+    fwd_gbs = fwd_bytes / (fwd_ms / nt * 1e-3) / 1e9
+    line = {"metric": "Gpts/s fwd+adjoint", "value": shots * npts * nt / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"born_lsrtm_gradient_{BN_NZI}x{BN_NXI}_habc{BN_W}_o2_nt{nt}_{shots}shots",
+                       "grid": [nz, nx], "shots": shots, "nt": nt, "ckpt_every": ck,
+                       "l2": "inputs larger than L2 (70 MB per field, 6 fields)"},
+            "shots_per_s": shots / (ms * 1e-3), "phases_ms": {"forward": fwd_ms, "adjoint": rev_ms},
+            "roofline": {"kernel": "habc_bwd_kernel", "bound": "hbm", "achieved": rev_gbs, "peak": peak,
+                         "peak_kind": kind, "unit": "GB/s", "frac": rev_gbs / peak, "traffic": None,
+                         "bytes_per_launch": rev_bytes, "launch_ms": rev_ms / (nt - 1)},
+            "roofline_forward": {"kernel": "acoustic_fwd_kernel<HABC> x2 (background, scattered)",
+                                 "achieved": fwd_gbs, "frac": fwd_gbs / peak, "unit": "GB/s",
+                                 "launch_ms": fwd_ms / nt},
+            # per step: 2 NT forward + NT ring gathers, NT-1 reverse, coefficients, misfit, reduction
+            "gpu_launches": args.steps * (3 * nt + (nt - 1) + 3), "clocks": clocks.summary()}
     print(json.dumps(line))
     return 0
 

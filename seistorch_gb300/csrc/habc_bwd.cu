@@ -162,7 +162,8 @@ __device__ __forceinline__ float oneway_t(const HabcBwdArgs& a, const float* l1,
   return acc;
 }
 
-__global__ void __launch_bounds__(256) habc_bwd_kernel(const HabcBwdArgs a) {
+template <int R>
+__global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
   const long long plane = (long long)a.nz * a.nx;
   const long long total = plane * a.nshots;
   const bool mult = a.multiple != 0;
@@ -176,23 +177,41 @@ __global__ void __launch_bounds__(256) habc_bwd_kernel(const HabcBwdArgs a) {
     const float* l1 = a.la1 + fb;
     const float* l2 = a.la2 + fb;
     const float kq = __ldg(a.k + o);
-    // interior part: 2 wi La1 + L(k wi La1) - wi La2
-    auto kwl = [&](int zz, int xx) -> float {
-      if (zz < 0 || zz >= a.nz || xx < 0 || xx >= a.nx) return 0.f;
-      const long long oo = (long long)zz * a.pitch + xx;
-      const HabcW w = habc_weights(zz, xx, a.nz, a.nx, a.hw, mult, __ldg(a.hb + oo));
-      return __ldg(a.k + oo) * w.wi * l1[oo];
-    };
-    const HabcW wq = habc_weights(z, x, a.nz, a.nx, a.hw, mult, __ldg(a.hb + o));
-    float lap = a.w.c[0] * kq * wq.wi * l1[o];
-    for (int j = 1; j <= a.R; ++j)
-      lap += a.w.c[j] * (kwl(z - j, x) + kwl(z + j, x) + kwl(z, x - j) + kwl(z, x + j));
-    float v = 2.f * wq.wi * l1[o] + lap - wq.wi * l2[o];
-    // one-way parts of the four sides
-    v += oneway_t(a, l1, l2, z, x, z, 1, 0, 0);
-    v += oneway_t(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
-    v += oneway_t(a, l1, l2, z, x, x, 0, 1, 2);
-    v += oneway_t(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
+    // Cells at least hw + R from every strip side: every stencil neighbour
+    // lies in the grid with wi = 1 and no one-way line reaches them, so the
+    // transpose is the plain 2 La1 + L(k La1) - La2.  With `multiple` the
+    // top has no strip, but the stencil must still stay below row 0.
+    const int far = a.hw + R;
+    const bool interior =
+        z >= (mult ? R : far) && a.nz - 1 - z >= far && x >= far && a.nx - 1 - x >= far;
+    float v;
+    if (interior) {
+      float lap = a.w.c[0] * kq * l1[o];
+      for (int j = 1; j <= R; ++j) {
+        const long long up = o - (long long)j * a.pitch, dn = o + (long long)j * a.pitch;
+        lap += a.w.c[j] * (__ldg(a.k + up) * l1[up] + __ldg(a.k + dn) * l1[dn] + __ldg(a.k + o - j) * l1[o - j] +
+                           __ldg(a.k + o + j) * l1[o + j]);
+      }
+      v = 2.f * l1[o] + lap - l2[o];
+    } else {
+      // interior part: 2 wi La1 + L(k wi La1) - wi La2
+      auto kwl = [&](int zz, int xx) -> float {
+        if (zz < 0 || zz >= a.nz || xx < 0 || xx >= a.nx) return 0.f;
+        const long long oo = (long long)zz * a.pitch + xx;
+        const HabcW w = habc_weights(zz, xx, a.nz, a.nx, a.hw, mult, __ldg(a.hb + oo));
+        return __ldg(a.k + oo) * w.wi * l1[oo];
+      };
+      const HabcW wq = habc_weights(z, x, a.nz, a.nx, a.hw, mult, __ldg(a.hb + o));
+      float lap = a.w.c[0] * kq * wq.wi * l1[o];
+      for (int j = 1; j <= R; ++j)
+        lap += a.w.c[j] * (kwl(z - j, x) + kwl(z + j, x) + kwl(z, x - j) + kwl(z, x + j));
+      v = 2.f * wq.wi * l1[o] + lap - wq.wi * l2[o];
+      // one-way parts of the four sides
+      v += oneway_t(a, l1, l2, z, x, z, 1, 0, 0);
+      v += oneway_t(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
+      v += oneway_t(a, l1, l2, z, x, x, 0, 1, 2);
+      v += oneway_t(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
+    }
     // residuals of the records of step j-1 (they sample U_j)
     if (a.resid != nullptr) {
       const int* rp = a.rec_row_ptr + (long long)b * a.nz;
@@ -206,28 +225,24 @@ __global__ void __launch_bounds__(256) habc_bwd_kernel(const HabcBwdArgs a) {
     a.lout[fb + o] = v;
     // gradient and reconstruction inside the undamped box
     const bool inbox = a.ring.inside(z, x);
-    if (inbox || a.uout != nullptr) {
+    if (inbox) {
       const float* u1 = a.ujm1 + fb;
       float L = a.w.c[0] * u1[o];
-      for (int j = 1; j <= a.R; ++j)
+      for (int j = 1; j <= R; ++j)
         L += a.w.c[j] * (ldz(u1, z - j, x, a.nz, a.nx, a.pitch) + ldz(u1, z + j, x, a.nz, a.nx, a.pitch) +
                          ldz(u1, z, x - j, a.nz, a.nx, a.pitch) + ldz(u1, z, x + j, a.nz, a.nx, a.pitch));
-      if (inbox) a.grad[fb + o] += v * kq * L;  // times 2 / vp in the shot reduction
+      a.grad[fb + o] += v * kq * L;  // times 2 / vp in the shot reduction (dJ/dvp)
       if (a.uout != nullptr) {
-        float u = 0.f;
-        if (inbox) {
-          float ujv = a.uj[fb + o];
-          if (a.src_ptr != nullptr) {
-            for (int q = a.src_ptr[b]; q < a.src_ptr[b + 1]; ++q)
-              if (a.src_z[q] == z && a.src_x[q] == x) ujv -= a.wavelet[(long long)a.src_wrow[q] * a.nt + a.t_src];
-          }
-          u = 2.f * u1[o] - ujv + kq * L;
-        } else {
-          const int ri = a.ring.index(z, x);
-          if (ri >= 0 && a.ring_in != nullptr) u = a.ring_in[(long long)b * a.ring.size + ri];
+        float ujv = a.uj[fb + o];
+        if (a.src_ptr != nullptr) {
+          for (int q = a.src_ptr[b]; q < a.src_ptr[b + 1]; ++q)
+            if (a.src_z[q] == z && a.src_x[q] == x) ujv -= a.wavelet[(long long)a.src_wrow[q] * a.nt + a.t_src];
         }
-        a.uout[fb + o] = u;
+        a.uout[fb + o] = 2.f * u1[o] - ujv + kq * L;
       }
+    } else if (a.uout != nullptr) {  // the saved ring around the box, 0 beyond it
+      const int ri = a.ring.index(z, x);
+      a.uout[fb + o] = (ri >= 0 && a.ring_in != nullptr) ? a.ring_in[(long long)b * a.ring.size + ri] : 0.f;
     }
   }
 }
@@ -277,7 +292,13 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
   const long long total = (long long)g.nz * g.nx * g.nshots;
   long long blocks = (total + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  habc_bwd_kernel<<<(unsigned)blocks, 256, 0, s>>>(a);
+  switch (a.R) {
+    case 1: habc_bwd_kernel<1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 2: habc_bwd_kernel<2><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 3: habc_bwd_kernel<3><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 4: habc_bwd_kernel<4><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
