@@ -125,9 +125,7 @@ __global__ void __launch_bounds__(NTHREADS) acoustic_fwd_kernel(const AcStepArgs
   extern __shared__ __align__(16) float smem[];
   float* s_u = smem;                           // (TZ + 2HR) x SROW
   float* s_um = s_u + (TZ + 2 * HR) * SROW;     // TZ x TX
-  float* s_g = s_um + TZ * TX;
-  float* s_k = s_g + TZ * TX;
-  int* s_src = reinterpret_cast<int*>(s_k + TZ * TX);  // [2 * MAX_TILE_SRC] + count
+  int* s_src = reinterpret_cast<int*>(s_um + TZ * TX);  // [2 * MAX_TILE_SRC] + count
   float* s_srcv = reinterpret_cast<float*>(s_src + 2 * MAX_TILE_SRC + 1);
 
   const int tid = threadIdx.x;
@@ -152,8 +150,6 @@ __global__ void __launch_bounds__(NTHREADS) acoustic_fwd_kernel(const AcStepArgs
     const int nb = chunk_bytes(z, x, a.nz, a.nx);
     const long long off = (long long)z * a.pitch + x;
     cp_async16(s_um + r * TX + 4 * cc, nb ? a.um + base + off : a.um, nb);
-    cp_async16(s_g + r * TX + 4 * cc, nb ? a.g + off : a.g, nb);
-    cp_async16(s_k + r * TX + 4 * cc, nb ? a.k + off : a.k, nb);
   }
   cp_async_commit();
   // sources of this shot that fall in the tile
@@ -198,8 +194,12 @@ __global__ void __launch_bounds__(NTHREADS) acoustic_fwd_kernel(const AcStepArgs
     const float4 right = lds4(s_u + sr * SROW + 2 * HX + xl);
     const float4 L = lap4<R>(win, left, right, a.w);
     const float4 vm = lds4(s_um + lr * TX + xl);
-    const float4 vg = lds4(s_g + lr * TX + xl);
-    const float4 vk = lds4(s_k + lr * TX + xl);
+    // coefficient rows straight from L2 (shared by every shot's tile; each
+    // cell reads only its own value, so they need no staging)
+    const bool cin = z < a.nz && x < a.nx;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 vg = cin ? __ldg(reinterpret_cast<const float4*>(a.g + (long long)z * a.pitch + x)) : zero4;
+    const float4 vk = cin ? __ldg(reinterpret_cast<const float4*>(a.k + (long long)z * a.pitch + x)) : zero4;
     float4 y;
     y.x = fmaf(vk.x, L.x, fmaf(vg.x, win[R].x - vm.x, vm.x));
     y.y = fmaf(vk.y, L.y, fmaf(vg.y, win[R].y - vm.y, vm.y));
@@ -405,7 +405,7 @@ __global__ void ring_copy_kernel(int nshots, Ring ring, int pitch, long long sst
 template <int R, int TZ, bool HABC>
 static size_t fwd_smem() {
   constexpr int HR = (HABC && R < 2) ? 2 : R;
-  return sizeof(float) * ((TZ + 2 * HR) * SROW + 3 * TZ * TX) + sizeof(int) * (3 * MAX_TILE_SRC + 1);
+  return sizeof(float) * ((TZ + 2 * HR) * SROW + TZ * TX) + sizeof(int) * (3 * MAX_TILE_SRC + 1);
 }
 template <int R, int TZ>
 static size_t vjp_smem() {
