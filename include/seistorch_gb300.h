@@ -189,6 +189,35 @@ int sgb_acoustic_backward_noalloc(const sgb_grid *grid, const sgb_acoustic_model
                                   float *const ubuf[3], int32_t ucur, int32_t uprev, float *grad_vp,
                                   sgb_stream_t stream);
 
+/* ---------------------------------------------------------------- VTI --- */
+
+/* The loop of vti_habc2._time_step (seistorch/equations2d/vti_habc2.py:26-56),
+ * second order, HABC: U+ = HABC(2U - U- + kx Lx(U) + kz Lz(U)) + sources,
+ * Lx / Lz the 1-D second differences along x / z (convkernel.py kernelx /
+ * kernely).  model->coef holds THREE planes [g][kx][kz] (g = 2 everywhere,
+ * kx = vp^2 dt^2 (1 + 2 eps + sk) / h^2, kz = vp^2 dt^2 (1 + sk) / h^2 with
+ * the reference's per-cell sk of eps, delta and the cell's FFT frequencies;
+ * the caller computes them); model->order must be 2 and model->boundary 1.
+ * Other arguments as sgb_acoustic_forward (no illumination). */
+int sgb_vti_forward(const sgb_grid *grid, const sgb_acoustic_model *model, const sgb_acquisition *acq,
+                    float *const buf[3], const sgb_bs_store *bs, int32_t *cur_out, int32_t *prev_out,
+                    sgb_stream_t stream);
+
+/* Adjoint of sgb_vti_forward: the exact HABC adjoint with the anisotropic
+ * interior update; returns dJ/dkx = sum_t La Lx(U) and dJ/dkz = sum_t La Lz(U)
+ * inside the undamped box (0 outside), from which the caller forms the
+ * vp / eps / delta gradients through its coefficient map.  grad_shot_x /
+ * grad_shot_z: scratch [nshots][nz][pitch] each; the rest as
+ * sgb_acoustic_backward. */
+int sgb_vti_backward(const sgb_grid *grid, const sgb_acoustic_model *model, const sgb_acquisition *acq,
+                     const sgb_bs_store *bs, float *const ubuf[3], int32_t ucur, int32_t uprev,
+                     float *const lbuf[3], float *grad_shot_x, float *grad_shot_z, float *grad_x,
+                     float *grad_z, sgb_stream_t stream);
+
+/* One step (no sources or receivers): the per-step equation-module drop-in. */
+int sgb_vti_step(const sgb_grid *grid, const sgb_acoustic_model *model, const float *u, const float *um,
+                 float *unext, sgb_stream_t stream);
+
 /* --------------------------------------------------- Born modelling --- */
 
 /* Born (linearised) modelling of the acoustic HABC equation for

@@ -268,6 +268,46 @@ def born_habc_step(vp, m, h1, h2, sh1, sh2, dt, h, b, order, multiple=False, dty
     return p0, np.asarray(h1, dtype), s0, np.asarray(sh1, dtype)
 
 
+def second_difference(u, axis, h, dtype=np.float64):
+    """Zero-padded 1-D second difference / h^2 along `axis` of (B, Nz, Nx)
+    fields (convkernel.py kernelx / kernely at spatial order 2: [1, -2, 1])."""
+    u = np.asarray(u, dtype)
+    up = np.pad(u, [(0, 0)] + [(1, 1) if ax == axis % 3 else (0, 0) for ax in (1, 2)])
+    n = u.shape[axis]
+    lo = np.take(up, np.arange(0, n), axis=axis)
+    hi = np.take(up, np.arange(2, n + 2), axis=axis)
+    return (lo + hi - 2 * u) * dtype(1.0 / (h * h))
+
+
+def vti_sk(eps, delta, h, dtype=np.float64):
+    """The reference's per-cell sk (vti_habc2.py:36-45): fftfreq of the rows
+    (named kx there) and columns (kz), meshgrid 'ij'."""
+    eps = np.asarray(eps, dtype)
+    delta = np.asarray(delta, dtype)
+    nz, nx = eps.shape
+    fx = np.fft.fftfreq(nz, d=h).astype(dtype)
+    fz = np.fft.fftfreq(nx, d=h).astype(dtype)
+    kx, kz = np.meshgrid(fx, fz, indexing="ij")
+    num = -2 * (eps - delta) * kx ** 2 * kz ** 2
+    den = (1 + 2 * eps) * kx ** 4 + kz ** 4 + 2 * (1 + delta) * kx ** 2 * kz ** 2
+    return num * (den + dtype(1e-26)) ** -1
+
+
+def vti_habc_step(vp, eps, delta, p1, p2, dt, h, b, multiple=False, dtype=np.float64):
+    """VTI step (vti_habc2.py:26-56): 2 p1 - p2 + vp^2 dt^2 ((1 + 2 eps) + sk)
+    d2x(p1) + vp^2 dt^2 (1 + sk) d2z(p1), then the HABC blend (with vp).
+    Returns (pnext, p1)."""
+    vp = np.asarray(vp, dtype)
+    eps = np.asarray(eps, dtype)
+    sk = vti_sk(eps, delta, h, dtype)
+    v2 = vp ** 2 * dtype(dt) ** 2
+    p1 = np.asarray(p1, dtype)
+    y = (2 * p1 - np.asarray(p2, dtype) + v2 * ((1 + 2 * eps) + sk) * second_difference(p1, 2, h, dtype)
+         + v2 * (1 + sk) * second_difference(p1, 1, h, dtype))
+    y = habc_apply(y, p1, p2, vp, b, dt, h, 50, multiple, dtype)
+    return y, p1
+
+
 def dfwd(a, axis):
     """a[i] - a[i-1], zero at index 0 (equations2d/utils.py:3-25, forward)."""
     out = a - np.roll(a, 1, axis=axis)
@@ -315,10 +355,10 @@ def elastic_step(vp, vs, rho, vx, vz, txx, tzz, txz, dt, h, d, dtype=np.float64)
 # ----------------------------------------------------------- time loop ---
 
 WAVEFIELDS = {"acoustic": ["h1", "h2"], "acoustic_habc": ["h1", "h2"],
-              "acoustic_lsrtm_habc": ["h1", "h2", "sh1", "sh2"],
+              "acoustic_lsrtm_habc": ["h1", "h2", "sh1", "sh2"], "vti_habc2": ["p1", "p2"],
               "elastic": ["vx", "vz", "txx", "tzz", "txz"]}
 MODEL_PARAMS = {"acoustic": ["vp"], "acoustic_habc": ["vp"], "acoustic_lsrtm_habc": ["vp", "m"],
-                "elastic": ["vp", "vs", "rho"]}
+                "vti_habc2": ["vp", "epsilon", "delta"], "elastic": ["vp", "vs", "rho"]}
 
 
 def forward(equation, models, d, dt, h, wavelet, sources, receivers, *,
@@ -339,8 +379,9 @@ def forward(equation, models, d, dt, h, wavelet, sources, receivers, *,
     wavelet = np.asarray(wavelet, np.float64)
     nt = len(wavelet) if nt is None else nt
     names = WAVEFIELDS[equation]
-    source_type = source_type or (["h1"] if equation != "elastic" else ["txx", "tzz"])
-    receiver_type = receiver_type or (["h1"] if equation != "elastic" else ["vx", "vz"])
+    first = WAVEFIELDS[equation][0]
+    source_type = source_type or ([first] if equation != "elastic" else ["txx", "tzz"])
+    receiver_type = receiver_type or ([first] if equation != "elastic" else ["vx", "vz"])
     B = len(sources)
     m0 = np.asarray(models[MODEL_PARAMS[equation][0]])
     nz, nx = m0.shape
@@ -363,6 +404,10 @@ def forward(equation, models, d, dt, h, wavelet, sources, receivers, *,
             out = born_habc_step(models["vp"], models["m"], fields["h1"], fields["h2"], fields["sh1"],
                                  fields["sh2"], dt, h, d, order, multiple, dtype)
             fields = dict(zip(names, out))
+        elif equation == "vti_habc2":
+            y, p1 = vti_habc_step(models["vp"], models["epsilon"], models["delta"], fields["p1"], fields["p2"],
+                                  dt, h, d, multiple, dtype)
+            fields["p1"], fields["p2"] = y, p1
         elif equation == "elastic":
             out = elastic_step(models["vp"], models["vs"], models["rho"],
                                *[fields[n] for n in names], dt, h, d, dtype)

@@ -150,6 +150,14 @@ SIGNATURES = {
     "sgb_acoustic_backward_noalloc": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel),
                                                      ctypes.POINTER(Acquisition), ctypes.POINTER(BsStore), PTR3,
                                                      c_i32, c_i32, c_ptr, c_ptr]),
+    "sgb_vti_forward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel),
+                                       ctypes.POINTER(Acquisition), PTR3, ctypes.POINTER(BsStore),
+                                       ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_ptr]),
+    "sgb_vti_backward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel),
+                                        ctypes.POINTER(Acquisition), ctypes.POINTER(BsStore), PTR3, c_i32, c_i32,
+                                        PTR3, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr]),
+    "sgb_vti_step": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel), c_ptr, c_ptr, c_ptr,
+                                    c_ptr]),
     "sgb_born_forward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel), c_ptr,
                                         ctypes.POINTER(Acquisition), PTR3, PTR3, c_ptr, ctypes.POINTER(BsStore),
                                         ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_ptr]),

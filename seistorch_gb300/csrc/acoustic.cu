@@ -118,6 +118,26 @@ __device__ __forceinline__ float4 lap4(const float4 (&win)[2 * R + 1], const flo
   return L;
 }
 
+// The x and z parts of lap4 (1-D second differences, centre -2 sum c).
+template <int R>
+__device__ __forceinline__ void lap4_xz(const float4 (&win)[2 * R + 1], const float4& left, const float4& right,
+                                        const FdWeights& w, float4& Lx, float4& Lz) {
+  const float a[12] = {left.x, left.y, left.z, left.w, win[R].x, win[R].y, win[R].z, win[R].w,
+                       right.x, right.y, right.z, right.w};
+  const float c0 = 0.5f * w.c[0];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    float sx = c0 * a[4 + m], sz = c0 * a[4 + m];
+#pragma unroll
+    for (int j = 1; j <= R; ++j) {
+      sx = fmaf(w.c[j], a[4 + m + j] + a[4 + m - j], sx);
+      sz = fmaf(w.c[j], comp(win[R + j], m) + comp(win[R - j], m), sz);
+    }
+    set_comp(Lx, m, sx);
+    set_comp(Lz, m, sz);
+  }
+}
+
 template <int R, int TZ, bool HABC>
 __global__ void __launch_bounds__(NTHREADS) acoustic_fwd_kernel(const AcStepArgs a) {
   constexpr int HR = (HABC && R < 2) ? 2 : R;
@@ -201,10 +221,20 @@ __global__ void __launch_bounds__(NTHREADS) acoustic_fwd_kernel(const AcStepArgs
     const float4 vg = cin ? __ldg(reinterpret_cast<const float4*>(a.g + (long long)z * a.pitch + x)) : zero4;
     const float4 vk = cin ? __ldg(reinterpret_cast<const float4*>(a.k + (long long)z * a.pitch + x)) : zero4;
     float4 y;
-    y.x = fmaf(vk.x, L.x, fmaf(vg.x, win[R].x - vm.x, vm.x));
-    y.y = fmaf(vk.y, L.y, fmaf(vg.y, win[R].y - vm.y, vm.y));
-    y.z = fmaf(vk.z, L.z, fmaf(vg.z, win[R].z - vm.z, vm.z));
-    y.w = fmaf(vk.w, L.w, fmaf(vg.w, win[R].w - vm.w, vm.w));
+    if (HABC && a.kz != nullptr) {  // VTI: k Lx + kz Lz
+      float4 Lx, Lz;
+      lap4_xz<R>(win, left, right, a.w, Lx, Lz);
+      const float4 vz = cin ? __ldg(reinterpret_cast<const float4*>(a.kz + (long long)z * a.pitch + x)) : zero4;
+      y.x = fmaf(vk.x, Lx.x, fmaf(vz.x, Lz.x, fmaf(vg.x, win[R].x - vm.x, vm.x)));
+      y.y = fmaf(vk.y, Lx.y, fmaf(vz.y, Lz.y, fmaf(vg.y, win[R].y - vm.y, vm.y)));
+      y.z = fmaf(vk.z, Lx.z, fmaf(vz.z, Lz.z, fmaf(vg.z, win[R].z - vm.z, vm.z)));
+      y.w = fmaf(vk.w, Lx.w, fmaf(vz.w, Lz.w, fmaf(vg.w, win[R].w - vm.w, vm.w)));
+    } else {
+      y.x = fmaf(vk.x, L.x, fmaf(vg.x, win[R].x - vm.x, vm.x));
+      y.y = fmaf(vk.y, L.y, fmaf(vg.y, win[R].y - vm.y, vm.y));
+      y.z = fmaf(vk.z, L.z, fmaf(vg.z, win[R].z - vm.z, vm.z));
+      y.w = fmaf(vk.w, L.w, fmaf(vg.w, win[R].w - vm.w, vm.w));
+    }
     if (z < a.nz && x < a.nx) {
       const long long po = (long long)z * a.pitch + x;
       if (a.born_out != nullptr) {  // m k L(u): the scattered field's source

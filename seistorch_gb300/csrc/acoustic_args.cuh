@@ -43,6 +43,9 @@ struct AcStepArgs {
   const float* __restrict__ born_m;  // [nz][pitch]
   float* __restrict__ born_out;      // [nshots][nz][pitch]
   const float* __restrict__ born_in;  // [nshots][nz][pitch]
+  // VTI (vti_habc2.py:26-56): with kz set, the update is
+  // 2u - u- + k Lx(u) + kz Lz(u) (k, kz: the x and z coefficient planes)
+  const float* __restrict__ kz;
   int* status;
 };
 

@@ -60,7 +60,8 @@ cudaError_t launch_ring_copy(const sgb_grid& gr, const Ring& ring, float* field,
                              cudaStream_t s);
 int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                            const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur, int32_t uprev,
-                           float* const lbuf[3], float* grad_shot, float* grad_vp, bool born, cudaStream_t s);
+                           float* const lbuf[3], float* grad_shot, float* grad_vp, bool born, cudaStream_t s,
+                           const float* kz = nullptr, float* grad_shot2 = nullptr, float* grad_out2 = nullptr);
 cudaError_t launch_acoustic_grad_reduce(const sgb_grid& gr, const float* grad_shot, const float* vp,
                                         const Ring& ring, float* grad_vp, cudaStream_t s);
 int pick_tz(int nz, int nx, int nshots, int tz_max);
@@ -80,7 +81,7 @@ int set_stream_config(int fwd, int bwd, int zc);
 cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
                             const Ring& ring, const float* la1, const float* la2, float* lout, const float* uj,
                             const float* ujm1, float* uout, float* grad, const float* ring_in, int t_src,
-                            const float* resid, cudaStream_t s);
+                            const float* resid, const float* kz, float* grad2, cudaStream_t s);
 
 }  // namespace sgb
 
@@ -129,6 +130,10 @@ AcStepArgs base_step_args(const sgb_grid* g, const sgb_acoustic_model* m) {
   return a;
 }
 
+
+int acoustic_forward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
+                          float* const buf[3], float* illum, const sgb_bs_store* bs, int32_t* cur_out,
+                          int32_t* prev_out, const float* kz, cudaStream_t s);
 
 }  // namespace
 
@@ -227,6 +232,26 @@ int sgb_acoustic_step_vjp(const sgb_grid* grid, const sgb_acoustic_model* model,
 int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                          float* const buf[3], float* illum, const sgb_bs_store* bs, int32_t* cur_out,
                          int32_t* prev_out, sgb_stream_t stream) {
+  return acoustic_forward_impl(grid, model, acq, buf, illum, bs, cur_out, prev_out, nullptr, (cudaStream_t)stream);
+}
+
+int sgb_vti_forward(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
+                    float* const buf[3], const sgb_bs_store* bs, int32_t* cur_out, int32_t* prev_out,
+                    sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (model == nullptr || model->coef == nullptr) return SGB_ERR_ARG;
+  if (model->boundary != 1 || model->order != 2) return SGB_ERR_UNSUPPORTED;  // vti_habc2: 2nd order, HABC
+  return acoustic_forward_impl(grid, model, acq, buf, nullptr, bs, cur_out, prev_out,
+                               model->coef + 2LL * grid->nz * grid->pitch, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+namespace {
+
+int acoustic_forward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
+                          float* const buf[3], float* illum, const sgb_bs_store* bs, int32_t* cur_out,
+                          int32_t* prev_out, const float* kz, cudaStream_t s) {
   if (int e = check_grid(grid)) return e;
   if (int e = check_model(grid, model)) return e;
   if (int e = check_acq(grid, acq)) return e;
@@ -236,8 +261,8 @@ int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, 
     if (!aligned16(buf[i])) return SGB_ERR_ALIGN;
   }
   if (acq->records != nullptr && acq->nch != 1) return SGB_ERR_UNSUPPORTED;
-  cudaStream_t s = (cudaStream_t)stream;
   AcStepArgs a = base_step_args(grid, model);
+  a.kz = kz;
   a.src_ptr = acq->nsrc > 0 ? acq->src_ptr : nullptr;
   a.src_z = acq->src_z;
   a.src_x = acq->src_x;
@@ -335,6 +360,10 @@ int sgb_acoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, 
   *prev_out = prev;
   return SGB_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int sgb_born_forward(const sgb_grid* grid, const sgb_acoustic_model* model, const float* m,
                      const sgb_acquisition* acq, float* const pbuf[3], float* const sbuf[3], float* born_src,
@@ -454,6 +483,38 @@ int sgb_born_step(const sgb_grid* grid, const sgb_acoustic_model* model, const f
   return SGB_OK;
 }
 
+int sgb_vti_backward(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
+                     const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur, int32_t uprev, float* const lbuf[3],
+                     float* grad_shot_x, float* grad_shot_z, float* grad_x, float* grad_z, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (model == nullptr || model->coef == nullptr) return SGB_ERR_ARG;
+  if (model->boundary != 1 || model->order != 2) return SGB_ERR_UNSUPPORTED;
+  if (grad_shot_z == nullptr || grad_z == nullptr) return SGB_ERR_ARG;
+  if (!aligned16(grad_shot_z)) return SGB_ERR_ALIGN;
+  return sgb::acoustic_backward_impl(grid, model, acq, bs, ubuf, ucur, uprev, lbuf, grad_shot_x, grad_x, false,
+                                     (cudaStream_t)stream, model->coef + 2LL * grid->nz * grid->pitch, grad_shot_z,
+                                     grad_z);
+}
+
+int sgb_vti_step(const sgb_grid* grid, const sgb_acoustic_model* model, const float* u, const float* um,
+                 float* unext, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (int e = check_model(grid, model)) return e;
+  if (model->boundary != 1 || model->order != 2) return SGB_ERR_UNSUPPORTED;
+  if (model->vp == nullptr || model->damp == nullptr) return SGB_ERR_ARG;
+  if (u == nullptr || um == nullptr || unext == nullptr) return SGB_ERR_ARG;
+  if (!aligned16(u) || !aligned16(um) || !aligned16(unext)) return SGB_ERR_ALIGN;
+  if (unext == u || unext == um) return SGB_ERR_ARG;
+  AcStepArgs a = base_step_args(grid, model);
+  a.u = u;
+  a.um = um;
+  a.un = unext;
+  a.kz = model->coef + 2LL * grid->nz * grid->pitch;
+  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 32);
+  SGB_CUDA_CHECK(launch_acoustic_fwd(1, true, tz, a, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
 int sgb_born_backward(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                       const sgb_bs_store* bs, float* const pbuf[3], int32_t pcur, int32_t pprev, float* const lbuf[3],
                       float* grad_shot, float* grad_m, sgb_stream_t stream) {
@@ -478,7 +539,8 @@ namespace sgb {
 // modelling) instead of (2/vp) times it (dJ/dvp).
 int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                            const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur, int32_t uprev,
-                           float* const lbuf[3], float* grad_shot, float* grad_vp, bool born, cudaStream_t s) {
+                           float* const lbuf[3], float* grad_shot, float* grad_vp, bool born, cudaStream_t s,
+                           const float* kz, float* grad_shot2, float* grad_out2) {
   if (int e = check_grid(grid)) return e;
   if (int e = check_model(grid, model)) return e;
   if (int e = check_acq(grid, acq)) return e;
@@ -494,14 +556,17 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
   }
   if (!aligned16(grad_shot)) return SGB_ERR_ALIGN;
   if (acq->records != nullptr && acq->nch != 1) return SGB_ERR_UNSUPPORTED;
-  if (born && model->boundary != 1) return SGB_ERR_UNSUPPORTED;
-  const float* gscale = born ? nullptr : model->vp;
+  if ((born || kz != nullptr) && model->boundary != 1) return SGB_ERR_UNSUPPORTED;
+  if (kz != nullptr && (grad_shot2 == nullptr || grad_out2 == nullptr)) return SGB_ERR_ARG;
+  // dJ/dvp = (2/vp) sum La k L(U); Born (dJ/dm) and VTI (dJ/dk, dJ/dkz) keep the plain sums
+  const float* gscale = (born || kz != nullptr) ? nullptr : model->vp;
   const long long plane = (long long)grid->nz * grid->pitch;
   const long long field = plane * grid->nshots;
   const Ring ring = make_ring(*grid, bs->iz0, bs->iz1, bs->ix0, bs->ix1, bs->ring);
   if (ring.size != bs->ring_size) return SGB_ERR_SHAPE;
   for (int i = 0; i < 3; ++i) SGB_CUDA_CHECK(cudaMemsetAsync(lbuf[i], 0, field * sizeof(float), s));
   SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot, 0, field * sizeof(float), s));
+  if (grad_shot2 != nullptr) SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot2, 0, field * sizeof(float), s));
   const int R = model->order / 2;
   const int nt = acq->nt;
   const int K = bs->ckpt_every;
@@ -521,7 +586,8 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
       const float* ring_in = j >= 3 ? bs->ring_store + (long long)(j - 3) * grid->nshots * ring.size : nullptr;
       const float* resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
       SGB_CUDA_CHECK(launch_habc_bwd(*grid, *model, *acq, ring, lbuf[l1], lbuf[l2], lbuf[lfree], ubuf[uj],
-                                     ubuf[ujm1], j >= 3 ? ubuf[ufree] : nullptr, grad_shot, ring_in, j - 1, resid, s));
+                                     ubuf[ujm1], j >= 3 ? ubuf[ufree] : nullptr, grad_shot, ring_in, j - 1, resid,
+                                     kz, grad_shot2, s));
       if (ck && j >= 3) {
         const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
         SGB_CUDA_CHECK(
@@ -537,6 +603,7 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
       lfree = old_l2;
     }
     SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, gscale, ring, grad_vp, s));
+    if (kz != nullptr) SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot2, nullptr, ring, grad_out2, s));
     return SGB_OK;
   }
   // tensor maps: haloed stencil boxes (136 x (TZ+2R)) and point boxes

@@ -72,7 +72,9 @@ struct HabcBwdArgs {
   const float* __restrict__ ujm1;  // U_{j-1}
   float* __restrict__ uout;        // U_{j-2}, or null
   float* __restrict__ grad;        // [nshots][nz][pitch] += La_j k L(U_{j-1}) inside the box
-  const float* __restrict__ k;     // vp^2 dt^2 / h^2
+  const float* __restrict__ k;     // vp^2 dt^2 / h^2 (VTI: the x coefficient plane)
+  const float* __restrict__ kz;    // VTI: the z coefficient plane (update k Lx + kz Lz), else null
+  float* __restrict__ grad2;       // VTI: [nshots][nz][pitch] += La_j Lz(U_{j-1}); grad gets La_j Lx(U_{j-1})
   const float* __restrict__ vp;
   const float* __restrict__ hb;    // blend weight b
   float lamf, muf;                 // 2 dt / h, dt^2 / h^2
@@ -184,8 +186,19 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
     const int far = a.hw + R;
     const bool interior =
         z >= (mult ? R : far) && a.nz - 1 - z >= far && x >= far && a.nx - 1 - x >= far;
+    const bool vti = a.kz != nullptr;
+    const float kzq = vti ? __ldg(a.kz + o) : 0.f;
+    const float ch = 0.5f * a.w.c[0];  // centre of the 1-D second difference
     float v;
-    if (interior) {
+    if (interior && vti) {
+      float lx = ch * kq * l1[o], lz = ch * kzq * l1[o];
+      for (int j = 1; j <= R; ++j) {
+        const long long up = o - (long long)j * a.pitch, dn = o + (long long)j * a.pitch;
+        lx += a.w.c[j] * (__ldg(a.k + o - j) * l1[o - j] + __ldg(a.k + o + j) * l1[o + j]);
+        lz += a.w.c[j] * (__ldg(a.kz + up) * l1[up] + __ldg(a.kz + dn) * l1[dn]);
+      }
+      v = 2.f * l1[o] + lx + lz - l2[o];
+    } else if (interior) {
       float lap = a.w.c[0] * kq * l1[o];
       for (int j = 1; j <= R; ++j) {
         const long long up = o - (long long)j * a.pitch, dn = o + (long long)j * a.pitch;
@@ -193,6 +206,23 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
                            __ldg(a.k + o + j) * l1[o + j]);
       }
       v = 2.f * l1[o] + lap - l2[o];
+    } else if (vti) {
+      // x neighbours weighted by k, z neighbours by kz, each with its interior share
+      auto wl = [&](int zz, int xx, const float* kp) -> float {
+        if (zz < 0 || zz >= a.nz || xx < 0 || xx >= a.nx) return 0.f;
+        const long long oo = (long long)zz * a.pitch + xx;
+        const HabcW w = habc_weights(zz, xx, a.nz, a.nx, a.hw, mult, __ldg(a.hb + oo));
+        return __ldg(kp + oo) * w.wi * l1[oo];
+      };
+      const HabcW wq = habc_weights(z, x, a.nz, a.nx, a.hw, mult, __ldg(a.hb + o));
+      float lap = ch * (kq + kzq) * wq.wi * l1[o];
+      for (int j = 1; j <= R; ++j)
+        lap += a.w.c[j] * (wl(z, x - j, a.k) + wl(z, x + j, a.k) + wl(z - j, x, a.kz) + wl(z + j, x, a.kz));
+      v = 2.f * wq.wi * l1[o] + lap - wq.wi * l2[o];
+      v += oneway_t(a, l1, l2, z, x, z, 1, 0, 0);
+      v += oneway_t(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
+      v += oneway_t(a, l1, l2, z, x, x, 0, 1, 2);
+      v += oneway_t(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
     } else {
       // interior part: 2 wi La1 + L(k wi La1) - wi La2
       auto kwl = [&](int zz, int xx) -> float {
@@ -227,18 +257,31 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
     const bool inbox = a.ring.inside(z, x);
     if (inbox) {
       const float* u1 = a.ujm1 + fb;
-      float L = a.w.c[0] * u1[o];
-      for (int j = 1; j <= R; ++j)
-        L += a.w.c[j] * (ldz(u1, z - j, x, a.nz, a.nx, a.pitch) + ldz(u1, z + j, x, a.nz, a.nx, a.pitch) +
-                         ldz(u1, z, x - j, a.nz, a.nx, a.pitch) + ldz(u1, z, x + j, a.nz, a.nx, a.pitch));
-      a.grad[fb + o] += v * kq * L;  // times 2 / vp in the shot reduction (dJ/dvp)
+      float upd;  // k L(U_{j-1}) (VTI: k Lx + kz Lz)
+      if (vti) {
+        float Lx = ch * u1[o], Lz = ch * u1[o];
+        for (int j = 1; j <= R; ++j) {
+          Lx += a.w.c[j] * (ldz(u1, z, x - j, a.nz, a.nx, a.pitch) + ldz(u1, z, x + j, a.nz, a.nx, a.pitch));
+          Lz += a.w.c[j] * (ldz(u1, z - j, x, a.nz, a.nx, a.pitch) + ldz(u1, z + j, x, a.nz, a.nx, a.pitch));
+        }
+        a.grad[fb + o] += v * Lx;  // dJ/dk
+        a.grad2[fb + o] += v * Lz;  // dJ/dkz
+        upd = kq * Lx + kzq * Lz;
+      } else {
+        float L = a.w.c[0] * u1[o];
+        for (int j = 1; j <= R; ++j)
+          L += a.w.c[j] * (ldz(u1, z - j, x, a.nz, a.nx, a.pitch) + ldz(u1, z + j, x, a.nz, a.nx, a.pitch) +
+                           ldz(u1, z, x - j, a.nz, a.nx, a.pitch) + ldz(u1, z, x + j, a.nz, a.nx, a.pitch));
+        a.grad[fb + o] += v * kq * L;  // times 2 / vp in the shot reduction (dJ/dvp)
+        upd = kq * L;
+      }
       if (a.uout != nullptr) {
         float ujv = a.uj[fb + o];
         if (a.src_ptr != nullptr) {
           for (int q = a.src_ptr[b]; q < a.src_ptr[b + 1]; ++q)
             if (a.src_z[q] == z && a.src_x[q] == x) ujv -= a.wavelet[(long long)a.src_wrow[q] * a.nt + a.t_src];
         }
-        a.uout[fb + o] = 2.f * u1[o] - ujv + kq * L;
+        a.uout[fb + o] = 2.f * u1[o] - ujv + upd;
       }
     } else if (a.uout != nullptr) {  // the saved ring around the box, 0 beyond it
       const int ri = a.ring.index(z, x);
@@ -252,8 +295,10 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
 cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
                             const Ring& ring, const float* la1, const float* la2, float* lout, const float* uj,
                             const float* ujm1, float* uout, float* grad, const float* ring_in, int t_src,
-                            const float* resid, cudaStream_t s) {
+                            const float* resid, const float* kz, float* grad2, cudaStream_t s) {
   HabcBwdArgs a;
+  a.kz = kz;
+  a.grad2 = grad2;
   a.nz = g.nz;
   a.nx = g.nx;
   a.pitch = g.pitch;

@@ -421,6 +421,129 @@ def born_loop(vp, refl, prop, damp, acq, ckpt_every=0):
     return _BornLoop.apply(refl, vp.detach(), prop, damp, acq, ckpt_every)
 
 
+def vti_coefficients(vp, eps, delta, dt, h):
+    """x / z coefficient planes of vti_habc2._time_step (vti_habc2.py:26-51):
+    sk = -2 (eps - delta) fx^2 fz^2 / ((1 + 2 eps) fx^4 + fz^4
+    + 2 (1 + delta) fx^2 fz^2 + 1e-26) with fx / fz the FFT frequencies of
+    the cell's row / column (torch.fft.fftfreq(n, d=h), as the reference's
+    meshgrid), kx = vp^2 dt^2 (1 + 2 eps + sk) / h^2, kz = vp^2 dt^2 (1 + sk) / h^2.
+    Differentiable in vp, eps and delta (the adjoint's chain rule)."""
+    nz, nx = vp.shape[-2:]
+    dev = vp.device
+    fx = torch.fft.fftfreq(nz, d=float(h), dtype=torch.float64, device=dev)
+    fz = torch.fft.fftfreq(nx, d=float(h), dtype=torch.float64, device=dev)
+    fxx, fzz = torch.meshgrid(fx, fz, indexing="ij")
+    vp, eps, delta = vp.double(), eps.double(), delta.double()
+    num = -2.0 * (eps - delta) * fxx ** 2 * fzz ** 2
+    den = (1.0 + 2.0 * eps) * fxx ** 4 + fzz ** 4 + 2.0 * (1.0 + delta) * fxx ** 2 * fzz ** 2
+    sk = num * (den + 1e-26) ** -1
+    v2 = vp ** 2 * float(dt) ** 2 / float(h) ** 2
+    return v2 * ((1.0 + 2.0 * eps) + sk), v2 * (1.0 + sk)
+
+
+class VTIPropagator(AcousticPropagator):
+    """VTI acoustic equation with the HABC (vti_habc2.py), 2nd order."""
+
+    def __init__(self, nz, nx, dt, h, bwidth=50, multiple=False, device=None):
+        super().__init__(nz, nx, dt, h, 2, "habc", bwidth, multiple, device)
+
+    def model_vti(self, vp, eps, delta, damp):
+        require_cuda(vp, "VTIPropagator.model_vti")
+        cx, cz = vti_coefficients(vp.detach(), eps.detach(), delta.detach(), self.dt, self.h)
+        coef = torch.empty(3, self.nz, self.pitch, dtype=torch.float32, device=vp.device)
+        coef[0] = 2.0
+        coef[1] = to_pitched(cx.float(), self.pitch)
+        coef[2] = to_pitched(cz.float(), self.pitch)
+        vpp = to_pitched(vp.detach().float(), self.pitch).contiguous()
+        dp = to_pitched(damp.detach().to(vp.device).float(), self.pitch).contiguous()
+        m = N.AcousticModel(2, BOUNDARY_HABC, 50, int(self.multiple), N.ptr(coef), N.ptr(vpp), N.ptr(dp))
+        return m, (vpp, dp, coef)
+
+    def step_vti(self, vp, eps, delta, damp, u, um):
+        m, keep = self.model_vti(vp, eps, delta, damp)
+        up = to_pitched(u.float(), self.pitch).contiguous()
+        ump = to_pitched(um.float(), self.pitch).contiguous()
+        out = torch.empty_like(up)
+        g = self.grid(u.shape[0])
+        N.call("sgb_vti_step", ctypes.byref(g), ctypes.byref(m), N.ptr(up), N.ptr(ump), N.ptr(out),
+               N.stream_handle())
+        return out[..., :self.nx]
+
+    def forward_vti(self, vp, eps, delta, damp, acq, *, save_for_adjoint=False, ckpt_every=0):
+        m, keep = self.model_vti(vp, eps, delta, damp)
+        B = acq.nshots
+        dev = vp.device
+        field = (B, self.nz, self.pitch)
+        buf = [torch.zeros(field, dtype=torch.float32, device=dev) for _ in range(3)]
+        records = torch.empty(acq.nt, max(acq.nrec, 1), 1, dtype=torch.float32, device=dev)
+        state = AcousticState()
+        bs_struct = None
+        if save_for_adjoint:
+            bs_struct = self._boundary_store(state, keep, B, acq.nt, ckpt_every, field, dev)
+        cur = ctypes.c_int32(0)
+        prev = ctypes.c_int32(0)
+        g = self.grid(B)
+        q = acq.struct(records if acq.nrec else None, 1)
+        N.call("sgb_vti_forward", ctypes.byref(g), ctypes.byref(m), ctypes.byref(q),
+               N.PTR3(*[b.data_ptr() for b in buf]), ctypes.byref(bs_struct) if bs_struct is not None else None,
+               ctypes.byref(cur), ctypes.byref(prev), N.stream_handle())
+        state.buf, state.cur, state.prev = buf, cur.value, prev.value
+        state.keep = keep
+        state.model = m
+        return records[:, :acq.nrec], state
+
+    def backward_vti(self, state, acq, grad_records):
+        """(dJ/dkx, dJ/dkz) planes (nz, nx) from dJ/d(records)."""
+        B = acq.nshots
+        dev = state.buf[0].device
+        resid = torch.zeros(acq.nt, max(acq.nrec, 1), 1, dtype=torch.float32, device=dev)
+        if acq.nrec:
+            resid[:, :acq.nrec] = grad_records.to(torch.float32).reshape(acq.nt, acq.nrec, 1)
+        field = (B, self.nz, self.pitch)
+        lbuf = [torch.empty(field, dtype=torch.float32, device=dev) for _ in range(3)]
+        gsx, gsz = torch.empty(field, dtype=torch.float32, device=dev), torch.empty(field, dtype=torch.float32, device=dev)
+        gx = torch.empty(self.nz, self.pitch, dtype=torch.float32, device=dev)
+        gz = torch.empty_like(gx)
+        g = self.grid(B)
+        q = acq.struct(resid, 1)
+        N.call("sgb_vti_backward", ctypes.byref(g), ctypes.byref(state.model), ctypes.byref(q),
+               ctypes.byref(state.bs), N.PTR3(*[b.data_ptr() for b in state.buf]), state.cur, state.prev,
+               N.PTR3(*[b.data_ptr() for b in lbuf]), N.ptr(gsx), N.ptr(gsz), N.ptr(gx), N.ptr(gz),
+               N.stream_handle())
+        return gx[:, :self.nx], gz[:, :self.nx]
+
+
+class _VTILoop(torch.autograd.Function):
+    """Whole VTI loop as one differentiable op: (vp, eps, delta) -> records."""
+
+    @staticmethod
+    def forward(ctx, vp, eps, delta, prop, damp, acq, ckpt_every):
+        need = any(ctx.needs_input_grad[:3])
+        rec, state = prop.forward_vti(vp, eps, delta, damp, acq, save_for_adjoint=need, ckpt_every=ckpt_every)
+        ctx.prop, ctx.acq, ctx.state = prop, acq, state
+        ctx.save_for_backward(vp, eps, delta)
+        return rec
+
+    @staticmethod
+    def backward(ctx, grad_rec):
+        if ctx.state.bs is None:
+            return (None,) * 7
+        gx, gz = ctx.prop.backward_vti(ctx.state, ctx.acq, grad_rec.contiguous())
+        ctx.state = None
+        vp, eps, delta = ctx.saved_tensors
+        with torch.enable_grad():
+            ins = [t.detach().requires_grad_(True) for t in (vp, eps, delta)]
+            cx, cz = vti_coefficients(*ins, ctx.prop.dt, ctx.prop.h)
+            grads = torch.autograd.grad((cx, cz), ins, (gx.double(), gz.double()), allow_unused=True)
+        out = [None if g_ is None else g_.to(t.dtype) for g_, t in zip(grads, (vp, eps, delta))]
+        return out[0], out[1], out[2], None, None, None, None
+
+
+def vti_loop(vp, eps, delta, prop, damp, acq, ckpt_every=0):
+    """Records (nt, nrec, 1) of the VTI loop; differentiable in vp, eps, delta."""
+    return _VTILoop.apply(vp, eps, delta, prop, damp, acq, ckpt_every)
+
+
 class UnevenBatch:
     """Acoustic PML time loops of several grids (different shapes, shots and
     trace lengths) run together: one persistent launch per step covers the

@@ -9,17 +9,19 @@ class Parameters:
         return {"acoustic": ["vp"],
                 "acoustic_habc": ["vp"],
                 "acoustic_lsrtm_habc": ["vp", "m"],
+                "vti_habc2": ["vp", "epsilon", "delta"],
                 "elastic": ["vp", "vs", "rho"]}
 
     @staticmethod
     def secondorder_equations():
-        return ["acoustic", "acoustic_habc", "acoustic_lsrtm_habc"]
+        return ["acoustic", "acoustic_habc", "acoustic_lsrtm_habc", "vti_habc2"]
 
 
 class Wavefield:
     _FIELDS = {"acoustic": ["h1", "h2"],
                "acoustic_habc": ["h1", "h2"],
                "acoustic_lsrtm_habc": ["h1", "h2", "sh1", "sh2"],
+               "vti_habc2": ["p1", "p2"],
                "elastic": ["vx", "vz", "txx", "tzz", "txz"]}
 
     def __init__(self, equation="acoustic"):
@@ -39,6 +41,10 @@ class Wavefield:
     @property
     def acoustic_lsrtm_habc(self):
         return list(self._FIELDS["acoustic_lsrtm_habc"])
+
+    @property
+    def vti_habc2(self):
+        return list(self._FIELDS["vti_habc2"])
 
     @property
     def elastic(self):

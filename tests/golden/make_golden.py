@@ -54,8 +54,13 @@ def run_case(ref, equation, models_int, *, order=2, width=20, multiple=False, ns
              grad=None, obs_models=None, source_type=None, receiver_type=None):
     torch.set_default_dtype(dtype)
     eqmod = {"acoustic": ref.acoustic, "acoustic_habc": ref.acoustic_habc,
-             "acoustic_lsrtm_habc": ref.acoustic_lsrtm_habc, "elastic": ref.elastic}[equation]
-    if equation == "acoustic_lsrtm_habc":
+             "acoustic_lsrtm_habc": ref.acoustic_lsrtm_habc, "vti_habc2": ref.vti_habc2,
+             "elastic": ref.elastic}[equation]
+    if equation == "vti_habc2":
+        # its 1-D kernels (convkernel.py:73-74, fixed 2nd order) in the run's dtype
+        eqmod.kernelx = ref.convkernel.kernelx.to(dtype)
+        eqmod.kernely = ref.convkernel.kernely.to(dtype)
+    elif equation == "acoustic_lsrtm_habc":
         # its Laplacian is acoustic_habc._laplacian, which reads acoustic_habc's kernel
         RL.set_spatial_order(ref.acoustic_habc, order, dtype)
     elif equation != "elastic":
@@ -171,6 +176,15 @@ def cases():
                                           habc=True, nt=200, grad=["m"], obs_models=None, receiver_type=["sh1"])
     C["grad_born_habc_o4"] = dict(equation="acoustic_lsrtm_habc", models_int=born, order=4, width=50,
                                   habc=True, nt=200, grad=["m"], obs_models=born_obs, receiver_type=["sh1"])
+    vti = {"vp": ah["vp"], "epsilon": layered(16, 24, [0.1, 0.2], 5, anomaly=0.05),
+           "delta": layered(16, 24, [0.05, 0.1], 6, anomaly=0.02)}
+    C["vti_habc2"] = dict(equation="vti_habc2", models_int=vti, order=2, width=50, habc=True, nt=240,
+                          source_type=["p1"], receiver_type=["p1"])
+    C["vti_habc2_multiple"] = dict(equation="vti_habc2", models_int=vti, order=2, width=50, habc=True,
+                                   multiple=True, nt=240, source_type=["p1"], receiver_type=["p1"])
+    C["grad_vti_habc2_zeroobs"] = dict(equation="vti_habc2", models_int=vti, order=2, width=50, habc=True, nt=200,
+                                       grad=["vp", "epsilon", "delta"], obs_models=None, source_type=["p1"],
+                                       receiver_type=["p1"])
     C["grad_elastic_zeroobs"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,
                                      nt=200, grad=["vp", "vs", "rho"], obs_models=None)
     C["grad_elastic"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,

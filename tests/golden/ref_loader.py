@@ -91,9 +91,11 @@ def _install_package():
     sys.modules["seistorch.equations2d"] = sub
 
 
-def _exec_patched(modname, path, device):
+def _exec_patched(modname, path, device, line_patches=()):
     with open(path) as f:
         src = f.read()
+    for old, new in line_patches:
+        src = src.replace(old, new)
     src = src.replace('device = "cuda"', f'device = "{device}"')
     spec = importlib.util.spec_from_loader(modname, loader=None, origin=path)
     mod = importlib.util.module_from_spec(spec)
@@ -116,6 +118,12 @@ def load(device="cpu"):
                                      os.path.join(PKG_DIR, "equations2d", "acoustic_habc.py"), device)
     ns.acoustic_lsrtm_habc = _exec_patched("seistorch.equations2d.acoustic_lsrtm_habc",
                                            os.path.join(PKG_DIR, "equations2d", "acoustic_lsrtm_habc.py"), device)
+    # convkernel.py:71 picks "cuda" or an Exception object as its device
+    ns.convkernel = _exec_patched(
+        "seistorch.equations2d.convkernel", os.path.join(PKG_DIR, "equations2d", "convkernel.py"), device,
+        [('device = "cuda" if torch.cuda.is_available() else Exception("No cuda device found")',
+          f'device = "{device}"')])
+    ns.vti_habc2 = importlib.import_module("seistorch.equations2d.vti_habc2")
     ns.elastic = importlib.import_module("seistorch.equations2d.elastic")
     ns.pml = importlib.import_module("seistorch.pml")
     ns.habc = importlib.import_module("seistorch.habc")
