@@ -218,6 +218,35 @@ int sgb_vti_backward(const sgb_grid *grid, const sgb_acoustic_model *model, cons
 int sgb_vti_step(const sgb_grid *grid, const sgb_acoustic_model *model, const float *u, const float *um,
                  float *unext, sgb_stream_t stream);
 
+/* --------------------------------------------------- variable density --- */
+
+/* The loop of acoustic_rho_habc._time_step
+ * (seistorch/equations2d/acoustic_rho_habc.py:34-58), second order, HABC:
+ * U+ = HABC(2U - U- + C (bx+ (U[x+1] - U) - bx- (U - U[x-1])
+ *                        + bz+ (U[z+1] - U) - bz- (U - U[z-1]))) + sources,
+ * rho_c: five planes [5][nz][pitch] = C = dt^2 rho vp^2 / h^2 and the
+ * buoyancy averages bx+ = (b + b[x+1]) / 2, bx- = (b[x-1] + b) / 2,
+ * bz+ = (b + b[z+1]) / 2, bz- = (b[z-1] + b) / 2 of b = 1 / rho with zeros
+ * beyond the grid (the reference's zero-padded convolutions); the caller
+ * computes them.  model: from sgb_acoustic_coefficients with boundary 1
+ * (order 2). */
+int sgb_rho_forward(const sgb_grid *grid, const sgb_acoustic_model *model, const float *rho_c,
+                    const sgb_acquisition *acq, float *const buf[3], const sgb_bs_store *bs,
+                    int32_t *cur_out, int32_t *prev_out, sgb_stream_t stream);
+
+/* Adjoint of sgb_rho_forward: the exact HABC adjoint of the variable-density
+ * update; grad5 receives the five planes dJ/dC, dJ/dbx+, dJ/dbx-, dJ/dbz+,
+ * dJ/dbz- inside the undamped box (0 outside), for the caller's chain rule
+ * to vp and rho.  grad_shot5: scratch [5][nshots][nz][pitch]. */
+int sgb_rho_backward(const sgb_grid *grid, const sgb_acoustic_model *model, const float *rho_c,
+                     const sgb_acquisition *acq, const sgb_bs_store *bs, float *const ubuf[3], int32_t ucur,
+                     int32_t uprev, float *const lbuf[3], float *grad_shot5, float *grad5,
+                     sgb_stream_t stream);
+
+/* One step without sources or receivers (the per-step drop-in). */
+int sgb_rho_step(const sgb_grid *grid, const sgb_acoustic_model *model, const float *rho_c, const float *u,
+                 const float *um, float *unext, sgb_stream_t stream);
+
 /* --------------------------------------------------- Born modelling --- */
 
 /* Born (linearised) modelling of the acoustic HABC equation for

@@ -308,6 +308,31 @@ def vti_habc_step(vp, eps, delta, p1, p2, dt, h, b, multiple=False, dtype=np.flo
     return y, p1
 
 
+def rho_habc_step(vp, rho, p1, p2, dt, h, b, multiple=False, dtype=np.float64):
+    """Variable-density step (acoustic_rho_habc.py:34-58): one-cell forward /
+    backward differences of p1 and buoyancy averages of 1/rho, all with the
+    zero padding of the reference's conv2d, then the HABC blend (with vp).
+    Returns (pnext, p1)."""
+    vp = np.asarray(vp, dtype)
+    rho = np.asarray(rho, dtype)
+    p1 = np.asarray(p1, dtype)
+    bu = 1 / rho
+    pp = np.pad(p1, ((0, 0), (1, 1), (1, 1)))
+    bp = np.pad(bu, 1)
+    pxp = pp[:, 1:-1, 2:] - p1
+    pxn = p1 - pp[:, 1:-1, :-2]
+    pzp = pp[:, 2:, 1:-1] - p1
+    pzn = p1 - pp[:, :-2, 1:-1]
+    bxp = (bu + bp[1:-1, 2:]) / 2
+    bxn = (bp[1:-1, :-2] + bu) / 2
+    bzp = (bu + bp[2:, 1:-1]) / 2
+    bzn = (bp[:-2, 1:-1] + bu) / 2
+    y = 2 * p1 - np.asarray(p2, dtype) + dtype(dt) ** 2 * dtype(h) ** -2 * rho * vp ** 2 * (
+        bxp * pxp - bxn * pxn + bzp * pzp - bzn * pzn)
+    y = habc_apply(y, p1, p2, vp, b, dt, h, 50, multiple, dtype)
+    return y, p1
+
+
 def dfwd(a, axis):
     """a[i] - a[i-1], zero at index 0 (equations2d/utils.py:3-25, forward)."""
     out = a - np.roll(a, 1, axis=axis)
@@ -356,9 +381,11 @@ def elastic_step(vp, vs, rho, vx, vz, txx, tzz, txz, dt, h, d, dtype=np.float64)
 
 WAVEFIELDS = {"acoustic": ["h1", "h2"], "acoustic_habc": ["h1", "h2"],
               "acoustic_lsrtm_habc": ["h1", "h2", "sh1", "sh2"], "vti_habc2": ["p1", "p2"],
+              "acoustic_rho_habc": ["h1", "h2"],
               "elastic": ["vx", "vz", "txx", "tzz", "txz"]}
 MODEL_PARAMS = {"acoustic": ["vp"], "acoustic_habc": ["vp"], "acoustic_lsrtm_habc": ["vp", "m"],
-                "vti_habc2": ["vp", "epsilon", "delta"], "elastic": ["vp", "vs", "rho"]}
+                "vti_habc2": ["vp", "epsilon", "delta"], "acoustic_rho_habc": ["vp", "rho"],
+                "elastic": ["vp", "vs", "rho"]}
 
 
 def forward(equation, models, d, dt, h, wavelet, sources, receivers, *,
@@ -404,6 +431,9 @@ def forward(equation, models, d, dt, h, wavelet, sources, receivers, *,
             out = born_habc_step(models["vp"], models["m"], fields["h1"], fields["h2"], fields["sh1"],
                                  fields["sh2"], dt, h, d, order, multiple, dtype)
             fields = dict(zip(names, out))
+        elif equation == "acoustic_rho_habc":
+            y, h1 = rho_habc_step(models["vp"], models["rho"], fields["h1"], fields["h2"], dt, h, d, multiple, dtype)
+            fields["h1"], fields["h2"] = y, h1
         elif equation == "vti_habc2":
             y, p1 = vti_habc_step(models["vp"], models["epsilon"], models["delta"], fields["p1"], fields["p2"],
                                   dt, h, d, multiple, dtype)

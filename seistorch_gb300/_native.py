@@ -158,6 +158,14 @@ SIGNATURES = {
                                         PTR3, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr]),
     "sgb_vti_step": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel), c_ptr, c_ptr, c_ptr,
                                     c_ptr]),
+    "sgb_rho_forward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel), c_ptr,
+                                       ctypes.POINTER(Acquisition), PTR3, ctypes.POINTER(BsStore),
+                                       ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_ptr]),
+    "sgb_rho_backward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel), c_ptr,
+                                        ctypes.POINTER(Acquisition), ctypes.POINTER(BsStore), PTR3, c_i32, c_i32,
+                                        PTR3, c_ptr, c_ptr, c_ptr]),
+    "sgb_rho_step": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel), c_ptr, c_ptr, c_ptr,
+                                    c_ptr, c_ptr]),
     "sgb_born_forward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel), c_ptr,
                                         ctypes.POINTER(Acquisition), PTR3, PTR3, c_ptr, ctypes.POINTER(BsStore),
                                         ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_ptr]),

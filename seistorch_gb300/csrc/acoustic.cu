@@ -221,7 +221,21 @@ __global__ void __launch_bounds__(NTHREADS) acoustic_fwd_kernel(const AcStepArgs
     const float4 vg = cin ? __ldg(reinterpret_cast<const float4*>(a.g + (long long)z * a.pitch + x)) : zero4;
     const float4 vk = cin ? __ldg(reinterpret_cast<const float4*>(a.k + (long long)z * a.pitch + x)) : zero4;
     float4 y;
-    if (HABC && a.kz != nullptr) {  // VTI: k Lx + kz Lz
+    if (HABC && R == 1 && a.rho_c != nullptr) {  // variable density: C D(u)
+      const long long po = (long long)z * a.pitch + x, pl = (long long)a.nz * a.pitch;
+      auto ld = [&](int q) {
+        return cin ? __ldg(reinterpret_cast<const float4*>(a.rho_c + q * pl + po)) : zero4;
+      };
+      const float4 C4 = ld(0), bxp = ld(1), bxn = ld(2), bzp = ld(3), bzn = ld(4);
+      const float xs[6] = {left.w, win[R].x, win[R].y, win[R].z, win[R].w, right.x};
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const float c = xs[m + 1];
+        const float D = comp(bxp, m) * (xs[m + 2] - c) - comp(bxn, m) * (c - xs[m]) +
+                        comp(bzp, m) * (comp(win[R + 1], m) - c) - comp(bzn, m) * (c - comp(win[R - 1], m));
+        set_comp(y, m, fmaf(comp(C4, m), D, fmaf(comp(vg, m), c - comp(vm, m), comp(vm, m))));
+      }
+    } else if (HABC && a.kz != nullptr) {  // VTI: k Lx + kz Lz
       float4 Lx, Lz;
       lap4_xz<R>(win, left, right, a.w, Lx, Lz);
       const float4 vz = cin ? __ldg(reinterpret_cast<const float4*>(a.kz + (long long)z * a.pitch + x)) : zero4;

@@ -46,6 +46,10 @@ struct AcStepArgs {
   // VTI (vti_habc2.py:26-56): with kz set, the update is
   // 2u - u- + k Lx(u) + kz Lz(u) (k, kz: the x and z coefficient planes)
   const float* __restrict__ kz;
+  // variable density (acoustic_rho_habc.py:34-58): with rho_c set (five
+  // planes C, bx+, bx-, bz+, bz-), the update is 2u - u- + C (bx+ (u[x+1] -
+  // u) - bx- (u - u[x-1]) + bz+ (u[z+1] - u) - bz- (u - u[z-1])); order 2
+  const float* __restrict__ rho_c;
   int* status;
 };
 

@@ -61,7 +61,8 @@ cudaError_t launch_ring_copy(const sgb_grid& gr, const Ring& ring, float* field,
 int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                            const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur, int32_t uprev,
                            float* const lbuf[3], float* grad_shot, float* grad_vp, bool born, cudaStream_t s,
-                           const float* kz = nullptr, float* grad_shot2 = nullptr, float* grad_out2 = nullptr);
+                           const float* kz = nullptr, float* grad_shot2 = nullptr, float* grad_out2 = nullptr,
+                           const float* rho_c = nullptr);
 cudaError_t launch_acoustic_grad_reduce(const sgb_grid& gr, const float* grad_shot, const float* vp,
                                         const Ring& ring, float* grad_vp, cudaStream_t s);
 int pick_tz(int nz, int nx, int nshots, int tz_max);
@@ -81,7 +82,8 @@ int set_stream_config(int fwd, int bwd, int zc);
 cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
                             const Ring& ring, const float* la1, const float* la2, float* lout, const float* uj,
                             const float* ujm1, float* uout, float* grad, const float* ring_in, int t_src,
-                            const float* resid, const float* kz, float* grad2, cudaStream_t s);
+                            const float* resid, const float* kz, float* grad2, const float* rho_c,
+                            float* grad_rho, cudaStream_t s);
 
 }  // namespace sgb
 
@@ -133,7 +135,7 @@ AcStepArgs base_step_args(const sgb_grid* g, const sgb_acoustic_model* m) {
 
 int acoustic_forward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                           float* const buf[3], float* illum, const sgb_bs_store* bs, int32_t* cur_out,
-                          int32_t* prev_out, const float* kz, cudaStream_t s);
+                          int32_t* prev_out, const float* kz, cudaStream_t s, const float* rho_c = nullptr);
 
 }  // namespace
 
@@ -245,13 +247,24 @@ int sgb_vti_forward(const sgb_grid* grid, const sgb_acoustic_model* model, const
                                model->coef + 2LL * grid->nz * grid->pitch, (cudaStream_t)stream);
 }
 
+int sgb_rho_forward(const sgb_grid* grid, const sgb_acoustic_model* model, const float* rho_c,
+                    const sgb_acquisition* acq, float* const buf[3], const sgb_bs_store* bs, int32_t* cur_out,
+                    int32_t* prev_out, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (model == nullptr || rho_c == nullptr) return SGB_ERR_ARG;
+  if (model->boundary != 1 || model->order != 2) return SGB_ERR_UNSUPPORTED;  // acoustic_rho_habc: 2nd order, HABC
+  if (!aligned16(rho_c)) return SGB_ERR_ALIGN;
+  return acoustic_forward_impl(grid, model, acq, buf, nullptr, bs, cur_out, prev_out, nullptr, (cudaStream_t)stream,
+                               rho_c);
+}
+
 }  // extern "C"
 
 namespace {
 
 int acoustic_forward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                           float* const buf[3], float* illum, const sgb_bs_store* bs, int32_t* cur_out,
-                          int32_t* prev_out, const float* kz, cudaStream_t s) {
+                          int32_t* prev_out, const float* kz, cudaStream_t s, const float* rho_c) {
   if (int e = check_grid(grid)) return e;
   if (int e = check_model(grid, model)) return e;
   if (int e = check_acq(grid, acq)) return e;
@@ -263,6 +276,7 @@ int acoustic_forward_impl(const sgb_grid* grid, const sgb_acoustic_model* model,
   if (acq->records != nullptr && acq->nch != 1) return SGB_ERR_UNSUPPORTED;
   AcStepArgs a = base_step_args(grid, model);
   a.kz = kz;
+  a.rho_c = rho_c;
   a.src_ptr = acq->nsrc > 0 ? acq->src_ptr : nullptr;
   a.src_z = acq->src_z;
   a.src_x = acq->src_x;
@@ -496,6 +510,36 @@ int sgb_vti_backward(const sgb_grid* grid, const sgb_acoustic_model* model, cons
                                      grad_z);
 }
 
+int sgb_rho_backward(const sgb_grid* grid, const sgb_acoustic_model* model, const float* rho_c,
+                     const sgb_acquisition* acq, const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur,
+                     int32_t uprev, float* const lbuf[3], float* grad_shot5, float* grad5, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (model == nullptr || rho_c == nullptr) return SGB_ERR_ARG;
+  if (model->boundary != 1 || model->order != 2) return SGB_ERR_UNSUPPORTED;
+  if (!aligned16(rho_c)) return SGB_ERR_ALIGN;
+  return sgb::acoustic_backward_impl(grid, model, acq, bs, ubuf, ucur, uprev, lbuf, grad_shot5, grad5, false,
+                                     (cudaStream_t)stream, nullptr, nullptr, nullptr, rho_c);
+}
+
+int sgb_rho_step(const sgb_grid* grid, const sgb_acoustic_model* model, const float* rho_c, const float* u,
+                 const float* um, float* unext, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (int e = check_model(grid, model)) return e;
+  if (model->boundary != 1 || model->order != 2) return SGB_ERR_UNSUPPORTED;
+  if (model->vp == nullptr || model->damp == nullptr || rho_c == nullptr) return SGB_ERR_ARG;
+  if (u == nullptr || um == nullptr || unext == nullptr) return SGB_ERR_ARG;
+  if (!aligned16(u) || !aligned16(um) || !aligned16(unext) || !aligned16(rho_c)) return SGB_ERR_ALIGN;
+  if (unext == u || unext == um) return SGB_ERR_ARG;
+  AcStepArgs a = base_step_args(grid, model);
+  a.u = u;
+  a.um = um;
+  a.un = unext;
+  a.rho_c = rho_c;
+  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 32);
+  SGB_CUDA_CHECK(launch_acoustic_fwd(1, true, tz, a, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
 int sgb_vti_step(const sgb_grid* grid, const sgb_acoustic_model* model, const float* u, const float* um,
                  float* unext, sgb_stream_t stream) {
   if (int e = check_grid(grid)) return e;
@@ -540,7 +584,7 @@ namespace sgb {
 int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                            const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur, int32_t uprev,
                            float* const lbuf[3], float* grad_shot, float* grad_vp, bool born, cudaStream_t s,
-                           const float* kz, float* grad_shot2, float* grad_out2) {
+                           const float* kz, float* grad_shot2, float* grad_out2, const float* rho_c) {
   if (int e = check_grid(grid)) return e;
   if (int e = check_model(grid, model)) return e;
   if (int e = check_acq(grid, acq)) return e;
@@ -556,16 +600,19 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
   }
   if (!aligned16(grad_shot)) return SGB_ERR_ALIGN;
   if (acq->records != nullptr && acq->nch != 1) return SGB_ERR_UNSUPPORTED;
-  if ((born || kz != nullptr) && model->boundary != 1) return SGB_ERR_UNSUPPORTED;
+  if ((born || kz != nullptr || rho_c != nullptr) && model->boundary != 1) return SGB_ERR_UNSUPPORTED;
   if (kz != nullptr && (grad_shot2 == nullptr || grad_out2 == nullptr)) return SGB_ERR_ARG;
-  // dJ/dvp = (2/vp) sum La k L(U); Born (dJ/dm) and VTI (dJ/dk, dJ/dkz) keep the plain sums
-  const float* gscale = (born || kz != nullptr) ? nullptr : model->vp;
+  // dJ/dvp = (2/vp) sum La k L(U); Born (dJ/dm), VTI (dJ/dk, dJ/dkz) and
+  // variable density (five coefficient gradients) keep the plain sums.  With
+  // rho_c, grad_shot holds five fields and grad_vp five planes.
+  const float* gscale = (born || kz != nullptr || rho_c != nullptr) ? nullptr : model->vp;
+  const int ngrad = rho_c != nullptr ? 5 : 1;
   const long long plane = (long long)grid->nz * grid->pitch;
   const long long field = plane * grid->nshots;
   const Ring ring = make_ring(*grid, bs->iz0, bs->iz1, bs->ix0, bs->ix1, bs->ring);
   if (ring.size != bs->ring_size) return SGB_ERR_SHAPE;
   for (int i = 0; i < 3; ++i) SGB_CUDA_CHECK(cudaMemsetAsync(lbuf[i], 0, field * sizeof(float), s));
-  SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot, 0, field * sizeof(float), s));
+  SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot, 0, ngrad * field * sizeof(float), s));
   if (grad_shot2 != nullptr) SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot2, 0, field * sizeof(float), s));
   const int R = model->order / 2;
   const int nt = acq->nt;
@@ -587,7 +634,7 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
       const float* resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
       SGB_CUDA_CHECK(launch_habc_bwd(*grid, *model, *acq, ring, lbuf[l1], lbuf[l2], lbuf[lfree], ubuf[uj],
                                      ubuf[ujm1], j >= 3 ? ubuf[ufree] : nullptr, grad_shot, ring_in, j - 1, resid,
-                                     kz, grad_shot2, s));
+                                     kz, grad_shot2, rho_c, rho_c != nullptr ? grad_shot : nullptr, s));
       if (ck && j >= 3) {
         const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
         SGB_CUDA_CHECK(
@@ -602,7 +649,15 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
       l1 = lfree;
       lfree = old_l2;
     }
-    SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, gscale, ring, grad_vp, s));
+    // the buoyancy planes also carry terms on the box's one-cell rim
+    Ring rim = ring;
+    rim.iz0 = ring.iz0 > 0 ? ring.iz0 - 1 : 0;
+    rim.ix0 = ring.ix0 > 0 ? ring.ix0 - 1 : 0;
+    rim.iz1 = ring.iz1 < grid->nz ? ring.iz1 + 1 : grid->nz;
+    rim.ix1 = ring.ix1 < grid->nx ? ring.ix1 + 1 : grid->nx;
+    for (int q = 0; q < ngrad; ++q)
+      SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot + q * field, gscale, q == 0 ? ring : rim,
+                                                 grad_vp + q * plane, s));
     if (kz != nullptr) SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot2, nullptr, ring, grad_out2, s));
     return SGB_OK;
   }

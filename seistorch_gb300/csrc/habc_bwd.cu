@@ -75,6 +75,10 @@ struct HabcBwdArgs {
   const float* __restrict__ k;     // vp^2 dt^2 / h^2 (VTI: the x coefficient plane)
   const float* __restrict__ kz;    // VTI: the z coefficient plane (update k Lx + kz Lz), else null
   float* __restrict__ grad2;       // VTI: [nshots][nz][pitch] += La_j Lz(U_{j-1}); grad gets La_j Lx(U_{j-1})
+  // variable density: planes C, bx+, bx-, bz+, bz- (update C D(U)), and five
+  // gradient fields [5][nshots][nz][pitch] (dJ/dC, dJ/dbx+, dJ/dbx-, dJ/dbz+, dJ/dbz-)
+  const float* __restrict__ rho_c;
+  float* __restrict__ grad_rho;
   const float* __restrict__ vp;
   const float* __restrict__ hb;    // blend weight b
   float lamf, muf;                 // 2 dt / h, dt^2 / h^2
@@ -187,10 +191,34 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
     const bool interior =
         z >= (mult ? R : far) && a.nz - 1 - z >= far && x >= far && a.nx - 1 - x >= far;
     const bool vti = a.kz != nullptr;
+    const bool rho = R == 1 && a.rho_c != nullptr;
     const float kzq = vti ? __ldg(a.kz + o) : 0.f;
     const float ch = 0.5f * a.w.c[0];  // centre of the 1-D second difference
+    const long long pl = (long long)a.nz * a.pitch;
     float v;
-    if (interior && vti) {
+    if (rho) {
+      // transpose of C D: the cell's own -(bx+ + bx- + bz+ + bz-) C w, plus
+      // bx+ C w of the left neighbour, bx- C w of the right one, bz+ C w of
+      // the row above and bz- C w of the row below (w = wi La1)
+      auto cw = [&](int zz, int xx, int q) -> float {  // C * coefficient q * wi * La1 at (zz, xx)
+        if (zz < 0 || zz >= a.nz || xx < 0 || xx >= a.nx) return 0.f;
+        const long long oo = (long long)zz * a.pitch + xx;
+        const float wi = interior ? 1.f : habc_weights(zz, xx, a.nz, a.nx, a.hw, mult, __ldg(a.hb + oo)).wi;
+        return __ldg(a.rho_c + oo) * __ldg(a.rho_c + q * pl + oo) * wi * l1[oo];
+      };
+      const float wq = interior ? 1.f : habc_weights(z, x, a.nz, a.nx, a.hw, mult, __ldg(a.hb + o)).wi;
+      const float sum = __ldg(a.rho_c + pl + o) + __ldg(a.rho_c + 2 * pl + o) + __ldg(a.rho_c + 3 * pl + o) +
+                        __ldg(a.rho_c + 4 * pl + o);
+      const float own = -sum * __ldg(a.rho_c + o) * wq * l1[o];
+      v = 2.f * wq * l1[o] + (own + cw(z, x - 1, 1) + cw(z, x + 1, 2) + cw(z - 1, x, 3) + cw(z + 1, x, 4)) -
+          wq * l2[o];
+      if (!interior) {
+        v += oneway_t(a, l1, l2, z, x, z, 1, 0, 0);
+        v += oneway_t(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
+        v += oneway_t(a, l1, l2, z, x, x, 0, 1, 2);
+        v += oneway_t(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
+      }
+    } else if (interior && vti) {
       float lx = ch * kq * l1[o], lz = ch * kzq * l1[o];
       for (int j = 1; j <= R; ++j) {
         const long long up = o - (long long)j * a.pitch, dn = o + (long long)j * a.pitch;
@@ -257,8 +285,24 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
     const bool inbox = a.ring.inside(z, x);
     if (inbox) {
       const float* u1 = a.ujm1 + fb;
-      float upd;  // k L(U_{j-1}) (VTI: k Lx + kz Lz)
-      if (vti) {
+      float upd;  // k L(U_{j-1}) (VTI: k Lx + kz Lz; variable density: C D(U))
+      if (rho) {
+        const float u0 = u1[o];
+        const float dxp = ldz(u1, z, x + 1, a.nz, a.nx, a.pitch) - u0, dxn = u0 - ldz(u1, z, x - 1, a.nz, a.nx, a.pitch);
+        const float dzp = ldz(u1, z + 1, x, a.nz, a.nx, a.pitch) - u0, dzn = u0 - ldz(u1, z - 1, x, a.nz, a.nx, a.pitch);
+        const float bxp = __ldg(a.rho_c + pl + o), bxn = __ldg(a.rho_c + 2 * pl + o);
+        const float bzp = __ldg(a.rho_c + 3 * pl + o), bzn = __ldg(a.rho_c + 4 * pl + o);
+        const float D = bxp * dxp - bxn * dxn + bzp * dzp - bzn * dzn;
+        const float C = __ldg(a.rho_c + o);
+        const long long fs = (long long)a.nshots * a.sstride;  // one gradient field
+        float* gr = a.grad_rho + fb + o;
+        gr[0] += v * D;
+        gr[fs] += v * C * dxp;
+        gr[2 * fs] -= v * C * dxn;
+        gr[3 * fs] += v * C * dzp;
+        gr[4 * fs] -= v * C * dzn;
+        upd = C * D;
+      } else if (vti) {
         float Lx = ch * u1[o], Lz = ch * u1[o];
         for (int j = 1; j <= R; ++j) {
           Lx += a.w.c[j] * (ldz(u1, z, x - j, a.nz, a.nx, a.pitch) + ldz(u1, z, x + j, a.nz, a.nx, a.pitch));
@@ -283,9 +327,28 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
         }
         a.uout[fb + o] = 2.f * u1[o] - ujv + upd;
       }
-    } else if (a.uout != nullptr) {  // the saved ring around the box, 0 beyond it
-      const int ri = a.ring.index(z, x);
-      a.uout[fb + o] = (ri >= 0 && a.ring_in != nullptr) ? a.ring_in[(long long)b * a.ring.size + ri] : 0.f;
+    } else {
+      if (rho) {
+        // the box's one-cell rim: the half-point buoyancy terms that reach
+        // into the box (their U values are the box's and the saved ring's),
+        // so that dJ/drho is complete at the box's edge cells
+        const bool xr = a.ring.inside(z, x + 1), xl = a.ring.inside(z, x - 1);
+        const bool zd = a.ring.inside(z + 1, x), zu = a.ring.inside(z - 1, x);
+        if (xr || xl || zd || zu) {
+          const float* u1 = a.ujm1 + fb;
+          const float u0 = u1[o], vC = v * __ldg(a.rho_c + o);
+          const long long fs = (long long)a.nshots * a.sstride;
+          float* gr = a.grad_rho + fb + o;
+          if (xr) gr[fs] += vC * (u1[o + 1] - u0);
+          if (xl) gr[2 * fs] -= vC * (u0 - u1[o - 1]);
+          if (zd) gr[3 * fs] += vC * (u1[o + a.pitch] - u0);
+          if (zu) gr[4 * fs] -= vC * (u0 - u1[o - a.pitch]);
+        }
+      }
+      if (a.uout != nullptr) {  // the saved ring around the box, 0 beyond it
+        const int ri = a.ring.index(z, x);
+        a.uout[fb + o] = (ri >= 0 && a.ring_in != nullptr) ? a.ring_in[(long long)b * a.ring.size + ri] : 0.f;
+      }
     }
   }
 }
@@ -295,10 +358,13 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
 cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
                             const Ring& ring, const float* la1, const float* la2, float* lout, const float* uj,
                             const float* ujm1, float* uout, float* grad, const float* ring_in, int t_src,
-                            const float* resid, const float* kz, float* grad2, cudaStream_t s) {
+                            const float* resid, const float* kz, float* grad2, const float* rho_c,
+                            float* grad_rho, cudaStream_t s) {
   HabcBwdArgs a;
   a.kz = kz;
   a.grad2 = grad2;
+  a.rho_c = rho_c;
+  a.grad_rho = grad_rho;
   a.nz = g.nz;
   a.nx = g.nx;
   a.pitch = g.pitch;

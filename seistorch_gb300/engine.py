@@ -544,6 +544,127 @@ def vti_loop(vp, eps, delta, prop, damp, acq, ckpt_every=0):
     return _VTILoop.apply(vp, eps, delta, prop, damp, acq, ckpt_every)
 
 
+def rho_coefficients(vp, rho, dt, h):
+    """Five planes of acoustic_rho_habc._time_step (acoustic_rho_habc.py:34-58):
+    C = dt^2 rho vp^2 / h^2 and the buoyancy averages bx+, bx-, bz+, bz- of
+    b = 1 / rho ((b + b[x+1]) / 2 ... with zeros beyond the grid, the
+    reference's zero-padded convolutions).  Differentiable in vp and rho."""
+    vp, rho = vp.double(), rho.double()
+    b = 1.0 / rho
+    bp = torch.nn.functional.pad(b, (1, 1, 1, 1))
+    bxp = (b + bp[1:-1, 2:]) / 2
+    bxn = (bp[1:-1, :-2] + b) / 2
+    bzp = (b + bp[2:, 1:-1]) / 2
+    bzn = (bp[:-2, 1:-1] + b) / 2
+    C = float(dt) ** 2 / float(h) ** 2 * rho * vp ** 2
+    return C, bxp, bxn, bzp, bzn
+
+
+class RhoPropagator(AcousticPropagator):
+    """Variable-density acoustic equation with the HABC (acoustic_rho_habc.py),
+    2nd order."""
+
+    def __init__(self, nz, nx, dt, h, bwidth=50, multiple=False, device=None):
+        super().__init__(nz, nx, dt, h, 2, "habc", bwidth, multiple, device)
+
+    def planes(self, vp, rho):
+        planes = rho_coefficients(vp.detach(), rho.detach(), self.dt, self.h)
+        out = torch.empty(5, self.nz, self.pitch, dtype=torch.float32, device=vp.device)
+        for i, p_ in enumerate(planes):
+            out[i] = to_pitched(p_.float(), self.pitch)
+        return out
+
+    def step_rho(self, vp, rho, damp, u, um):
+        m, keep = self.model(vp, damp)
+        rc = self.planes(vp, rho)
+        up = to_pitched(u.float(), self.pitch).contiguous()
+        ump = to_pitched(um.float(), self.pitch).contiguous()
+        out = torch.empty_like(up)
+        g = self.grid(u.shape[0])
+        N.call("sgb_rho_step", ctypes.byref(g), ctypes.byref(m), N.ptr(rc), N.ptr(up), N.ptr(ump), N.ptr(out),
+               N.stream_handle())
+        return out[..., :self.nx]
+
+    def forward_rho(self, vp, rho, damp, acq, *, save_for_adjoint=False, ckpt_every=0):
+        m, keep = self.model(vp, damp)
+        rc = self.planes(vp, rho)
+        B = acq.nshots
+        dev = vp.device
+        field = (B, self.nz, self.pitch)
+        buf = [torch.zeros(field, dtype=torch.float32, device=dev) for _ in range(3)]
+        records = torch.empty(acq.nt, max(acq.nrec, 1), 1, dtype=torch.float32, device=dev)
+        state = AcousticState()
+        bs_struct = None
+        if save_for_adjoint:
+            bs_struct = self._boundary_store(state, keep, B, acq.nt, ckpt_every, field, dev)
+        cur = ctypes.c_int32(0)
+        prev = ctypes.c_int32(0)
+        g = self.grid(B)
+        q = acq.struct(records if acq.nrec else None, 1)
+        N.call("sgb_rho_forward", ctypes.byref(g), ctypes.byref(m), N.ptr(rc), ctypes.byref(q),
+               N.PTR3(*[b.data_ptr() for b in buf]), ctypes.byref(bs_struct) if bs_struct is not None else None,
+               ctypes.byref(cur), ctypes.byref(prev), N.stream_handle())
+        state.buf, state.cur, state.prev = buf, cur.value, prev.value
+        state.keep = (keep, rc)
+        state.model = m
+        state.rho_c = rc
+        return records[:, :acq.nrec], state
+
+    def backward_rho(self, state, acq, grad_records):
+        """The five coefficient gradients (5, nz, nx) from dJ/d(records)."""
+        B = acq.nshots
+        dev = state.buf[0].device
+        resid = torch.zeros(acq.nt, max(acq.nrec, 1), 1, dtype=torch.float32, device=dev)
+        if acq.nrec:
+            resid[:, :acq.nrec] = grad_records.to(torch.float32).reshape(acq.nt, acq.nrec, 1)
+        field = (B, self.nz, self.pitch)
+        lbuf = [torch.empty(field, dtype=torch.float32, device=dev) for _ in range(3)]
+        gshot = torch.empty(5, *field, dtype=torch.float32, device=dev)
+        grad = torch.empty(5, self.nz, self.pitch, dtype=torch.float32, device=dev)
+        g = self.grid(B)
+        q = acq.struct(resid, 1)
+        N.call("sgb_rho_backward", ctypes.byref(g), ctypes.byref(state.model), N.ptr(state.rho_c), ctypes.byref(q),
+               ctypes.byref(state.bs), N.PTR3(*[b.data_ptr() for b in state.buf]), state.cur, state.prev,
+               N.PTR3(*[b.data_ptr() for b in lbuf]), N.ptr(gshot), N.ptr(grad), N.stream_handle())
+        return grad[:, :, :self.nx]
+
+
+class _RhoLoop(torch.autograd.Function):
+    """Whole variable-density loop as one differentiable op: (vp, rho) -> records."""
+
+    @staticmethod
+    def forward(ctx, vp, rho, prop, damp, acq, ckpt_every):
+        need = any(ctx.needs_input_grad[:2])
+        rec, state = prop.forward_rho(vp, rho, damp, acq, save_for_adjoint=need, ckpt_every=ckpt_every)
+        ctx.prop, ctx.acq, ctx.state = prop, acq, state
+        ctx.save_for_backward(vp, rho)
+        return rec
+
+    @staticmethod
+    def backward(ctx, grad_rec):
+        if ctx.state.bs is None:
+            return (None,) * 6
+        g5 = ctx.prop.backward_rho(ctx.state, ctx.acq, grad_rec.contiguous())
+        ctx.state = None
+        vp, rho = ctx.saved_tensors
+        with torch.enable_grad():
+            ins = [t.detach().requires_grad_(True) for t in (vp, rho)]
+            planes = rho_coefficients(*ins, ctx.prop.dt, ctx.prop.h)
+            grads = torch.autograd.grad(planes, ins, [g.double() for g in g5], allow_unused=True)
+        # defined inside the undamped box (the rim terms only complete the
+        # box's edge cells), 0 outside, as the other adjoints
+        iz0, iz1, ix0, ix1 = interior_box(ctx.prop.nz, ctx.prop.nx, ctx.prop.bwidth, ctx.prop.multiple)
+        box = torch.zeros_like(vp, dtype=torch.bool)
+        box[iz0:iz1, ix0:ix1] = True
+        out = [None if g_ is None else torch.where(box, g_, 0.0).to(t.dtype) for g_, t in zip(grads, (vp, rho))]
+        return out[0], out[1], None, None, None, None
+
+
+def rho_loop(vp, rho, prop, damp, acq, ckpt_every=0):
+    """Records (nt, nrec, 1) of the variable-density loop; differentiable in vp and rho."""
+    return _RhoLoop.apply(vp, rho, prop, damp, acq, ckpt_every)
+
+
 class UnevenBatch:
     """Acoustic PML time loops of several grids (different shapes, shots and
     trace lengths) run together: one persistent launch per step covers the

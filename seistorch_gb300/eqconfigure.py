@@ -10,11 +10,12 @@ class Parameters:
                 "acoustic_habc": ["vp"],
                 "acoustic_lsrtm_habc": ["vp", "m"],
                 "vti_habc2": ["vp", "epsilon", "delta"],
+                "acoustic_rho_habc": ["vp", "rho"],
                 "elastic": ["vp", "vs", "rho"]}
 
     @staticmethod
     def secondorder_equations():
-        return ["acoustic", "acoustic_habc", "acoustic_lsrtm_habc", "vti_habc2"]
+        return ["acoustic", "acoustic_habc", "acoustic_rho_habc", "acoustic_lsrtm_habc", "vti_habc2"]
 
 
 class Wavefield:
@@ -22,6 +23,7 @@ class Wavefield:
                "acoustic_habc": ["h1", "h2"],
                "acoustic_lsrtm_habc": ["h1", "h2", "sh1", "sh2"],
                "vti_habc2": ["p1", "p2"],
+               "acoustic_rho_habc": ["h1", "h2"],
                "elastic": ["vx", "vz", "txx", "tzz", "txz"]}
 
     def __init__(self, equation="acoustic"):
@@ -41,6 +43,10 @@ class Wavefield:
     @property
     def acoustic_lsrtm_habc(self):
         return list(self._FIELDS["acoustic_lsrtm_habc"])
+
+    @property
+    def acoustic_rho_habc(self):
+        return list(self._FIELDS["acoustic_rho_habc"])
 
     @property
     def vti_habc2(self):

@@ -1,0 +1,65 @@
+"""Variable-density acoustic equation with the hybrid absorbing boundary
+(seistorch/equations2d/acoustic_rho_habc.py): 2 p1 - p2 + dt^2 h^-2 rho vp^2
+(bx+ dx+ p - bx- dx- p + bz+ dz+ p - bz- dz- p) with averaged buoyancies,
+then the one-way-wave blend (``engine.rho_coefficients``).  ``_time_step`` is
+one native step (``sgb_rho_step``); the whole loop with its adjoint runs
+through ``WaveRNN`` (``engine.rho_loop``)."""
+import torch
+
+from .. import engine
+from ._acoustic_common import _scalar
+
+_CACHE = {}
+
+
+def _propagator(shape, dt, h, multiple, device):
+    key = (tuple(shape), dt, h, multiple, str(device))
+    prop = _CACHE.get(key)
+    if prop is None:
+        prop = engine.RhoPropagator(shape[-2], shape[-1], dt, h, 50, multiple, device)
+        _CACHE[key] = prop
+    return prop
+
+
+def _step(args, multiple):
+    vp, rho = args[0:2]
+    p1, p2 = args[2:4]
+    dt, h, b = args[4:7]
+    engine.require_cuda(p1, "_time_step")
+    squeeze = p1.ndim == 2
+    if squeeze:
+        p1, p2 = p1[None], p2[None]
+    if torch.is_grad_enabled() and any(t.requires_grad for t in (vp, rho, p1, p2)):
+        raise NotImplementedError("the per-step variable-density op is forward-only; differentiate the whole "
+                                  "loop through WaveRNN (engine.rho_loop)")
+    prop = _propagator(p1.shape, _scalar(dt), _scalar(h), multiple, p1.device)
+    y = prop.step_rho(vp, rho, b.to(p1.device), p1, p2).to(p1.dtype)
+    return (y[0], p1[0]) if squeeze else (y, p1)
+
+
+def _time_step(*args, **kwargs):
+    habcs = kwargs.get("habcs")
+    multiple = habcs is not None and habcs[0] is None
+    return _step(args, multiple)
+
+
+def _backward(args, multiple):
+    """Reverse step of the reference's boundary-saving path
+    (acoustic_rho_habc.py:60-121): the forward update with (p1, p2) =
+    (u_{n+1}, u_n), saved strips restored, the source re-added."""
+    from .utils import restore_boundaries
+    h_bd, _ = args[-2]
+    src_type, src_func, src_values = args[-1]
+    y, p1 = _step(args[:7], multiple)
+    with torch.no_grad():
+        y = restore_boundaries(y, h_bd, multiple=multiple)
+    y = src_func(y, src_values, 1)
+    return y, p1
+
+
+def _time_step_backward(*args, **kwargs):
+    return _backward(args, False)
+
+
+def _time_step_backward_multiple(*args, **kwargs):
+    return _backward(args, True)

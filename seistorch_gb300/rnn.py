@@ -113,6 +113,15 @@ class WaveRNN(torch.nn.Module):
             ck = geom.ckpt_every or engine.default_ckpt_every(acq.nt)
             rec = engine.born_loop(models[0].to(torch.float32), models[1].to(torch.float32), prop, d, acq, ck)
             self._fields = prop
+        elif eq == "acoustic_rho_habc":
+            if list(geom.source_type) != ["h1"] or list(geom.receiver_type) != ["h1"]:
+                raise NotImplementedError("acoustic_rho_habc injects into and records h1")
+            if not geom.use_habc:
+                raise NotImplementedError("acoustic_rho_habc runs with the HABC boundary")
+            prop = engine.RhoPropagator(nz, nx, geom.dt, float(geom.h), geom.bwidth, geom.multiple, device)
+            ck = geom.ckpt_every or engine.default_ckpt_every(acq.nt)
+            rec = engine.rho_loop(models[0].to(torch.float32), models[1].to(torch.float32), prop, d, acq, ck)
+            self._fields = prop
         elif eq == "vti_habc2":
             if list(geom.source_type) != ["p1"] or list(geom.receiver_type) != ["p1"]:
                 raise NotImplementedError("vti_habc2 injects into and records p1")

@@ -55,8 +55,13 @@ def run_case(ref, equation, models_int, *, order=2, width=20, multiple=False, ns
     torch.set_default_dtype(dtype)
     eqmod = {"acoustic": ref.acoustic, "acoustic_habc": ref.acoustic_habc,
              "acoustic_lsrtm_habc": ref.acoustic_lsrtm_habc, "vti_habc2": ref.vti_habc2,
-             "elastic": ref.elastic}[equation]
-    if equation == "vti_habc2":
+             "acoustic_rho_habc": ref.acoustic_rho_habc, "elastic": ref.elastic}[equation]
+    if equation == "acoustic_rho_habc":
+        # its one-cell difference / averaging kernels (convkernel.py:79-89) in the run's dtype
+        for n in ("kernelx_gc_pos", "kernelx_gc_neg", "kernely_gc_pos", "kernely_gc_neg", "kernelx_gc_pos2",
+                  "kernelx_gc_neg2", "kernely_gc_pos2", "kernely_gc_neg2"):
+            setattr(eqmod, n, getattr(ref.convkernel, n).to(dtype))
+    elif equation == "vti_habc2":
         # its 1-D kernels (convkernel.py:73-74, fixed 2nd order) in the run's dtype
         eqmod.kernelx = ref.convkernel.kernelx.to(dtype)
         eqmod.kernely = ref.convkernel.kernely.to(dtype)
@@ -185,6 +190,12 @@ def cases():
     C["grad_vti_habc2_zeroobs"] = dict(equation="vti_habc2", models_int=vti, order=2, width=50, habc=True, nt=200,
                                        grad=["vp", "epsilon", "delta"], obs_models=None, source_type=["p1"],
                                        receiver_type=["p1"])
+    rho = {"vp": ah["vp"], "rho": layered(16, 24, [1000.0, 2200.0], 7, anomaly=300.0)}
+    C["rho_habc"] = dict(equation="acoustic_rho_habc", models_int=rho, order=2, width=50, habc=True, nt=240)
+    C["rho_habc_multiple"] = dict(equation="acoustic_rho_habc", models_int=rho, order=2, width=50, habc=True,
+                                  multiple=True, nt=240)
+    C["grad_rho_habc_zeroobs"] = dict(equation="acoustic_rho_habc", models_int=rho, order=2, width=50, habc=True,
+                                      nt=200, grad=["vp", "rho"], obs_models=None)
     C["grad_elastic_zeroobs"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,
                                      nt=200, grad=["vp", "vs", "rho"], obs_models=None)
     C["grad_elastic"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,

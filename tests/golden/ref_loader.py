@@ -124,6 +124,7 @@ def load(device="cpu"):
         [('device = "cuda" if torch.cuda.is_available() else Exception("No cuda device found")',
           f'device = "{device}"')])
     ns.vti_habc2 = importlib.import_module("seistorch.equations2d.vti_habc2")
+    ns.acoustic_rho_habc = importlib.import_module("seistorch.equations2d.acoustic_rho_habc")
     ns.elastic = importlib.import_module("seistorch.equations2d.elastic")
     ns.pml = importlib.import_module("seistorch.pml")
     ns.habc = importlib.import_module("seistorch.habc")
