@@ -189,11 +189,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="acoustic_gradient",
                     choices=["acoustic_gradient", "elastic_gradient", "uneven_forward", "learned_fwi", "learned_net",
-                             "born_gradient", "vti_gradient"],
+                             "born_gradient", "vti_gradient", "rho_gradient"],
                     help="acoustic_gradient (default, the headline line); elastic_gradient: 300x800 + 50 PML "
                          "elastic forward+adjoint; uneven_forward: 4 grid sizes x 64 shots in one launch per step; "
                          "born_gradient: least-squares RTM gradient (Born modelling, HABC); "
-                         "vti_gradient: VTI (vti_habc2) vp / eps / delta gradient")
+                         "vti_gradient: VTI (vti_habc2) vp / eps / delta gradient; "
+                         "rho_gradient: variable-density (acoustic_rho_habc) vp / rho gradient")
     ap.add_argument("--pairs", type=int, default=2000, help="learned_fwi: training pairs")
     ap.add_argument("--epochs", type=int, default=12, help="learned_fwi: training epochs")
     ap.add_argument("--iters", type=int, default=20, help="learned_fwi: FWI iterations")
@@ -211,6 +212,8 @@ def main():
         return bench_born(args)
     if args.workload == "vti_gradient":
         return bench_vti(args)
+    if args.workload == "rho_gradient":
+        return bench_rho(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -712,6 +715,98 @@ def bench_vti(args):
                                  "frac": fwd_gbs / peak, "unit": "GB/s", "launch_ms": fwd_ms / nt},
             # per step: NT forward + NT ring gathers, NT-1 reverse, coefficients, misfit, 2 reductions
             "gpu_launches": args.steps * (2 * nt + (nt - 1) + 3), "clocks": clocks.summary()}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------- variable density ---
+# acoustic_rho_habc gradient: the Born grid and geometry (400 x 1000 + 50
+# HABC, 2nd order, 2000 steps, 32 shots), the layered vp and a Gardner
+# density rho = 310 vp^0.25; L2 residual against data from the true model,
+# gradient at the smoothed model (vp, rho).
+def bench_rho(args):
+    import torch
+    from scipy.ndimage import gaussian_filter
+    from seistorch_gb300 import _native, engine
+    from seistorch_gb300.habc import generate_habc_coefficients_2d
+    from seistorch_gb300.postprocess import L2
+    from seistorch_gb300.utils import ricker_wave
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm is timed on the acoustic "
+                          "gradient workload only"}))
+        return 0
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _native.load(build_if_missing=False)
+    nt = args.nt if args.nt != NT else BN_NT
+    shots = args.shots if args.shots != NSHOTS else BN_SHOTS
+    v0, m_true = born_models()
+    vp_true = v0 * (1.0 + 0.5 * m_true)
+    rho_true = 310.0 * vp_true ** 0.25
+    init = [gaussian_filter(a, sigma=12) for a in (vp_true, rho_true)]
+    nz, nx = v0.shape
+    b = generate_habc_coefficients_2d((nz, nx), BN_W).to(torch.float32)
+    wav = ricker_wave(BN_FM, BN_DT, nt, delay=int(1.2 / BN_FM / BN_DT), dtype="numpy")
+    xs = np.linspace(0, BN_NXI - 1, shots).round().astype(int)
+    src = [[(BN_W + 2, BN_W + int(x))] for x in xs]
+    rec = [([BN_W + 2] * BN_NXI, list(range(BN_W, BN_W + BN_NXI)))] * shots
+    prop = engine.RhoPropagator(nz, nx, BN_DT, BN_H, BN_W, False, dev)
+    acq = engine.Acquisition(nz, nx, src, rec, wav, dev)
+    t = lambda a, rg=False: torch.tensor(a, dtype=torch.float32, device=dev, requires_grad=rg)
+    bb = b.to(dev)
+    ck = engine.default_ckpt_every(nt)
+    with torch.no_grad():
+        obs = engine.rho_loop(t(vp_true), t(rho_true), prop, bb, acq).contiguous()
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def step(timing=None):
+        ms = [t(a, True) for a in init]
+        e0, e1, e2 = ev(), ev(), ev()
+        e0.record(stream)
+        r = engine.rho_loop(*ms, prop, bb, acq, ck)
+        e1.record(stream)
+        loss = L2()(r, obs)
+        loss.backward()
+        e2.record(stream)
+        if timing is not None:
+            timing.append((e0, e1, e2))
+        return loss
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    timing = []
+    with ClockSampler(0) as clocks:
+        t0, t1 = ev(), ev()
+        t0.record(stream)
+        for _ in range(args.steps):
+            step(timing)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms_ = t0.elapsed_time(t1) / args.steps
+    fwd_ms = float(np.median([a.elapsed_time(c) for a, c, _ in timing]))
+    rev_ms = float(np.median([c.elapsed_time(e) for _, c, e in timing]))
+    npts = nz * nx
+    fwd_bytes = shots * npts * 12 + npts * 32   # read u, u-, write u+; g, C, 4 buoyancy, vp, b planes
+    rev_bytes = shots * npts * 64 + npts * 32   # read La1, La2, U_j, U_{j-1}; write La_j, U_{j-2}; 5 gradients r/w
+    peak, kind = measured_peaks()
+    rev_gbs = rev_bytes / (rev_ms / (nt - 1) * 1e-3) / 1e9
+    fwd_gbs = fwd_bytes / (fwd_ms / nt * 1e-3) / 1e9
+    line = {"metric": "Gpts/s fwd+adjoint", "value": shots * npts * nt / (ms_ * 1e-3) / 1e9, "unit": "Gpts/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"rho_l2_gradient_{BN_NZI}x{BN_NXI}_habc{BN_W}_o2_nt{nt}_{shots}shots",
+                       "grid": [nz, nx], "shots": shots, "nt": nt, "ckpt_every": ck,
+                       "l2": "inputs larger than L2 (70 MB per field)"},
+            "shots_per_s": shots / (ms_ * 1e-3), "phases_ms": {"forward": fwd_ms, "adjoint": rev_ms},
+            "roofline": {"kernel": "habc_bwd_kernel (variable density)", "bound": "hbm", "achieved": rev_gbs,
+                         "peak": peak, "peak_kind": kind, "unit": "GB/s", "frac": rev_gbs / peak, "traffic": None,
+                         "bytes_per_launch": rev_bytes, "launch_ms": rev_ms / (nt - 1)},
+            "roofline_forward": {"kernel": "acoustic_fwd_kernel<HABC> (variable density)", "achieved": fwd_gbs,
+                                 "frac": fwd_gbs / peak, "unit": "GB/s", "launch_ms": fwd_ms / nt},
+            # per step: NT forward + NT ring gathers, NT-1 reverse, coefficients, misfit, 5 reductions
+            "gpu_launches": args.steps * (2 * nt + (nt - 1) + 7), "clocks": clocks.summary()}
     print(json.dumps(line))
     return 0
 
