@@ -232,3 +232,61 @@ def test_pickled_geometry_and_shot_files_round_trip(tmp_path):
     path = io.write_shots(str(tmp_path / "obs.hdf5"), shots)
     for i in range(2):
         assert np.array_equal(io.read_shot(path, i), shots[i])
+
+
+def test_vti_coefficient_map_matches_oracle():
+    """engine.vti_coefficients (the planes the VTI kernels and their chain
+    rule use) against the oracle's restatement of vti_habc2.py:36-51."""
+    from oracle import fd2d
+    from seistorch_gb300 import engine
+    g = load("vti_habc2")
+    vp, eps, delta = (g["models"][n] for n in ("vp", "epsilon", "delta"))
+    t = lambda a: torch.tensor(a, dtype=torch.float64)
+    cx, cz = engine.vti_coefficients(t(vp), t(eps), t(delta), g["dt"], g["h"])
+    sk = fd2d.vti_sk(eps, delta, g["h"])
+    v2 = vp ** 2 * g["dt"] ** 2 / g["h"] ** 2
+    assert rel_l2(cx.numpy(), v2 * (1 + 2 * eps + sk)) < 1e-14
+    assert rel_l2(cz.numpy(), v2 * (1 + sk)) < 1e-14
+    assert np.abs(sk[0]).max() == 0 and np.abs(sk[:, 0]).max() == 0  # zero frequency rows / columns
+
+
+def test_rho_coefficient_map_zero_padding():
+    """engine.rho_coefficients: C = dt^2 rho vp^2 / h^2 and the buoyancy
+    averages with zeros beyond the grid (acoustic_rho_habc.py:44-51)."""
+    from seistorch_gb300 import engine
+    rng = np.random.default_rng(0)
+    vp = 1500 + 1000 * rng.random((5, 6))
+    rho = 1000 + 1500 * rng.random((5, 6))
+    C, bxp, bxn, bzp, bzn = (p.numpy() for p in engine.rho_coefficients(torch.tensor(vp), torch.tensor(rho),
+                                                                         0.001, 10.0))
+    b = 1 / rho
+    assert np.allclose(C, 1e-8 * rho * vp ** 2, rtol=1e-14)
+    assert np.allclose(bxp[:, :-1], (b[:, :-1] + b[:, 1:]) / 2) and np.allclose(bxp[:, -1], b[:, -1] / 2)
+    assert np.allclose(bxn[:, 1:], (b[:, :-1] + b[:, 1:]) / 2) and np.allclose(bxn[:, 0], b[:, 0] / 2)
+    assert np.allclose(bzp[:-1], (b[:-1] + b[1:]) / 2) and np.allclose(bzp[-1], b[-1] / 2)
+    assert np.allclose(bzn[1:], (b[:-1] + b[1:]) / 2) and np.allclose(bzn[0], b[0] / 2)
+
+
+def test_neighbour_equation_entry_points_validate(lib):
+    """The Born, VTI and variable-density entry points refuse a PML model or a
+    missing plane before any CUDA call."""
+    from seistorch_gb300 import _native as N
+    g = N.Grid(64, 64, 64, 1, 0.001, 10.0)
+    pml = N.AcousticModel(2, 0, 50, 0, ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16))
+    habc4 = N.AcousticModel(4, 1, 50, 0, ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16))
+    p = ctypes.c_void_p(16)
+    assert lib.sgb_born_step(ctypes.byref(g), ctypes.byref(pml), p, p, p, p, p, p, p, p, None) == 5
+    assert lib.sgb_vti_step(ctypes.byref(g), ctypes.byref(pml), p, p, p, None) == 5
+    assert lib.sgb_vti_step(ctypes.byref(g), ctypes.byref(habc4), p, p, p, None) == 5  # 2nd order only
+    assert lib.sgb_rho_step(ctypes.byref(g), ctypes.byref(habc4), p, p, p, p, None) == 5
+    habc2 = N.AcousticModel(2, 1, 50, 0, ctypes.c_void_p(16), ctypes.c_void_p(16), ctypes.c_void_p(16))
+    assert lib.sgb_rho_step(ctypes.byref(g), ctypes.byref(habc2), None, p, p, p, None) == 1
+    assert lib.sgb_rho_step(ctypes.byref(g), ctypes.byref(habc2), ctypes.c_void_p(20), p, p, ctypes.c_void_p(32),
+                            None) == 3
+
+
+def test_born_loop_refuses_a_velocity_gradient():
+    from seistorch_gb300 import engine
+    vp = torch.ones(4, 4, requires_grad=True)
+    with pytest.raises(NotImplementedError):
+        engine.born_loop(vp, torch.zeros(4, 4), None, None, None)
