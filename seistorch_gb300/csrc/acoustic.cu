@@ -260,8 +260,11 @@ __global__ void __launch_bounds__(NTHREADS) acoustic_fwd_kernel(const AcStepArgs
         const float4 sb = *reinterpret_cast<const float4*>(a.born_in + base + po);
         y = make_float4(y.x + sb.x, y.y + sb.y, y.z + sb.z, y.w + sb.w);
       }
-      if (HABC) {
-#pragma unroll
+      // the blend only on strip cells; one copy of its code (not unrolled),
+      // so the row loop stays small in the instruction cache
+      const bool strip_lane = z < a.hw || z >= a.nz - a.hw || x < a.hw || x + 3 >= a.nx - a.hw;
+      if (HABC && strip_lane) {
+#pragma unroll 1
         for (int m = 0; m < 4; ++m)
           if (x + m < a.nx) set_comp(y, m, habc_point(T, a, z, x + m, comp(y, m)));
       }
