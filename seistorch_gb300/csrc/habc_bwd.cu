@@ -97,7 +97,16 @@ struct HabcBwdArgs {
   const int* __restrict__ rec_col;
   int nch;
   const float* __restrict__ resid;
+  // cells [tz0, tz1) x [tx0, tx1) (tx0, tx1 multiples of 4) are done by
+  // habc_bwd_interior_kernel; empty (tx1 = tx0) when that kernel is not used
+  int tz0, tz1, tx0, tx1;
 };
+
+// Is the group of four columns at x0 (a multiple of 4) in row z one of the
+// interior kernel's?  The two kernels split the cells with this predicate.
+__device__ __forceinline__ bool in_tiled(const HabcBwdArgs& a, int z, int x0) {
+  return z >= a.tz0 && z < a.tz1 && x0 >= a.tx0 && x0 + 4 <= a.tx1;
+}
 
 __device__ __forceinline__ float ldz(const float* p, int z, int x, int nz, int nx, int pitch) {
   return (z >= 0 && z < nz && x >= 0 && x < nx) ? __ldg(p + (long long)z * pitch + x) : 0.f;
@@ -168,16 +177,46 @@ __device__ __forceinline__ float oneway_t(const HabcBwdArgs& a, const float* l1,
   return acc;
 }
 
+// Cells of a shot outside the interior kernel's region, numbered rows
+// [0, tz0) in full, then rows [tz0, tz1) without columns [tx0, tx1), then
+// rows [tz1, nz) in full (all cells when the region is empty).
+struct FrameCells {
+  int nx, tz0, tz1, tx0, tx1, midw;
+  long long top, mid, plane;
+  __host__ __device__ FrameCells(const HabcBwdArgs& a)
+      : nx(a.nx), tz0(a.tz0), tz1(a.tz1), tx0(a.tx0), tx1(a.tx1), midw(a.tx0 + (a.nx - a.tx1)) {
+    top = (long long)tz0 * nx;
+    mid = (long long)(tz1 - tz0) * midw;
+    plane = top + mid + (long long)(a.nz - tz1) * nx;
+  }
+  __host__ __device__ void cell(long long r, int& z, int& x) const {
+    if (r < top) {
+      z = (int)(r / nx);
+      x = (int)(r % nx);
+    } else if (r < top + mid) {
+      const long long q = r - top;
+      const int c = (int)(q % midw);
+      z = tz0 + (int)(q / midw);
+      x = c < tx0 ? c : tx1 + (c - tx0);
+    } else {
+      const long long q = r - top - mid;
+      z = tz1 + (int)(q / nx);
+      x = (int)(q % nx);
+    }
+  }
+};
+
 template <int R>
 __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
-  const long long plane = (long long)a.nz * a.nx;
+  const FrameCells fc(a);
+  const long long plane = fc.plane;
   const long long total = plane * a.nshots;
   const bool mult = a.multiple != 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     const int b = (int)(i / plane);
-    const long long r = i - (long long)b * plane;
-    const int z = (int)(r / a.nx), x = (int)(r % a.nx);
+    int z, x;
+    fc.cell(i - (long long)b * plane, z, x);
     const long long fb = (long long)b * a.sstride;
     const long long o = (long long)z * a.pitch + x;
     const float* l1 = a.la1 + fb;
@@ -353,6 +392,102 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
   }
 }
 
+// Interior cells (at least hw + R from every strip side, inside the box;
+// plain equation: no VTI or density planes): the transpose
+// 2 La1 + L(k La1) - La2, the gradient term and the reconstruction, with
+// k La1 and U_{j-1} of an 8 x 128 tile plus its halo staged once in shared
+// memory.  Block (32, 8): warp w owns row z0 + w, lane l columns x0 + 4l.
+constexpr int HT_Z = 8, HT_X = 128, HT_H = 4;  // rows, columns, column halo (>= R)
+template <int R>
+__global__ void __launch_bounds__(256) habc_bwd_interior_kernel(const HabcBwdArgs a) {
+  constexpr int ROWS = HT_Z + 2 * R, W = HT_X + 2 * HT_H;
+  __shared__ __align__(16) float s_kl[ROWS][W];
+  __shared__ __align__(16) float s_u[ROWS][W];
+  const int b = blockIdx.z;
+  const int z0 = a.tz0 + blockIdx.y * HT_Z, x0 = a.tx0 + blockIdx.x * HT_X;
+  const long long fb = (long long)b * a.sstride;
+  const float* l1 = a.la1 + fb;
+  const float* u1 = a.ujm1 + fb;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  // stage: rows z0-R .. z0+HT_Z+R-1, columns x0-4 .. x0+131 (zeros off the grid)
+  for (int c = tid; c < ROWS * (W / 4); c += 256) {
+    const int rr = c / (W / 4), cc = c - rr * (W / 4);
+    const int z = z0 - R + rr, x = x0 - HT_H + 4 * cc;
+    float4 kl = make_float4(0.f, 0.f, 0.f, 0.f), uu = kl;
+    if (z >= 0 && z < a.nz && x >= 0 && x + 4 <= a.pitch) {
+      const long long o = (long long)z * a.pitch + x;
+      const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
+      const float4 l4 = *reinterpret_cast<const float4*>(l1 + o);
+      kl = make_float4(k4.x * l4.x, k4.y * l4.y, k4.z * l4.z, k4.w * l4.w);
+      uu = *reinterpret_cast<const float4*>(u1 + o);
+    }
+    *reinterpret_cast<float4*>(&s_kl[rr][4 * cc]) = kl;
+    *reinterpret_cast<float4*>(&s_u[rr][4 * cc]) = uu;
+  }
+  __syncthreads();
+  const int z = z0 + threadIdx.y, x = x0 + 4 * threadIdx.x;
+  if (!in_tiled(a, z, x)) return;
+  const int rr = R + threadIdx.y, cx = HT_H + 4 * threadIdx.x;
+  const long long o = (long long)z * a.pitch + x;
+  const float4 l2 = *reinterpret_cast<const float4*>(a.la2 + fb + o);
+  const float4 l1c = *reinterpret_cast<const float4*>(l1 + o);
+  const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
+  float v[4], L[4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    float lap = a.w.c[0] * s_kl[rr][cx + m];
+    float lu = a.w.c[0] * s_u[rr][cx + m];
+#pragma unroll
+    for (int j = 1; j <= R; ++j) {
+      lap += a.w.c[j] * (s_kl[rr - j][cx + m] + s_kl[rr + j][cx + m] + s_kl[rr][cx + m - j] + s_kl[rr][cx + m + j]);
+      lu += a.w.c[j] * (s_u[rr - j][cx + m] + s_u[rr + j][cx + m] + s_u[rr][cx + m - j] + s_u[rr][cx + m + j]);
+    }
+    v[m] = 2.f * comp(l1c, m) + lap - comp(l2, m);
+    L[m] = lu;
+  }
+  // residuals of the records of step j-1 in this row
+  if (a.resid != nullptr) {
+    const int* rp = a.rec_row_ptr + (long long)b * a.nz;
+    int lo = rp[z], hi = rp[z + 1];  // receivers of the row, sorted by column
+    const int end = hi;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (a.rec_x[mid] < x) lo = mid + 1; else hi = mid;
+    }
+    for (int q = lo; q < end && a.rec_x[q] < x + 4; ++q) {
+      const int dx = a.rec_x[q] - x;
+      const float rv = a.resid[(long long)a.rec_col[q] * a.nch];
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+        if (dx == m) v[m] += rv;
+    }
+  }
+  *reinterpret_cast<float4*>(a.lout + fb + o) = make_float4(v[0], v[1], v[2], v[3]);
+  float4* gp = reinterpret_cast<float4*>(a.grad + fb + o);
+  const float4 g0 = *gp;
+  *gp = make_float4(g0.x + v[0] * k4.x * L[0], g0.y + v[1] * k4.y * L[1], g0.z + v[2] * k4.z * L[2],
+                    g0.w + v[3] * k4.w * L[3]);
+  if (a.uout != nullptr) {
+    const float4 uj = *reinterpret_cast<const float4*>(a.uj + fb + o);
+    float ujv[4] = {uj.x, uj.y, uj.z, uj.w};
+    if (a.src_ptr != nullptr) {
+      for (int q = a.src_ptr[b]; q < a.src_ptr[b + 1]; ++q) {
+        const int dx = a.src_x[q] - x;
+        if (a.src_z[q] == z && dx >= 0 && dx < 4) {
+          const float wv = a.wavelet[(long long)a.src_wrow[q] * a.nt + a.t_src];
+#pragma unroll
+          for (int m = 0; m < 4; ++m)
+            if (dx == m) ujv[m] -= wv;
+        }
+      }
+    }
+    float uo[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + comp(k4, m) * L[m];
+    *reinterpret_cast<float4*>(a.uout + fb + o) = make_float4(uo[0], uo[1], uo[2], uo[3]);
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
@@ -400,7 +535,32 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
   a.rec_col = q.rec_col;
   a.nch = q.nch;
   a.resid = resid;
-  const long long total = (long long)g.nz * g.nx * g.nshots;
+  // interior region of the tiled kernel (plain equation only)
+  const int R = a.R, far = a.hw + R;
+  a.tz0 = a.multiple ? R : far;
+  a.tz1 = g.nz - far;
+  a.tx0 = (far + 3) / 4 * 4;
+  a.tx1 = (g.nx - far) / 4 * 4;
+  const bool tiled = kz == nullptr && rho_c == nullptr && R <= HT_H && a.tz1 > a.tz0 && a.tx1 > a.tx0 &&
+                     a.tz0 >= R && a.tz1 + R <= g.nz;
+  if (!tiled) a.tz0 = a.tz1 = a.tx0 = a.tx1 = 0;
+  if (tiled) {
+    // the box must cover the region (the gradient and the reconstruction
+    // are written there unconditionally)
+    if (a.tz0 < ring.iz0 || a.tz1 > ring.iz1 || a.tx0 < ring.ix0 || a.tx1 > ring.ix1) {
+      a.tz0 = a.tz1 = a.tx0 = a.tx1 = 0;
+    } else {
+      const dim3 grid((unsigned)((a.tx1 - a.tx0 + HT_X - 1) / HT_X), (unsigned)((a.tz1 - a.tz0 + HT_Z - 1) / HT_Z),
+                      (unsigned)g.nshots);
+      switch (R) {
+        case 1: habc_bwd_interior_kernel<1><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+        case 2: habc_bwd_interior_kernel<2><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+        case 3: habc_bwd_interior_kernel<3><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+        case 4: habc_bwd_interior_kernel<4><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+      }
+    }
+  }
+  const long long total = FrameCells(a).plane * g.nshots;
   long long blocks = (total + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
   switch (a.R) {
