@@ -393,15 +393,16 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
 }
 
 // Interior cells (at least hw + R from every strip side, inside the box;
-// plain equation: no VTI or density planes): the transpose
+// plain or VTI equation, not variable density): the transpose
 // 2 La1 + L(k La1) - La2, the gradient term and the reconstruction, with
 // k La1 and U_{j-1} of an 8 x 128 tile plus its halo staged once in shared
 // memory.  Block (32, 8): warp w owns row z0 + w, lane l columns x0 + 4l.
 constexpr int HT_Z = 8, HT_X = 128, HT_H = 4;  // rows, columns, column halo (>= R)
-template <int R>
+template <int R, bool VTI>
 __global__ void __launch_bounds__(256) habc_bwd_interior_kernel(const HabcBwdArgs a) {
   constexpr int ROWS = HT_Z + 2 * R, W = HT_X + 2 * HT_H;
-  __shared__ __align__(16) float s_kl[ROWS][W];
+  __shared__ __align__(16) float s_kl[ROWS][W];              // k La1 (VTI: kx La1)
+  __shared__ __align__(16) float s_kzl[VTI ? ROWS : 1][W];   // VTI: kz La1
   __shared__ __align__(16) float s_u[ROWS][W];
   const int b = blockIdx.z;
   const int z0 = a.tz0 + blockIdx.y * HT_Z, x0 = a.tx0 + blockIdx.x * HT_X;
@@ -413,15 +414,20 @@ __global__ void __launch_bounds__(256) habc_bwd_interior_kernel(const HabcBwdArg
   for (int c = tid; c < ROWS * (W / 4); c += 256) {
     const int rr = c / (W / 4), cc = c - rr * (W / 4);
     const int z = z0 - R + rr, x = x0 - HT_H + 4 * cc;
-    float4 kl = make_float4(0.f, 0.f, 0.f, 0.f), uu = kl;
+    float4 kl = make_float4(0.f, 0.f, 0.f, 0.f), uu = kl, kzl = kl;
     if (z >= 0 && z < a.nz && x >= 0 && x + 4 <= a.pitch) {
       const long long o = (long long)z * a.pitch + x;
       const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
       const float4 l4 = *reinterpret_cast<const float4*>(l1 + o);
       kl = make_float4(k4.x * l4.x, k4.y * l4.y, k4.z * l4.z, k4.w * l4.w);
+      if (VTI) {
+        const float4 q4 = __ldg(reinterpret_cast<const float4*>(a.kz + o));
+        kzl = make_float4(q4.x * l4.x, q4.y * l4.y, q4.z * l4.z, q4.w * l4.w);
+      }
       uu = *reinterpret_cast<const float4*>(u1 + o);
     }
     *reinterpret_cast<float4*>(&s_kl[rr][4 * cc]) = kl;
+    if (VTI) *reinterpret_cast<float4*>(&s_kzl[rr][4 * cc]) = kzl;
     *reinterpret_cast<float4*>(&s_u[rr][4 * cc]) = uu;
   }
   __syncthreads();
@@ -432,18 +438,35 @@ __global__ void __launch_bounds__(256) habc_bwd_interior_kernel(const HabcBwdArg
   const float4 l2 = *reinterpret_cast<const float4*>(a.la2 + fb + o);
   const float4 l1c = *reinterpret_cast<const float4*>(l1 + o);
   const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
-  float v[4], L[4];
+  float v[4], L[4], Lz[4];  // VTI: L = Lx(U), Lz = Lz(U)
+  const float ch = 0.5f * a.w.c[0];
 #pragma unroll
   for (int m = 0; m < 4; ++m) {
-    float lap = a.w.c[0] * s_kl[rr][cx + m];
-    float lu = a.w.c[0] * s_u[rr][cx + m];
+    if (VTI) {  // the per-cell VTI interior path, term by term
+      float lx = ch * s_kl[rr][cx + m], lz = ch * s_kzl[rr][cx + m];
+      float ux = ch * s_u[rr][cx + m], uz = ch * s_u[rr][cx + m];
 #pragma unroll
-    for (int j = 1; j <= R; ++j) {
-      lap += a.w.c[j] * (s_kl[rr - j][cx + m] + s_kl[rr + j][cx + m] + s_kl[rr][cx + m - j] + s_kl[rr][cx + m + j]);
-      lu += a.w.c[j] * (s_u[rr - j][cx + m] + s_u[rr + j][cx + m] + s_u[rr][cx + m - j] + s_u[rr][cx + m + j]);
+      for (int j = 1; j <= R; ++j) {
+        lx += a.w.c[j] * (s_kl[rr][cx + m - j] + s_kl[rr][cx + m + j]);
+        lz += a.w.c[j] * (s_kzl[rr - j][cx + m] + s_kzl[rr + j][cx + m]);
+        ux += a.w.c[j] * (s_u[rr][cx + m - j] + s_u[rr][cx + m + j]);
+        uz += a.w.c[j] * (s_u[rr - j][cx + m] + s_u[rr + j][cx + m]);
+      }
+      v[m] = 2.f * comp(l1c, m) + lx + lz - comp(l2, m);
+      L[m] = ux;
+      Lz[m] = uz;
+    } else {
+      float lap = a.w.c[0] * s_kl[rr][cx + m];
+      float lu = a.w.c[0] * s_u[rr][cx + m];
+#pragma unroll
+      for (int j = 1; j <= R; ++j) {
+        lap += a.w.c[j] * (s_kl[rr - j][cx + m] + s_kl[rr + j][cx + m] + s_kl[rr][cx + m - j] + s_kl[rr][cx + m + j]);
+        lu += a.w.c[j] * (s_u[rr - j][cx + m] + s_u[rr + j][cx + m] + s_u[rr][cx + m - j] + s_u[rr][cx + m + j]);
+      }
+      v[m] = 2.f * comp(l1c, m) + lap - comp(l2, m);
+      L[m] = lu;
+      Lz[m] = 0.f;
     }
-    v[m] = 2.f * comp(l1c, m) + lap - comp(l2, m);
-    L[m] = lu;
   }
   // residuals of the records of step j-1 in this row
   if (a.resid != nullptr) {
@@ -465,8 +488,17 @@ __global__ void __launch_bounds__(256) habc_bwd_interior_kernel(const HabcBwdArg
   *reinterpret_cast<float4*>(a.lout + fb + o) = make_float4(v[0], v[1], v[2], v[3]);
   float4* gp = reinterpret_cast<float4*>(a.grad + fb + o);
   const float4 g0 = *gp;
-  *gp = make_float4(g0.x + v[0] * k4.x * L[0], g0.y + v[1] * k4.y * L[1], g0.z + v[2] * k4.z * L[2],
-                    g0.w + v[3] * k4.w * L[3]);
+  float4 kz4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (VTI) {  // dJ/dkx += La Lx(U), dJ/dkz += La Lz(U)
+    *gp = make_float4(g0.x + v[0] * L[0], g0.y + v[1] * L[1], g0.z + v[2] * L[2], g0.w + v[3] * L[3]);
+    float4* gq = reinterpret_cast<float4*>(a.grad2 + fb + o);
+    const float4 h0 = *gq;
+    *gq = make_float4(h0.x + v[0] * Lz[0], h0.y + v[1] * Lz[1], h0.z + v[2] * Lz[2], h0.w + v[3] * Lz[3]);
+    kz4 = __ldg(reinterpret_cast<const float4*>(a.kz + o));
+  } else {
+    *gp = make_float4(g0.x + v[0] * k4.x * L[0], g0.y + v[1] * k4.y * L[1], g0.z + v[2] * k4.z * L[2],
+                      g0.w + v[3] * k4.w * L[3]);
+  }
   if (a.uout != nullptr) {
     const float4 uj = *reinterpret_cast<const float4*>(a.uj + fb + o);
     float ujv[4] = {uj.x, uj.y, uj.z, uj.w};
@@ -483,7 +515,8 @@ __global__ void __launch_bounds__(256) habc_bwd_interior_kernel(const HabcBwdArg
     }
     float uo[4];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + comp(k4, m) * L[m];
+    for (int m = 0; m < 4; ++m)
+      uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + (VTI ? comp(k4, m) * L[m] + comp(kz4, m) * Lz[m] : comp(k4, m) * L[m]);
     *reinterpret_cast<float4*>(a.uout + fb + o) = make_float4(uo[0], uo[1], uo[2], uo[3]);
   }
 }
@@ -541,8 +574,9 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
   a.tz1 = g.nz - far;
   a.tx0 = (far + 3) / 4 * 4;
   a.tx1 = (g.nx - far) / 4 * 4;
-  const bool tiled = kz == nullptr && rho_c == nullptr && R <= HT_H && a.tz1 > a.tz0 && a.tx1 > a.tx0 &&
-                     a.tz0 >= R && a.tz1 + R <= g.nz;
+  const bool vti = kz != nullptr;
+  const bool tiled = rho_c == nullptr && R <= HT_H && a.tz1 > a.tz0 && a.tx1 > a.tx0 && a.tz0 >= R &&
+                     a.tz1 + R <= g.nz;
   if (!tiled) a.tz0 = a.tz1 = a.tx0 = a.tx1 = 0;
   if (tiled) {
     // the box must cover the region (the gradient and the reconstruction
@@ -552,11 +586,15 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
     } else {
       const dim3 grid((unsigned)((a.tx1 - a.tx0 + HT_X - 1) / HT_X), (unsigned)((a.tz1 - a.tz0 + HT_Z - 1) / HT_Z),
                       (unsigned)g.nshots);
-      switch (R) {
-        case 1: habc_bwd_interior_kernel<1><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-        case 2: habc_bwd_interior_kernel<2><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-        case 3: habc_bwd_interior_kernel<3><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-        case 4: habc_bwd_interior_kernel<4><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+      switch (R * 2 + (vti ? 1 : 0)) {
+        case 2: habc_bwd_interior_kernel<1, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+        case 3: habc_bwd_interior_kernel<1, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+        case 4: habc_bwd_interior_kernel<2, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+        case 5: habc_bwd_interior_kernel<2, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+        case 6: habc_bwd_interior_kernel<3, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+        case 7: habc_bwd_interior_kernel<3, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+        case 8: habc_bwd_interior_kernel<4, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+        case 9: habc_bwd_interior_kernel<4, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
       }
     }
   }
