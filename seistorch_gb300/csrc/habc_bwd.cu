@@ -206,7 +206,9 @@ struct FrameCells {
   }
 };
 
-template <int R>
+// EQ: 0 plain (acoustic_habc, Born), 1 VTI, 2 variable density -- one
+// instantiation per equation, so each carries only its own branches.
+template <int R, int EQ>
 __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
   const FrameCells fc(a);
   const long long plane = fc.plane;
@@ -229,8 +231,8 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
     const int far = a.hw + R;
     const bool interior =
         z >= (mult ? R : far) && a.nz - 1 - z >= far && x >= far && a.nx - 1 - x >= far;
-    const bool vti = a.kz != nullptr;
-    const bool rho = R == 1 && a.rho_c != nullptr;
+    constexpr bool vti = EQ == 1;
+    constexpr bool rho = EQ == 2 && R == 1;
     const float kzq = vti ? __ldg(a.kz + o) : 0.f;
     const float ch = 0.5f * a.w.c[0];  // centre of the 1-D second difference
     const long long pl = (long long)a.nz * a.pitch;
@@ -601,11 +603,18 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
   const long long total = FrameCells(a).plane * g.nshots;
   long long blocks = (total + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  switch (a.R) {
-    case 1: habc_bwd_kernel<1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 2: habc_bwd_kernel<2><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 3: habc_bwd_kernel<3><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 4: habc_bwd_kernel<4><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+  const int eq = rho_c != nullptr ? 2 : (kz != nullptr ? 1 : 0);
+  if (eq == 2 && a.R != 1) return cudaErrorInvalidValue;  // variable density: 2nd order only
+  switch (a.R * 3 + eq) {
+    case 3: habc_bwd_kernel<1, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 4: habc_bwd_kernel<1, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 5: habc_bwd_kernel<1, 2><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 6: habc_bwd_kernel<2, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 7: habc_bwd_kernel<2, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 9: habc_bwd_kernel<3, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 10: habc_bwd_kernel<3, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 12: habc_bwd_kernel<4, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 13: habc_bwd_kernel<4, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
