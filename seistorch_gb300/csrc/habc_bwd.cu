@@ -20,6 +20,15 @@
 // the PML adjoint (U_{j-2} = 2 U_{j-1} - (U_j - S w) + k L(U_{j-1})) and
 // dJ/dvp += La_j (2k / vp) L(U_{j-1}) there; the ring of order/2 cells
 // around the box comes from the forward's store.
+//
+// Two kernels share each reverse step: habc_bwd_interior_kernel takes the
+// cells at least hw + R from every strip side (there wi = 1 for the whole
+// stencil and no one-way line reaches), with k La1 and U_{j-1} tiles staged
+// in shared memory; habc_bwd_kernel takes the remaining frame of cells one
+// by one.  The same equations carry the VTI (k Lx + kz Lz, vti_habc2.py),
+// variable-density (C D(U), acoustic_rho_habc.py) and Born (the scattered
+// field's adjoint against the background's reconstruction,
+// acoustic_lsrtm_habc.py) gradients.
 #include "sgb_common.cuh"
 #include "acoustic_args.cuh"
 
