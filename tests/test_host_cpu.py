@@ -290,3 +290,21 @@ def test_born_loop_refuses_a_velocity_gradient():
     vp = torch.ones(4, 4, requires_grad=True)
     with pytest.raises(NotImplementedError):
         engine.born_loop(vp, torch.zeros(4, 4), None, None, None)
+
+
+def test_every_registered_equation_has_the_reference_entry_points():
+    """build_model loads seistorch_gb300.equations2d.<equation> and needs its
+    _time_step / _time_step_backward(_multiple) (model.py:64-80); the
+    registry's parameter and wavefield lists name the same equations."""
+    import importlib
+    from seistorch_gb300.eqconfigure import Parameters, Wavefield
+    paras = Parameters.valid_model_paras()
+    for eq in paras:
+        mod = importlib.import_module(f"seistorch_gb300.equations2d.{eq}")
+        for fn in ("_time_step", "_time_step_backward", "_time_step_backward_multiple"):
+            assert callable(getattr(mod, fn, None)), (eq, fn)
+        assert Wavefield(eq).wavefields, eq
+    for eq in Parameters.secondorder_equations():
+        assert eq in paras and len(Wavefield(eq).wavefields) in (2, 4), eq
+    assert paras["acoustic_lsrtm_habc"] == ["vp", "m"]
+    assert Wavefield("vti_habc2").wavefields == ["p1", "p2"]
