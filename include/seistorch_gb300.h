@@ -32,8 +32,9 @@ typedef enum {
   SGB_ERR_UNSUPPORTED = 5, /* order / option outside what the kernels cover   */
   SGB_ERR_NONFINITE = 6,   /* NaN/Inf found in records (rnn.py:215 -> type.py:41-46) */
   SGB_ERR_CAPACITY = 7,    /* too many sources inside one tile                */
-  SGB_ERR_SCRATCH = 8      /* problem larger than the fixed scratch of an
+  SGB_ERR_SCRATCH = 8,     /* problem larger than the fixed scratch of an
                               allocation-free entry point                    */
+  SGB_ERR_CFL = 9          /* vmax * dt / h above the scheme's stability limit */
 } sgb_status;
 
 /* Grid shared by every equation. dt, h in seconds / metres. */
@@ -79,7 +80,9 @@ typedef struct {
 typedef struct {
   int32_t order;        /* 2, 4, 6 or 8                                       */
   int32_t boundary;     /* 0 = PML, 1 = HABC                                   */
-  int32_t habc_width;   /* 50 (acoustic_habc.py:79, habc.py)                  */
+  int32_t habc_width;   /* 50 (acoustic_habc.py:79, habc.py); HABC with 0: no
+                           blend -- the plain undamped update of the reverse
+                           steps (acoustic_habc.py:223-268)                   */
   int32_t multiple;     /* free surface at the top (no top absorbing layer)    */
   const float *coef;    /* [2][nz][pitch]                                      */
   const float *vp;      /* [nz][pitch] (HABC one-way coefficients)            */
@@ -105,8 +108,28 @@ const char *sgb_status_string(int status);
 int sgb_last_cuda_error(void);
 
 /* Reads (and with reset != 0 clears) the device status word that kernels set
- * on capacity faults (bit 1: too many sources in one tile).  Synchronous. */
+ * (bit 1: too many sources in one tile; bit 2: an mbarrier wait ran out of
+ * polls and the kernel stopped early).  Synchronous. */
 int sgb_device_status(int *out, int reset);
+
+/* Stability check of the explicit time stepping (host-only, no GPU work).
+ * The reference has no such check (a too-large dt shows up as NaN records,
+ * type.py:41-46); here the Python layer calls it before every loop.
+ * scheme 0: 2nd-order-in-time acoustic family with the cross stencil of
+ * `order` (2/4/6/8; acoustic.py:60-86) -- vmax * dt / h <= 2 / sqrt(max
+ * eigenvalue of -h^2 L) (0.707, 0.612, 0.575, 0.555 for orders 2/4/6/8);
+ * scheme 1: the elastic velocity-stress staggered grid (elastic.py:7-37,
+ * order 2) -- vmax * dt / h <= 1/sqrt(2).  Writes the Courant number and
+ * the limit (either pointer may be NULL); returns SGB_ERR_CFL above it. */
+int sgb_cfl_check(int32_t scheme, int32_t order, float vmax, float dt, float h, float *courant_out,
+                  float *limit_out);
+
+/* Diagnostic of the bounded waits (no counterpart in the reference): one
+ * block waits on an mbarrier for at most `polls` polls (1 .. 2^21).  With
+ * arrive = 0 nothing completes the barrier, the wait runs out, sets bit 2 of
+ * the device status word and the kernel returns; with arrive != 0 the wait
+ * succeeds and sets nothing.  No copy is ever in flight. */
+int sgb_debug_wait_probe(uint32_t polls, int32_t arrive, sgb_stream_t stream);
 
 /* Select the tile-pipeline variant used by later PML calls (host-only,
  * process-wide): fwd_cfg in [0, 6) and bwd_cfg in [0, 4) index the compiled
@@ -137,6 +160,42 @@ int sgb_acoustic_step(const sgb_grid *grid, const sgb_acoustic_model *model, con
 int sgb_acoustic_step_vjp(const sgb_grid *grid, const sgb_acoustic_model *model, const float *u,
                           const float *gy, const float *gh1, float *gu, float *gum,
                           float *gvp_acc, sgb_stream_t stream);
+
+/* Inputs and outputs of sgb_habc_step_vjp.  Fields [nshots][nz][pitch],
+ * planes [nz][pitch]; outputs are overwritten. */
+typedef struct {
+  const float *u;      /* U_n (h1 / p1)                                           */
+  const float *um;     /* U_{n-1} (h2 / p2)                                       */
+  const float *gy;     /* dJ/dy of the step's output                              */
+  float *gu;           /* out dJ/dU_n                                             */
+  float *gum;          /* out dJ/dU_{n-1}                                         */
+  float *gparam;       /* out sum over shots of wi * gy * dI/dtheta, I the interior
+                          update: 1 plane (L(U)) for the plain equation and Born,
+                          2 for VTI (Lx(U), Lz(U)), 5 for variable density
+                          (D(U), C dx+U, -C dx-U, C dz+U, -C dz-U)                */
+  float *gvp_oneway;   /* out sum over shots of gy * d(one-way blend)/dvp, or NULL
+                          (unused when model->habc_width == 0)                    */
+  const float *kz;     /* VTI: the z coefficient plane (coef = [g][kx][kz]), else NULL */
+  const float *rho_c;  /* variable density: planes C, bx+, bx-, bz+, bz-, else NULL  */
+  const float *born_m; /* Born, scattered field: reflectivity m, else NULL        */
+  const float *born_u; /* Born: the background field U_n of the m k L(U) source   */
+  float *born_gu;      /* Born: out dJ/d(background U_n) through the source       */
+  float *born_gm;      /* Born: out dJ/dm (plane)                                 */
+} sgb_habc_vjp_io;
+
+/* Vector-Jacobian product of one step of the HABC family (autograd of
+ * acoustic_habc._time_step, acoustic_habc.py:206-221; vti_habc2._time_step,
+ * vti_habc2.py:25-60; acoustic_rho_habc._time_step, acoustic_rho_habc.py:31-58;
+ * one field of acoustic_lsrtm_habc._time_step, acoustic_lsrtm_habc.py:11-30):
+ * the transposed interior update weighted by each cell's interior share, the
+ * transposed one-way blends of the four strips (mask precedence, corner
+ * halves, the depth-49 roll wrap), over the whole grid.  model->boundary must
+ * be 1; habc_width 0 gives the VJP of the unblended reverse step
+ * (acoustic_habc.py:223-268).  The caller maps gparam through the
+ * coefficient map (k = vp^2 dt^2 / h^2: dJ/dvp += gparam * 2k / vp) and adds
+ * gvp_oneway to dJ/dvp. */
+int sgb_habc_step_vjp(const sgb_grid *grid, const sgb_acoustic_model *model, const sgb_habc_vjp_io *io,
+                      sgb_stream_t stream);
 
 /* Whole time loop (rnn.py:178-205) in one call: nt steps of the model with
  * source injection and receiver sampling fused into the step kernel.
@@ -179,7 +238,9 @@ int sgb_acoustic_backward(const sgb_grid *grid, const sgb_acoustic_model *model,
  * 4 * nshots * nz * pitch must not exceed 8,388,608 floats; larger problems
  * return SGB_ERR_SCRATCH before any work.  The first call on a device looks
  * up the array's address there (cudaGetSymbolAddress with that device
- * current); make that first call before any stream capture.  All calls share
+ * current); make that first call before any stream capture.  The address
+ * is cached per device for the life of the process: after cudaDeviceReset
+ * on a device, do not call this entry point on that device again.  All calls share
  * the one array, which keeps the last call's contents (the adjoint clears what
  * must start at zero), so calls that overlap on the GPU -- on different
  * streams or threads -- race and must be serialised by the caller.  No

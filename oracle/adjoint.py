@@ -19,7 +19,7 @@ def _inject(fields, b, zs, xs, vals):
 
 
 def acoustic_pml_gradient(vp, d, dt, h, wavelet, sources, receivers, record_grads, order=2,
-                          dtype=np.float64):
+                          dtype=np.float64, keep_every=None):
     """dJ/dvp for the 2nd-order acoustic PML loop (acoustic.py:73-86).
 
     Forward: U_{i+1} = A U_i - Bc U_{i-1} + Kv Lh(U_i) + S w_i with
@@ -28,6 +28,10 @@ def acoustic_pml_gradient(vp, d, dt, h, wavelet, sources, receivers, record_grad
     Adjoint (Lh is self-adjoint, zero padded):
       lam_k = R^T g_{k-1} + A lam_{k+1} + Lh(Kv lam_{k+1}) - Bc lam_{k+2}
     Gradient: dJ/dvp = sum_i lam_{i+1} * 2 vp inv * Lh(U_i).
+    Every forward state is kept by default; with ``keep_every = S`` only
+    the pairs (U_{a-1}, U_a) at a = 0, S, 2S, ... are kept and each segment
+    is recomputed in the reverse sweep (the same float64 arithmetic, so the
+    result is identical), which bounds memory for long runs.
     """
     vp = np.asarray(vp, dtype)
     d = np.asarray(d, dtype)
@@ -43,12 +47,39 @@ def acoustic_pml_gradient(vp, d, dt, h, wavelet, sources, receivers, record_grad
     for b, pts in enumerate(sources):
         for (z, x) in pts:
             smask[b, z, x] = 1
-    U = [np.zeros((B, nz, nx), dtype), np.zeros((B, nz, nx), dtype)]  # U_{-1}, U_0
-    for i in range(nt):
-        un = U[-1]
-        y = A * un - Bc * U[-2] + Kv * fd2d.laplacian(un, order, h, dtype)
-        U.append(y + smask * dtype(np.float32(wavelet[i])))
-    # U[k+1] holds U_k for k = -1..nt
+
+    def step(um1, u0, i):
+        y = A * u0 - Bc * um1 + Kv * fd2d.laplacian(u0, order, h, dtype)
+        return y + smask * dtype(np.float32(wavelet[i]))
+
+    zero = np.zeros((B, nz, nx), dtype)
+    if keep_every is None:
+        U = [zero, zero]  # U_{-1}, U_0
+        for i in range(nt):
+            U.append(step(U[-2], U[-1], i))
+
+        def states_reversed():  # U_{nt-1}, ..., U_0
+            for m in range(nt - 1, -1, -1):
+                yield U[m + 1]
+    else:
+        S = int(keep_every)
+        ck = {}
+        prev, cur = zero, zero
+        for i in range(nt):
+            if i % S == 0:
+                ck[i] = (prev, cur)  # (U_{i-1}, U_i)
+            prev, cur = cur, step(prev, cur, i)
+
+        def states_reversed():
+            for a in sorted(ck, reverse=True):
+                um1, u0 = ck[a]
+                seg = [u0]
+                for i in range(a, min(a + S, nt) - 1):
+                    um1, u0 = u0, step(um1, u0, i)
+                    seg.append(u0)
+                yield from reversed(seg)
+
+    states = states_reversed()
     grad = np.zeros((nz, nx), dtype)
     lam1 = np.zeros((B, nz, nx), dtype)   # lam_{k+1}
     lam2 = np.zeros((B, nz, nx), dtype)   # lam_{k+2}
@@ -57,7 +88,7 @@ def acoustic_pml_gradient(vp, d, dt, h, wavelet, sources, receivers, record_grad
         for b, (zs, xs) in enumerate(receivers):
             _inject(lam, b, zs, xs, np.asarray(record_grads[b][k - 1][:, 0], dtype))
         # term i = k-1: lam_k * dU_k/dvp = lam_k * 2 vp inv Lh(U_{k-1})
-        grad += np.sum(lam * fd2d.laplacian(U[k], order, h, dtype), axis=0)
+        grad += np.sum(lam * fd2d.laplacian(next(states), order, h, dtype), axis=0)
         lam2, lam1 = lam1, lam
     return grad * dtype(2.0) * vp * inv
 

@@ -91,6 +91,12 @@ class AcousticModel(ctypes.Structure):
                 ("coef", c_ptr), ("vp", c_ptr), ("damp", c_ptr)]
 
 
+class HabcVjpIO(ctypes.Structure):
+    _fields_ = [("u", c_ptr), ("um", c_ptr), ("gy", c_ptr), ("gu", c_ptr), ("gum", c_ptr), ("gparam", c_ptr),
+                ("gvp_oneway", c_ptr), ("kz", c_ptr), ("rho_c", c_ptr), ("born_m", c_ptr), ("born_u", c_ptr),
+                ("born_gu", c_ptr), ("born_gm", c_ptr)]
+
+
 class BsStore(ctypes.Structure):
     _fields_ = [("iz0", c_i32), ("iz1", c_i32), ("ix0", c_i32), ("ix1", c_i32), ("ring", c_i32),
                 ("ring_size", c_i32), ("ring_store", c_ptr), ("ckpt_every", c_i32),
@@ -141,6 +147,8 @@ SIGNATURES = {
                                          c_ptr, c_ptr]),
     "sgb_acoustic_step_vjp": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel), c_ptr,
                                              c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr]),
+    "sgb_habc_step_vjp": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel),
+                                         ctypes.POINTER(HabcVjpIO), c_ptr]),
     "sgb_acoustic_forward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel),
                                             ctypes.POINTER(Acquisition), PTR3, c_ptr, ctypes.POINTER(BsStore),
                                             ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_ptr]),
@@ -199,6 +207,9 @@ SIGNATURES = {
     "sgb_nn_adam": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_f32, c_f32, c_f32, c_f32, c_i32,
                                    c_f32, c_ptr]),
     "sgb_nn_mse": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr]),
+    "sgb_cfl_check": (ctypes.c_int, [c_i32, c_i32, c_f32, c_f32, c_f32, ctypes.POINTER(c_f32),
+                                     ctypes.POINTER(c_f32)]),
+    "sgb_debug_wait_probe": (ctypes.c_int, [ctypes.c_uint32, c_i32, c_ptr]),
     "sgb_l2_misfit": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr]),
     "sgb_grad_precondition": (ctypes.c_int, [c_i32, c_i32, c_i32, c_ptr, c_ptr, c_f32, c_ptr, c_ptr, c_ptr]),
     "sgb_grad_smooth": (ctypes.c_int, [c_i32, c_i32, c_i32, c_ptr, c_i32, c_ptr, c_i32, c_i32, c_ptr, c_ptr,
@@ -267,6 +278,26 @@ def call(name, *args):
     if fn is None:
         raise NativeError(f"{LIB_NAME} does not export {name}")
     check(fn(*args), name)
+
+
+SCHEME_ACOUSTIC = 0   # 2nd-order-in-time cross-stencil family (acoustic, HABC, Born, VTI, density)
+SCHEME_ELASTIC = 1    # velocity-stress staggered grid
+
+
+def cfl_check(scheme, order, vmax, dt, h):
+    """Courant number vmax*dt/h against the scheme's stability limit (host
+    only).  Returns (courant, limit); raises NativeError (CFL) above it."""
+    lib = load()
+    c = c_f32(0.0)
+    lim = c_f32(0.0)
+    st = lib.sgb_cfl_check(int(scheme), int(order), float(vmax), float(dt), float(h), ctypes.byref(c),
+                           ctypes.byref(lim))
+    if st == 9:
+        raise NativeError(f"CFL condition violated: vmax*dt/h = {c.value:.4f} exceeds the limit {lim.value:.4f} "
+                          f"of the order-{order} {'elastic' if scheme == SCHEME_ELASTIC else 'acoustic'} scheme "
+                          f"(vmax {vmax:.1f} m/s, dt {dt:g} s, h {h:g} m)")
+    check(st, "sgb_cfl_check")
+    return c.value, lim.value
 
 
 def device_status(reset=True):

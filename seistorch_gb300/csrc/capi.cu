@@ -79,6 +79,8 @@ int fwd_tile_shots();
 int bwd_tile_rows();
 int stencil_box_width(int R);
 int set_stream_config(int fwd, int bwd, int zc);
+cudaError_t launch_habc_step_vjp(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_habc_vjp_io& io,
+                                 cudaStream_t s);
 cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
                             const Ring& ring, const float* la1, const float* la2, float* lout, const float* uj,
                             const float* ujm1, float* uout, float* grad, const float* ring_in, int t_src,
@@ -93,6 +95,36 @@ using namespace sgb;
 
 namespace {
 
+// The bounded-wait path of every pipelined kernel, on its own: thread 0
+// initialises an mbarrier that expects one arrival, arrives on it only when
+// `arrive` is set, and then waits for its first phase for at most `polls`
+// polls.  Without the arrival nothing ever completes the phase, so the wait
+// runs out, sets DEV_ERR_TIMEOUT in the status word and the kernel returns
+// normally.  No copy is in flight at any time.
+__global__ void wait_probe_kernel(int* status, uint32_t polls, int arrive) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    if (arrive) mbar_arrive(&bar);
+    mbar_wait_n(&bar, 0, status, polls);
+  }
+}
+
+// Largest eigenvalue of -L for the order's cross stencil (per h^2): twice the
+// maximum over the 1-D wavenumber of 2 sum_j c_j (1 - cos(j theta)).
+double stencil_symbol_max_2d(int order) {
+  const FdWeights w = fd_weights(order);
+  double best = 0.0;
+  for (int i = 0; i <= 4096; ++i) {
+    const double th = M_PI * i / 4096.0;
+    double s = 0.0;
+    for (int j = 1; j <= 4; ++j) s += 2.0 * w.c[j] * (1.0 - std::cos(j * th));
+    if (s > best) best = s;
+  }
+  return 2.0 * best;
+}
+
 
 int check_model(const sgb_grid* g, const sgb_acoustic_model* m) {
   if (m == nullptr || m->coef == nullptr) return SGB_ERR_ARG;
@@ -101,8 +133,9 @@ int check_model(const sgb_grid* g, const sgb_acoustic_model* m) {
   if (!aligned16(m->coef)) return SGB_ERR_ALIGN;
   if (m->boundary == 1) {
     if (m->vp == nullptr || m->damp == nullptr) return SGB_ERR_ARG;
-    // the one-way extrapolation reads two cells inward of each 50-cell strip
-    if (m->habc_width <= 0 || m->habc_width + 2 > g->nx || m->habc_width + 2 > g->nz) return SGB_ERR_SHAPE;
+    // the one-way extrapolation reads two cells inward of each 50-cell strip;
+    // width 0 is the unblended update of the reverse steps
+    if (m->habc_width < 0 || m->habc_width + 2 > g->nx || m->habc_width + 2 > g->nz) return SGB_ERR_SHAPE;
   }
   return SGB_OK;
 }
@@ -154,11 +187,44 @@ const char* sgb_status_string(int s) {
     case SGB_ERR_NONFINITE: return "non-finite values in the records";
     case SGB_ERR_CAPACITY: return "too many sources inside one tile";
     case SGB_ERR_SCRATCH: return "problem larger than the fixed scratch of the allocation-free entry point";
+    case SGB_ERR_CFL: return "CFL condition violated: max velocity * dt / h exceeds the scheme's stability limit";
   }
   return "unknown status";
 }
 
 int sgb_last_cuda_error(void) { return g_last_cuda_error; }
+
+int sgb_cfl_check(int32_t scheme, int32_t order, float vmax, float dt, float h, float* courant_out,
+                  float* limit_out) {
+  if (!(dt > 0.f) || !(h > 0.f) || !(vmax >= 0.f) || !std::isfinite(vmax) || !std::isfinite(dt) ||
+      !std::isfinite(h))
+    return SGB_ERR_ARG;
+  double limit;
+  if (scheme == 0) {
+    // u+ = 2u - u- + C^2 h^2 L(u) (leapfrog): stable while C^2 * max eig(-h^2 L) <= 4
+    if (order != 2 && order != 4 && order != 6 && order != 8) return SGB_ERR_UNSUPPORTED;
+    limit = 2.0 / std::sqrt(stencil_symbol_max_2d(order));
+  } else if (scheme == 1) {
+    // 2nd-order velocity-stress staggered grid: vp dt / h <= 1 / sqrt(2)
+    if (order != 2) return SGB_ERR_UNSUPPORTED;
+    limit = 1.0 / std::sqrt(2.0);
+  } else {
+    return SGB_ERR_ARG;
+  }
+  const double courant = (double)vmax * dt / h;
+  if (courant_out != nullptr) *courant_out = (float)courant;
+  if (limit_out != nullptr) *limit_out = (float)limit;
+  return courant > limit ? SGB_ERR_CFL : SGB_OK;
+}
+
+int sgb_debug_wait_probe(uint32_t polls, int32_t arrive, sgb_stream_t stream) {
+  int* st = status_ptr();
+  if (st == nullptr) return SGB_ERR_CUDA;
+  if (polls < 1 || polls > MBAR_SPIN_LIMIT) return SGB_ERR_ARG;
+  wait_probe_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(st, polls, arrive != 0);
+  SGB_CUDA_CHECK(cudaGetLastError());
+  return SGB_OK;
+}
 
 int sgb_device_status(int* out, int reset) {
   int* p = status_ptr();
@@ -228,6 +294,27 @@ int sgb_acoustic_step_vjp(const sgb_grid* grid, const sgb_acoustic_model* model,
   a.vp = model->vp;
   a.w = fd_weights(model->order);
   SGB_CUDA_CHECK(launch_acoustic_vjp(model->order / 2, a, (cudaStream_t)stream));
+  return SGB_OK;
+}
+
+int sgb_habc_step_vjp(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_habc_vjp_io* io,
+                      sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (int e = check_model(grid, model)) return e;
+  if (io == nullptr) return SGB_ERR_ARG;
+  if (model->boundary != 1) return SGB_ERR_UNSUPPORTED;  // PML: sgb_acoustic_step_vjp
+  if (io->kz != nullptr && io->rho_c != nullptr) return SGB_ERR_ARG;
+  if ((io->kz != nullptr || io->rho_c != nullptr) && (model->order != 2 || io->born_m != nullptr))
+    return SGB_ERR_UNSUPPORTED;
+  const float* need[6] = {io->u, io->um, io->gy, io->gu, io->gum, io->gparam};
+  for (const float* q : need) {
+    if (q == nullptr) return SGB_ERR_ARG;
+    if (!aligned16(q)) return SGB_ERR_ALIGN;
+  }
+  if (io->born_m != nullptr && (io->born_u == nullptr || io->born_gu == nullptr || io->born_gm == nullptr))
+    return SGB_ERR_ARG;
+  if (io->gu == io->gy || io->gum == io->gy || io->gu == io->gum) return SGB_ERR_ARG;
+  SGB_CUDA_CHECK(launch_habc_step_vjp(*grid, *model, *io, (cudaStream_t)stream));
   return SGB_OK;
 }
 

@@ -123,9 +123,12 @@ __device__ __forceinline__ float ldz(const float* p, int z, int x, int nz, int n
 
 // One-way transpose of side s at cell q = (z, x): contributions of the
 // strip cells p = q, q - d, q - 2d (and the wrap to the line's edge cell).
-// depth(q) along s is dq; (sz, sx) is the inward step d.
-__device__ __forceinline__ float oneway_t(const HabcBwdArgs& a, const float* l1, const float* l2, int z, int x,
-                                          int dq, int sz, int sx, int side) {
+// depth(q) along s is dq; (sz, sx) is the inward step d.  USE1 / USE2 select
+// the transposes of the U_n terms (applied to l1) and of the U_{n-1} terms
+// (applied to l2).
+template <bool USE1, bool USE2, class Args>
+__device__ __forceinline__ float oneway_t(const Args& a, const float* l1, const float* l2, int z, int x, int dq,
+                                          int sz, int sx, int side) {
   const int hw = a.hw;
   if (dq > hw) return 0.f;
   const bool mult = a.multiple != 0;
@@ -147,7 +150,8 @@ __device__ __forceinline__ float oneway_t(const HabcBwdArgs& a, const float* l1,
       float lam, mu;
       coefs(z, x, lam, mu);
       const long long o = (long long)z * a.pitch + x;
-      acc += ws * ((2.f - lam - mu) * l1[o] + (lam - 1.f) * l2[o]);
+      if (USE1) acc += ws * (2.f - lam - mu) * l1[o];
+      if (USE2) acc += ws * (lam - 1.f) * l2[o];
     }
   }
   // p = q - d (depth dq - 1): U[p + d] and P[p + d] terms
@@ -158,9 +162,11 @@ __device__ __forceinline__ float oneway_t(const HabcBwdArgs& a, const float* l1,
       float lam, mu;
       coefs(pz, px, lam, mu);
       const long long o = (long long)pz * a.pitch + px;
-      acc += ws * ((lam + 2.f * mu) * l1[o] - lam * l2[o]);
+      if (USE1) acc += ws * (lam + 2.f * mu) * l1[o];
+      if (USE2) acc -= ws * lam * l2[o];
     }
   }
+  if (!USE1) return acc;
   // p = q - 2d (depth dq - 2, whose p2 is q when dq - 2 + 2 <= hw)
   if (dq >= 2 && dq <= hw) {
     const int pz = z - 2 * sz, px = x - 2 * sx;
@@ -263,10 +269,10 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
       v = 2.f * wq * l1[o] + (own + cw(z, x - 1, 1) + cw(z, x + 1, 2) + cw(z - 1, x, 3) + cw(z + 1, x, 4)) -
           wq * l2[o];
       if (!interior) {
-        v += oneway_t(a, l1, l2, z, x, z, 1, 0, 0);
-        v += oneway_t(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
-        v += oneway_t(a, l1, l2, z, x, x, 0, 1, 2);
-        v += oneway_t(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
+        v += oneway_t<true, true>(a, l1, l2, z, x, z, 1, 0, 0);
+        v += oneway_t<true, true>(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
+        v += oneway_t<true, true>(a, l1, l2, z, x, x, 0, 1, 2);
+        v += oneway_t<true, true>(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
       }
     } else if (interior && vti) {
       float lx = ch * kq * l1[o], lz = ch * kzq * l1[o];
@@ -297,10 +303,10 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
       for (int j = 1; j <= R; ++j)
         lap += a.w.c[j] * (wl(z, x - j, a.k) + wl(z, x + j, a.k) + wl(z - j, x, a.kz) + wl(z + j, x, a.kz));
       v = 2.f * wq.wi * l1[o] + lap - wq.wi * l2[o];
-      v += oneway_t(a, l1, l2, z, x, z, 1, 0, 0);
-      v += oneway_t(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
-      v += oneway_t(a, l1, l2, z, x, x, 0, 1, 2);
-      v += oneway_t(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
+      v += oneway_t<true, true>(a, l1, l2, z, x, z, 1, 0, 0);
+      v += oneway_t<true, true>(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
+      v += oneway_t<true, true>(a, l1, l2, z, x, x, 0, 1, 2);
+      v += oneway_t<true, true>(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
     } else {
       // interior part: 2 wi La1 + L(k wi La1) - wi La2
       auto kwl = [&](int zz, int xx) -> float {
@@ -315,10 +321,10 @@ __global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
         lap += a.w.c[j] * (kwl(z - j, x) + kwl(z + j, x) + kwl(z, x - j) + kwl(z, x + j));
       v = 2.f * wq.wi * l1[o] + lap - wq.wi * l2[o];
       // one-way parts of the four sides
-      v += oneway_t(a, l1, l2, z, x, z, 1, 0, 0);
-      v += oneway_t(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
-      v += oneway_t(a, l1, l2, z, x, x, 0, 1, 2);
-      v += oneway_t(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
+      v += oneway_t<true, true>(a, l1, l2, z, x, z, 1, 0, 0);
+      v += oneway_t<true, true>(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
+      v += oneway_t<true, true>(a, l1, l2, z, x, x, 0, 1, 2);
+      v += oneway_t<true, true>(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
     }
     // residuals of the records of step j-1 (they sample U_j)
     if (a.resid != nullptr) {
@@ -532,6 +538,186 @@ __global__ void __launch_bounds__(256) habc_bwd_interior_kernel(const HabcBwdArg
   }
 }
 
+
+// ------------------------------------------------ single-step VJP ---
+// The transpose of ONE step y = HABC(g (U - P) + P + I(U)) (I the
+// equation's interior operator) for autograd of the per-step
+// _time_step: gu = (dy/dU)^T G, gum = (dy/dP)^T G over the whole grid
+// (strips included), the interior-operator parameter terms sum_b wi G dI/dtheta
+// (plain: L(U), VTI: Lx(U) and Lz(U), variable density: D(U) and the four
+// C-weighted one-cell differences), and the one-way terms' velocity
+// derivative sum_b G sum_s ws d(one_s)/dvp.  With hw = 0 there is no blend
+// (the reverse step of the boundary-saving path, acoustic_habc.py:223-245).
+// Born (acoustic_lsrtm_habc.py:11-30): for the scattered field the source
+// m k L(p) adds dJ/dm = sum_b wi G k L(p), its k term to the L plane and
+// L(m k wi G) to dJ/dp.  One thread per cell loops over the shots, so the
+// parameter sums need no atomics.
+struct HabcVjpArgs {
+  int nz, nx, pitch, nshots, hw, multiple;
+  long long sstride;
+  const float* __restrict__ u;
+  const float* __restrict__ um;
+  const float* __restrict__ gy;
+  float* __restrict__ gu;
+  float* __restrict__ gum;
+  const float* __restrict__ g;
+  const float* __restrict__ k;
+  const float* __restrict__ kz;
+  const float* __restrict__ rho_c;
+  const float* __restrict__ vp;
+  const float* __restrict__ hb;
+  float lamf, muf;
+  FdWeights w;
+  float* __restrict__ gparam;  // [nplanes][nz][pitch]
+  float* __restrict__ gc;      // [nz][pitch] or null
+  const float* __restrict__ born_m;
+  const float* __restrict__ born_u;
+  float* __restrict__ born_gu;
+  float* __restrict__ born_gm;
+};
+
+template <int R, int EQ>
+__global__ void __launch_bounds__(256) habc_step_vjp_kernel(const HabcVjpArgs a) {
+  const long long cells = (long long)a.nz * a.nx;
+  const long long pl = (long long)a.nz * a.pitch;
+  const bool mult = a.multiple != 0;
+  constexpr bool vti = EQ == 1;
+  constexpr bool rho = EQ == 2 && R == 1;
+  const bool born = EQ == 0 && a.born_m != nullptr;
+  const float ch = 0.5f * a.w.c[0];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < cells;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int z = (int)(i / a.nx), x = (int)(i - (long long)z * a.nx);
+    const long long o = (long long)z * a.pitch + x;
+    // every stencil neighbour in the grid and outside the strips: wi = 1
+    const int far = a.hw + R;
+    const bool interior = z >= (mult ? R : far) && a.nz - 1 - z >= far && x >= far && a.nx - 1 - x >= far;
+    const HabcW wq = interior ? HabcW{1.f, 0.f, 0.f, 0.f, 0.f}
+                              : habc_weights(z, x, a.nz, a.nx, a.hw, mult, __ldg(a.hb + o));
+    auto wi_at = [&](int zz, int xx) -> float {
+      return interior ? 1.f
+                      : habc_weights(zz, xx, a.nz, a.nx, a.hw, mult, __ldg(a.hb + (long long)zz * a.pitch + xx)).wi;
+    };
+    const float gq = __ldg(a.g + o), kq = __ldg(a.k + o);
+    const float kzq = vti ? __ldg(a.kz + o) : 0.f;
+    const float mq = born ? __ldg(a.born_m + o) : 0.f;
+    float pacc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    float cacc = 0.f, macc = 0.f;
+    for (int b = 0; b < a.nshots; ++b) {
+      const long long fb = (long long)b * a.sstride;
+      const float* G = a.gy + fb;
+      const float* U = a.u + fb;
+      const float* P = a.um + fb;
+      // weighted adjoint at a neighbour (0 off the grid), times a coefficient plane
+      auto kwg = [&](int zz, int xx, const float* kp) -> float {
+        if (zz < 0 || zz >= a.nz || xx < 0 || xx >= a.nx) return 0.f;
+        const long long oo = (long long)zz * a.pitch + xx;
+        return __ldg(kp + oo) * wi_at(zz, xx) * G[oo];
+      };
+      const float Gw = wq.wi * G[o];
+      float tu;
+      if (rho) {
+        auto cw = [&](int zz, int xx, int q) -> float {
+          if (zz < 0 || zz >= a.nz || xx < 0 || xx >= a.nx) return 0.f;
+          const long long oo = (long long)zz * a.pitch + xx;
+          return __ldg(a.rho_c + oo) * __ldg(a.rho_c + q * pl + oo) * wi_at(zz, xx) * G[oo];
+        };
+        const float sum = __ldg(a.rho_c + pl + o) + __ldg(a.rho_c + 2 * pl + o) + __ldg(a.rho_c + 3 * pl + o) +
+                          __ldg(a.rho_c + 4 * pl + o);
+        tu = gq * Gw - sum * __ldg(a.rho_c + o) * Gw + cw(z, x - 1, 1) + cw(z, x + 1, 2) + cw(z - 1, x, 3) +
+             cw(z + 1, x, 4);
+      } else if (vti) {
+        float lap = ch * (kq + kzq) * Gw;
+        for (int j = 1; j <= R; ++j)
+          lap += a.w.c[j] * (kwg(z, x - j, a.k) + kwg(z, x + j, a.k) + kwg(z - j, x, a.kz) + kwg(z + j, x, a.kz));
+        tu = gq * Gw + lap;
+      } else {
+        float lap = a.w.c[0] * kq * Gw;
+        for (int j = 1; j <= R; ++j)
+          lap += a.w.c[j] * (kwg(z - j, x, a.k) + kwg(z + j, x, a.k) + kwg(z, x - j, a.k) + kwg(z, x + j, a.k));
+        tu = gq * Gw + lap;
+      }
+      float tum = (1.f - gq) * Gw;
+      if (!interior && a.hw > 0) {
+        tu += oneway_t<true, false>(a, G, nullptr, z, x, z, 1, 0, 0);
+        tu += oneway_t<true, false>(a, G, nullptr, z, x, a.nz - 1 - z, -1, 0, 1);
+        tu += oneway_t<true, false>(a, G, nullptr, z, x, x, 0, 1, 2);
+        tu += oneway_t<true, false>(a, G, nullptr, z, x, a.nx - 1 - x, 0, -1, 3);
+        tum += oneway_t<false, true>(a, nullptr, G, z, x, z, 1, 0, 0);
+        tum += oneway_t<false, true>(a, nullptr, G, z, x, a.nz - 1 - z, -1, 0, 1);
+        tum += oneway_t<false, true>(a, nullptr, G, z, x, x, 0, 1, 2);
+        tum += oneway_t<false, true>(a, nullptr, G, z, x, a.nx - 1 - x, 0, -1, 3);
+      }
+      a.gu[fb + o] = tu;
+      a.gum[fb + o] = tum;
+      // interior-operator parameter terms (each cell's own coefficients)
+      if (rho) {
+        const float u0 = U[o];
+        const float dxp = ldz(U, z, x + 1, a.nz, a.nx, a.pitch) - u0, dxn = u0 - ldz(U, z, x - 1, a.nz, a.nx, a.pitch);
+        const float dzp = ldz(U, z + 1, x, a.nz, a.nx, a.pitch) - u0, dzn = u0 - ldz(U, z - 1, x, a.nz, a.nx, a.pitch);
+        const float bxp = __ldg(a.rho_c + pl + o), bxn = __ldg(a.rho_c + 2 * pl + o);
+        const float bzp = __ldg(a.rho_c + 3 * pl + o), bzn = __ldg(a.rho_c + 4 * pl + o);
+        const float C = __ldg(a.rho_c + o);
+        pacc[0] += Gw * (bxp * dxp - bxn * dxn + bzp * dzp - bzn * dzn);
+        pacc[1] += Gw * C * dxp;
+        pacc[2] -= Gw * C * dxn;
+        pacc[3] += Gw * C * dzp;
+        pacc[4] -= Gw * C * dzn;
+      } else if (vti) {
+        float Lx = ch * U[o], Lz = ch * U[o];
+        for (int j = 1; j <= R; ++j) {
+          Lx += a.w.c[j] * (ldz(U, z, x - j, a.nz, a.nx, a.pitch) + ldz(U, z, x + j, a.nz, a.nx, a.pitch));
+          Lz += a.w.c[j] * (ldz(U, z - j, x, a.nz, a.nx, a.pitch) + ldz(U, z + j, x, a.nz, a.nx, a.pitch));
+        }
+        pacc[0] += Gw * Lx;
+        pacc[1] += Gw * Lz;
+      } else {
+        float L = a.w.c[0] * U[o];
+        for (int j = 1; j <= R; ++j)
+          L += a.w.c[j] * (ldz(U, z - j, x, a.nz, a.nx, a.pitch) + ldz(U, z + j, x, a.nz, a.nx, a.pitch) +
+                           ldz(U, z, x - j, a.nz, a.nx, a.pitch) + ldz(U, z, x + j, a.nz, a.nx, a.pitch));
+        pacc[0] += Gw * L;
+      }
+      if (born) {  // source m k L(p): its k and m terms, and L(m k wi G) into dJ/dp
+        const float* Pb = a.born_u + fb;
+        float Lp = a.w.c[0] * Pb[o];
+        float lg = a.w.c[0] * mq * kq * Gw;
+        for (int j = 1; j <= R; ++j) {
+          Lp += a.w.c[j] * (ldz(Pb, z - j, x, a.nz, a.nx, a.pitch) + ldz(Pb, z + j, x, a.nz, a.nx, a.pitch) +
+                            ldz(Pb, z, x - j, a.nz, a.nx, a.pitch) + ldz(Pb, z, x + j, a.nz, a.nx, a.pitch));
+          lg += a.w.c[j] * (kwg(z - j, x, a.born_m) * ldz(a.k, z - j, x, a.nz, a.nx, a.pitch) +
+                            kwg(z + j, x, a.born_m) * ldz(a.k, z + j, x, a.nz, a.nx, a.pitch) +
+                            kwg(z, x - j, a.born_m) * ldz(a.k, z, x - j, a.nz, a.nx, a.pitch) +
+                            kwg(z, x + j, a.born_m) * ldz(a.k, z, x + j, a.nz, a.nx, a.pitch));
+        }
+        pacc[0] += Gw * mq * Lp;
+        macc += Gw * kq * Lp;
+        a.born_gu[fb + o] = lg;
+      }
+      // velocity derivative of the one-way extrapolations (lam = c lamf, mu = c^2 muf)
+      if (!interior && a.hw > 0 && a.gc != nullptr) {
+        const float c = __ldg(a.vp + o);
+        const float dl = a.lamf, dm = 2.f * c * a.muf;
+        auto done = [&](int dq, int sz, int sx, int ze, int xe) -> float {
+          const long long d1 = (long long)sz * a.pitch + sx;
+          const float U2 = (dq + 2 <= a.hw) ? U[o + 2 * d1] : U[(long long)ze * a.pitch + xe];
+          return (-dl - dm) * U[o] + (dl + 2.f * dm) * U[o + d1] - dm * U2 + dl * P[o] - dl * P[o + d1];
+        };
+        float s = 0.f;
+        if (wq.wt != 0.f) s += wq.wt * done(z, 1, 0, 0, x);
+        if (wq.wb != 0.f) s += wq.wb * done(a.nz - 1 - z, -1, 0, a.nz - 1, x);
+        if (wq.wl != 0.f) s += wq.wl * done(x, 0, 1, z, 0);
+        if (wq.wr != 0.f) s += wq.wr * done(a.nx - 1 - x, 0, -1, z, a.nx - 1);
+        cacc += G[o] * s;
+      }
+    }
+    const int np = rho ? 5 : (vti ? 2 : 1);
+    for (int q = 0; q < np; ++q) a.gparam[q * pl + o] = pacc[q];
+    if (a.gc != nullptr) a.gc[o] = cacc;
+    if (born) a.born_gm[o] = macc;
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
@@ -624,6 +810,54 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
     case 10: habc_bwd_kernel<3, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
     case 12: habc_bwd_kernel<4, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
     case 13: habc_bwd_kernel<4, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_habc_step_vjp(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_habc_vjp_io& io,
+                                 cudaStream_t s) {
+  HabcVjpArgs a;
+  a.nz = g.nz;
+  a.nx = g.nx;
+  a.pitch = g.pitch;
+  a.nshots = g.nshots;
+  a.hw = m.habc_width;
+  a.multiple = m.multiple;
+  a.sstride = (long long)g.nz * g.pitch;
+  a.u = io.u;
+  a.um = io.um;
+  a.gy = io.gy;
+  a.gu = io.gu;
+  a.gum = io.gum;
+  a.g = m.coef;
+  a.k = m.coef + (long long)g.nz * g.pitch;
+  a.kz = io.kz;
+  a.rho_c = io.rho_c;
+  a.vp = m.vp;
+  a.hb = m.damp;
+  a.lamf = 2.f * g.dt / g.h;
+  a.muf = (g.dt * g.dt) / (g.h * g.h);
+  a.w = fd_weights(m.order);
+  a.gparam = io.gparam;
+  a.gc = io.gvp_oneway;
+  a.born_m = io.born_m;
+  a.born_u = io.born_u;
+  a.born_gu = io.born_gu;
+  a.born_gm = io.born_gm;
+  const long long cells = (long long)g.nz * g.nx;
+  long long blocks = (cells + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  const int R = m.order / 2;
+  const int eq = io.rho_c != nullptr ? 2 : (io.kz != nullptr ? 1 : 0);
+  if (eq != 0 && R != 1) return cudaErrorInvalidValue;  // VTI and variable density: 2nd order
+  switch (R * 3 + eq) {
+    case 3: habc_step_vjp_kernel<1, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 4: habc_step_vjp_kernel<1, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 5: habc_step_vjp_kernel<1, 2><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 6: habc_step_vjp_kernel<2, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 9: habc_step_vjp_kernel<3, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+    case 12: habc_step_vjp_kernel<4, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "seistorch_gb300.h"
 
 namespace sgb {
@@ -26,9 +28,13 @@ __device__ __align__(256) float g_noalloc_scratch[kScratchFloats];
 
 // Host-side cache of the array's device address, one entry per device.  The
 // array's name in host code is only a host-side stand-in; the address comes
-// from cudaGetSymbolAddress with the device current.
+// from cudaGetSymbolAddress with the device current.  Entries are atomic:
+// host threads making their first call on a device at the same time each
+// look the address up and store the same value.  cudaDeviceReset destroys
+// the context the address belongs to, so a caller that resets a device must
+// not call this entry point on that device again in the same process.
 constexpr int kMaxDevices = 64;
-float* g_scratch_addr[kMaxDevices] = {nullptr};
+std::atomic<float*> g_scratch_addr[kMaxDevices];
 
 }  // namespace
 
@@ -45,13 +51,14 @@ extern "C" int sgb_acoustic_backward_noalloc(const sgb_grid* grid, const sgb_aco
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return sgb::set_cuda_error(e);
   if (dev < 0 || dev >= kMaxDevices) return SGB_ERR_ARG;
-  if (g_scratch_addr[dev] == nullptr) {
+  float* base = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (base == nullptr) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return sgb::set_cuda_error(e);
-    g_scratch_addr[dev] = static_cast<float*>(p);
+    base = static_cast<float*>(p);
+    g_scratch_addr[dev].store(base, std::memory_order_release);
   }
-  float* base = g_scratch_addr[dev];
   // field is a multiple of 4 floats (pitch % 4 == 0 is checked downstream),
   // so every sub-buffer keeps the 16-byte alignment the kernels need.
   float* const lbuf[3] = {base, base + field, base + 2 * field};

@@ -38,6 +38,10 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -52,12 +56,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait for phase `parity` of `bar`; false (and a status bit) on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
-  for (uint32_t i = 0; i < MBAR_SPIN_LIMIT; ++i)
+// Wait for phase `parity` of `bar` for at most `limit` polls; false (and a
+// status bit) when it runs out.
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, uint32_t parity, int* status, uint32_t limit) {
+  for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   if (status != nullptr) atomicOr(status, DEV_ERR_TIMEOUT);
   return false;
+}
+
+// Bounded wait for phase `parity` of `bar`; false (and a status bit) on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
+  return mbar_wait_n(bar, parity, status, MBAR_SPIN_LIMIT);
 }
 
 // 3-D tiled TMA load (box from `map` at element coords x, y, z) into shared

@@ -12,7 +12,7 @@ import ctypes
 import torch
 
 from . import _native as N
-from .engine import grid_struct, interior_box, pitch_of, require_cuda, to_pitched
+from .engine import check_cfl, grid_struct, interior_box, pitch_of, require_cuda, to_pitched
 
 FIELDS = ("vx", "vz", "txx", "tzz", "txz")  # Wavefield('elastic') order (eqconfigure.py:45-127)
 
@@ -67,6 +67,7 @@ class ElasticPropagator:
     def model(self, vp, vs, rho, damp):
         """Pitched model planes and the six coefficient planes."""
         require_cuda(vp, "ElasticPropagator.model")
+        check_cfl(vp, N.SCHEME_ELASTIC, 2, self.dt, self.h)
         planes = [to_pitched(m.detach().to(vp.device), self.pitch).contiguous() for m in (vp, vs, rho, damp)]
         coef = torch.empty(6, self.nz, self.pitch, dtype=torch.float32, device=vp.device)
         g = self.grid(1)

@@ -8,6 +8,7 @@ raise when CUDA or the library is unavailable.
 """
 import ctypes
 import math
+import weakref
 
 import numpy as np
 import torch
@@ -28,6 +29,27 @@ def require_cuda(t, what):
         raise RuntimeError(f"{what}: seistorch_gb300 needs a CUDA GPU (sm_103a); no CPU fallback")
     if t is not None and not t.is_cuda:
         raise RuntimeError(f"{what}: expected a CUDA tensor, got {t.device}")
+
+
+_CFL_LAST = {}
+
+
+def check_cfl(vel, scheme, order, dt, h, vmax_of=None):
+    """Refuse a time step above the scheme's stability limit (sgb_cfl_check).
+
+    ``vel`` is the model tensor the step depends on; ``vmax_of(vel)`` gives
+    the effective maximum velocity (default: vel.max()).  The maximum is read
+    once per tensor and version, so a per-step loop over the same model pays
+    the device read once."""
+    key = (scheme, int(order), float(dt), float(h))
+    hit = _CFL_LAST.get(key)
+    if hit is not None and hit[0]() is vel and hit[1] == vel._version:
+        return
+    vmax = float(vmax_of(vel)) if vmax_of is not None else float(vel.detach().max())
+    N.cfl_check(scheme, order, vmax, dt, h)
+    if len(_CFL_LAST) > 64:
+        _CFL_LAST.clear()
+    _CFL_LAST[key] = (weakref.ref(vel), vel._version)
 
 
 def to_pitched(a, pitch, dtype=torch.float32):
@@ -172,16 +194,19 @@ class AcousticPropagator:
         self.device = torch.device(device) if device is not None else torch.device("cuda")
 
     # -- coefficients
-    def model(self, vp, damp):
-        """Pitched vp / damping planes and the (g, k) coefficient planes."""
+    def model(self, vp, damp, blend=True):
+        """Pitched vp / damping planes and the (g, k) coefficient planes.
+        ``blend=False`` (HABC only) drops the one-way blend: the plain
+        undamped update of the reference's reverse steps."""
         require_cuda(vp, "AcousticPropagator.model")
+        check_cfl(vp, N.SCHEME_ACOUSTIC, self.order, self.dt, self.h)
         vpp = to_pitched(vp.detach(), self.pitch).contiguous()
         dp = to_pitched(damp.detach().to(vp.device), self.pitch).contiguous()
         coef = torch.empty(2, self.nz, self.pitch, dtype=torch.float32, device=vp.device)
         g = grid_struct(self.nz, self.nx, self.pitch, 1, self.dt, self.h)
         N.call("sgb_acoustic_coefficients", ctypes.byref(g), N.ptr(vpp), N.ptr(dp), self.boundary,
                N.ptr(coef), N.stream_handle())
-        m = N.AcousticModel(self.order, self.boundary, 50, int(self.multiple), N.ptr(coef),
+        m = N.AcousticModel(self.order, self.boundary, 50 if blend else 0, int(self.multiple), N.ptr(coef),
                             N.ptr(vpp), N.ptr(dp))
         return m, (vpp, dp, coef)
 
@@ -189,8 +214,8 @@ class AcousticPropagator:
         return grid_struct(self.nz, self.nx, self.pitch, nshots, self.dt, self.h)
 
     # -- one step (equation-module drop-in)
-    def step(self, vp, damp, u, um):
-        m, keep = self.model(vp, damp)
+    def step(self, vp, damp, u, um, blend=True):
+        m, keep = self.model(vp, damp, blend)
         B = u.shape[0]
         up = to_pitched(u, self.pitch).contiguous()
         ump = to_pitched(um, self.pitch).contiguous()
@@ -213,6 +238,42 @@ class AcousticPropagator:
         N.call("sgb_acoustic_step_vjp", ctypes.byref(g), ctypes.byref(m), N.ptr(up), N.ptr(gyp),
                N.ptr(gh1p), N.ptr(gu), N.ptr(gum), N.ptr(gvp), N.stream_handle())
         return gu[..., :self.nx], gum[..., :self.nx], gvp[:, :self.nx]
+
+    def habc_vjp(self, m, u, um, gy, kz=None, rho_c=None, born=None):
+        """sgb_habc_step_vjp on pitched copies: dict of gu, gum (fields),
+        gparam (1, 2 or 5 planes), gc (one-way velocity term) and, with
+        ``born = (m plane, background U_n)``, born_gu and born_gm."""
+        B = u.shape[0]
+        pit = lambda t: to_pitched(t.to(torch.float32), self.pitch).contiguous()
+        up, ump, gyp = pit(u), pit(um), pit(gy)
+        dev = up.device
+        out = {"gu": torch.empty_like(up), "gum": torch.empty_like(up),
+               "gparam": torch.empty(5 if rho_c is not None else (2 if kz is not None else 1), self.nz,
+                                     self.pitch, dtype=torch.float32, device=dev),
+               "gc": torch.empty(self.nz, self.pitch, dtype=torch.float32, device=dev)}
+        bm = bu = None
+        if born is not None:
+            bm = to_pitched(born[0].detach().to(device=dev, dtype=torch.float32), self.pitch).contiguous()
+            bu = pit(born[1])
+            out["born_gu"] = torch.empty_like(up)
+            out["born_gm"] = torch.empty(self.nz, self.pitch, dtype=torch.float32, device=dev)
+        io = N.HabcVjpIO(N.ptr(up), N.ptr(ump), N.ptr(gyp), N.ptr(out["gu"]), N.ptr(out["gum"]),
+                         N.ptr(out["gparam"]), N.ptr(out["gc"]), N.ptr(kz), N.ptr(rho_c), N.ptr(bm), N.ptr(bu),
+                         N.ptr(out.get("born_gu")), N.ptr(out.get("born_gm")))
+        g = self.grid(B)
+        N.call("sgb_habc_step_vjp", ctypes.byref(g), ctypes.byref(m), ctypes.byref(io), N.stream_handle())
+        nx = self.nx
+        return {k: v[..., :nx] for k, v in out.items()}
+
+    def step_vjp_habc(self, vp, damp, u, um, gy, blend=True):
+        """VJP of one HABC step (acoustic_habc._time_step): dJ/du, dJ/dum and
+        dJ/dvp over the whole grid (k = vp^2 dt^2 / h^2, so dk/dvp = 2 vp dt^2 / h^2)."""
+        m, keep = self.model(vp, damp, blend)
+        r = self.habc_vjp(m, u, um, gy)
+        gvp = r["gparam"][0] * (2.0 * (self.dt / self.h) ** 2) * vp.detach().to(torch.float32)
+        if blend:
+            gvp = gvp + r["gc"]
+        return r["gu"], r["gum"], gvp
 
     # -- whole loop
     def forward(self, vp, damp, acq, *, save_for_adjoint=False, illumination=False, ckpt_every=0,
@@ -361,9 +422,20 @@ class BornPropagator(AcousticPropagator):
         state.scattered = sbuf
         return records[:, :acq.nrec], state
 
-    def step_born(self, vp, refl, damp, p, pm, sc, scm):
+    def step_vjp_born(self, vp, refl, damp, p, pm, sc, scm, gp, gs, blend=True):
+        """VJP of one Born step (acoustic_lsrtm_habc._time_step) given dJ/dp+
+        and dJ/ds+: dJ/d(p, pm, s, sm), dJ/dvp and dJ/dm."""
+        m, keep = self.model(vp, damp, blend)
+        rp = self.habc_vjp(m, p, pm, gp)
+        rs = self.habc_vjp(m, sc, scm, gs, born=(refl, p))
+        gvp = (rp["gparam"][0] + rs["gparam"][0]) * (2.0 * (self.dt / self.h) ** 2) * vp.detach().to(torch.float32)
+        if blend:
+            gvp = gvp + rp["gc"] + rs["gc"]
+        return rp["gu"] + rs["born_gu"], rp["gum"], rs["gu"], rs["gum"], gvp, rs["born_gm"]
+
+    def step_born(self, vp, refl, damp, p, pm, sc, scm, blend=True):
         """One step of both fields (no sources or receivers): (p+, s+)."""
-        m, keep = self.model(vp, damp)
+        m, keep = self.model(vp, damp, blend)
         B = p.shape[0]
         pit = lambda t: to_pitched(t.to(torch.float32), self.pitch).contiguous()
         pp, ppm, ps, psm = pit(p), pit(pm), pit(sc), pit(scm)
@@ -447,20 +519,41 @@ class VTIPropagator(AcousticPropagator):
     def __init__(self, nz, nx, dt, h, bwidth=50, multiple=False, device=None):
         super().__init__(nz, nx, dt, h, 2, "habc", bwidth, multiple, device)
 
-    def model_vti(self, vp, eps, delta, damp):
+    def model_vti(self, vp, eps, delta, damp, blend=True):
         require_cuda(vp, "VTIPropagator.model_vti")
         cx, cz = vti_coefficients(vp.detach(), eps.detach(), delta.detach(), self.dt, self.h)
+        # stability of 2u - u- + kx Lx + kz Lz: the isotropic limit with the
+        # velocity sqrt((kx + kz) / 2) h / dt
+        check_cfl(vp, N.SCHEME_ACOUSTIC, 2, self.dt, self.h,
+                  lambda _: float(((cx + cz) / 2).clamp_min(0).max().sqrt()) * self.h / self.dt)
         coef = torch.empty(3, self.nz, self.pitch, dtype=torch.float32, device=vp.device)
         coef[0] = 2.0
         coef[1] = to_pitched(cx.float(), self.pitch)
         coef[2] = to_pitched(cz.float(), self.pitch)
         vpp = to_pitched(vp.detach().float(), self.pitch).contiguous()
         dp = to_pitched(damp.detach().to(vp.device).float(), self.pitch).contiguous()
-        m = N.AcousticModel(2, BOUNDARY_HABC, 50, int(self.multiple), N.ptr(coef), N.ptr(vpp), N.ptr(dp))
+        m = N.AcousticModel(2, BOUNDARY_HABC, 50 if blend else 0, int(self.multiple), N.ptr(coef), N.ptr(vpp),
+                            N.ptr(dp))
         return m, (vpp, dp, coef)
 
-    def step_vti(self, vp, eps, delta, damp, u, um):
-        m, keep = self.model_vti(vp, eps, delta, damp)
+    def step_vjp_vti(self, vp, eps, delta, damp, u, um, gy, blend=True):
+        """VJP of one VTI step (vti_habc2._time_step): dJ/du, dJ/dum and
+        dJ/d(vp, eps, delta), the coefficient planes' terms mapped through
+        the differentiable coefficient map."""
+        m, keep = self.model_vti(vp, eps, delta, damp, blend)
+        r = self.habc_vjp(m, u, um, gy, kz=keep[2][2])
+        with torch.enable_grad():
+            ins = [t.detach().requires_grad_(True) for t in (vp, eps, delta)]
+            cx, cz = vti_coefficients(*ins, self.dt, self.h)
+            grads = torch.autograd.grad((cx, cz), ins, (r["gparam"][0].double(), r["gparam"][1].double()),
+                                        allow_unused=True)
+        grads = [torch.zeros_like(t, dtype=torch.float64) if g_ is None else g_ for g_, t in zip(grads, ins)]
+        if blend:
+            grads[0] = grads[0] + r["gc"].double()
+        return r["gu"], r["gum"], grads
+
+    def step_vti(self, vp, eps, delta, damp, u, um, blend=True):
+        m, keep = self.model_vti(vp, eps, delta, damp, blend)
         up = to_pitched(u.float(), self.pitch).contiguous()
         ump = to_pitched(um.float(), self.pitch).contiguous()
         out = torch.empty_like(up)
@@ -574,8 +667,23 @@ class RhoPropagator(AcousticPropagator):
             out[i] = to_pitched(p_.float(), self.pitch)
         return out
 
-    def step_rho(self, vp, rho, damp, u, um):
-        m, keep = self.model(vp, damp)
+    def step_vjp_rho(self, vp, rho, damp, u, um, gy, blend=True):
+        """VJP of one variable-density step (acoustic_rho_habc._time_step):
+        dJ/du, dJ/dum and dJ/d(vp, rho) through the differentiable planes."""
+        m, keep = self.model(vp, damp, blend)
+        rc = self.planes(vp, rho)
+        r = self.habc_vjp(m, u, um, gy, rho_c=rc)
+        with torch.enable_grad():
+            ins = [t.detach().requires_grad_(True) for t in (vp, rho)]
+            planes = rho_coefficients(*ins, self.dt, self.h)
+            grads = torch.autograd.grad(planes, ins, [r["gparam"][q].double() for q in range(5)], allow_unused=True)
+        grads = [torch.zeros_like(t, dtype=torch.float64) if g_ is None else g_ for g_, t in zip(grads, ins)]
+        if blend:
+            grads[0] = grads[0] + r["gc"].double()
+        return r["gu"], r["gum"], grads
+
+    def step_rho(self, vp, rho, damp, u, um, blend=True):
+        m, keep = self.model(vp, damp, blend)
         rc = self.planes(vp, rho)
         up = to_pitched(u.float(), self.pitch).contiguous()
         ump = to_pitched(um.float(), self.pitch).contiguous()

@@ -2,7 +2,8 @@
 (seistorch/equations2d/acoustic_rho_habc.py): 2 p1 - p2 + dt^2 h^-2 rho vp^2
 (bx+ dx+ p - bx- dx- p + bz+ dz+ p - bz- dz- p) with averaged buoyancies,
 then the one-way-wave blend (``engine.rho_coefficients``).  ``_time_step`` is
-one native step (``sgb_rho_step``); the whole loop with its adjoint runs
+one native step (``sgb_rho_step``) with its native VJP
+(``sgb_habc_step_vjp``) for autograd; the whole loop with its adjoint runs
 through ``WaveRNN`` (``engine.rho_loop``)."""
 import torch
 
@@ -21,7 +22,21 @@ def _propagator(shape, dt, h, multiple, device):
     return prop
 
 
-def _step(args, multiple):
+class _RhoStep(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, vp, rho, p1, p2, damp, prop, blend):
+        ctx.prop, ctx.blend = prop, blend
+        ctx.save_for_backward(vp, rho, p1, p2, damp)
+        return prop.step_rho(vp, rho, damp, p1, p2, blend)
+
+    @staticmethod
+    def backward(ctx, gy):
+        vp, rho, p1, p2, damp = ctx.saved_tensors
+        gu, gum, gm = ctx.prop.step_vjp_rho(vp, rho, damp, p1, p2, gy.contiguous(), ctx.blend)
+        return gm[0].to(vp.dtype), gm[1].to(rho.dtype), gu.to(p1.dtype), gum.to(p2.dtype), None, None, None
+
+
+def _step(args, multiple, blend=True):
     vp, rho = args[0:2]
     p1, p2 = args[2:4]
     dt, h, b = args[4:7]
@@ -29,11 +44,8 @@ def _step(args, multiple):
     squeeze = p1.ndim == 2
     if squeeze:
         p1, p2 = p1[None], p2[None]
-    if torch.is_grad_enabled() and any(t.requires_grad for t in (vp, rho, p1, p2)):
-        raise NotImplementedError("the per-step variable-density op is forward-only; differentiate the whole "
-                                  "loop through WaveRNN (engine.rho_loop)")
     prop = _propagator(p1.shape, _scalar(dt), _scalar(h), multiple, p1.device)
-    y = prop.step_rho(vp, rho, b.to(p1.device), p1, p2).to(p1.dtype)
+    y = _RhoStep.apply(vp, rho, p1, p2, b.to(p1.device), prop, blend).to(p1.dtype)
     return (y[0], p1[0]) if squeeze else (y, p1)
 
 
@@ -45,12 +57,13 @@ def _time_step(*args, **kwargs):
 
 def _backward(args, multiple):
     """Reverse step of the reference's boundary-saving path
-    (acoustic_rho_habc.py:60-121): the forward update with (p1, p2) =
-    (u_{n+1}, u_n), saved strips restored, the source re-added."""
+    (acoustic_rho_habc.py:60-121): the interior update without the one-way
+    blend with (p1, p2) = (u_{n+1}, u_n), saved strips restored, the source
+    re-added."""
     from .utils import restore_boundaries
     h_bd, _ = args[-2]
     src_type, src_func, src_values = args[-1]
-    y, p1 = _step(args[:7], multiple)
+    y, p1 = _step(args[:7], multiple, blend=False)
     with torch.no_grad():
         y = restore_boundaries(y, h_bd, multiple=multiple)
     y = src_func(y, src_values, 1)

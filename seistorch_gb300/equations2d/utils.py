@@ -3,17 +3,21 @@ import torch
 
 
 def diff_using_roll(input, dim=-1, forward=True, padding_value=0):
-    """forward: x[i] - x[i-1] (0 at i=0); backward: x[i+1] - x[i] (0 at the
-    last index) (utils.py:3-48)."""
+    """forward: x[i] - x[i-1]; backward: x[i+1] - x[i] (utils.py:3-48).
+
+    The wrapped edge value is replaced by ``padding_value`` only for
+    ``dim == 1`` (index 0 / -1 of axis 1) and ``dim == 2`` (index 0 / -1 of
+    the LAST axis); any other ``dim`` keeps the roll's wrap, as the
+    reference does."""
+    edge = 0 if forward else -1
     if forward:
         diff = input - torch.roll(input, shifts=1, dims=dim)
-        idx = [slice(None)] * input.ndim
-        idx[dim] = 0
     else:
         diff = torch.roll(input, shifts=-1, dims=dim) - input
-        idx = [slice(None)] * input.ndim
-        idx[dim] = -1
-    diff[tuple(idx)] = padding_value
+    if dim == 1:
+        diff[:, edge] = padding_value
+    elif dim == 2:
+        diff[..., edge] = padding_value
     return diff
 
 

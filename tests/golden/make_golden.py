@@ -3,7 +3,7 @@
 Run in a container that holds the reference source tree (see
 ``ref_loader.REF_ROOT``)::
 
-    python tests/golden/make_golden.py
+    SEISTORCH_REF_ROOT=<reference checkout> python tests/golden/make_golden.py
 
 Each case runs the reference ``WaveRNN``/``WaveCell`` time loop
 (rnn.py:100-217, cell.py:50-77) with its own equation modules, PML/HABC
@@ -51,7 +51,7 @@ def acquisition(nz_int, nx_int, nshots, width, multiple, step=3):
 
 def run_case(ref, equation, models_int, *, order=2, width=20, multiple=False, nshots=2,
              nt=200, dt=0.001, h=10.0, fm=15.0, habc=False, dtype=torch.float64,
-             grad=None, obs_models=None, source_type=None, receiver_type=None):
+             grad=None, obs_models=None, source_type=None, receiver_type=None, boundary_saving=False):
     torch.set_default_dtype(dtype)
     eqmod = {"acoustic": ref.acoustic, "acoustic_habc": ref.acoustic_habc,
              "acoustic_lsrtm_habc": ref.acoustic_lsrtm_habc, "vti_habc2": ref.vti_habc2,
@@ -84,11 +84,20 @@ def run_case(ref, equation, models_int, *, order=2, width=20, multiple=False, ns
     st = source_type or (["h1"] if equation != "elastic" else ["txx", "tzz"])
     rt = receiver_type or (["h1"] if equation != "elastic" else ["vx", "vz"])
 
+    # model.py:87 marks the second-order equations' step function; the
+    # boundary-saving reverse sweep reads it (checkpoint_new.py:147)
+    eqmod._time_step.ACOUSTIC2nd = equation in ref.eqconfigure.Parameters.secondorder_equations()
+
     def forward(models, requires_grad=()):
         geom = RL.make_geom(ref, equation, models, d, dt, h, use_habc=habc, bwidth=width,
                             multiple=multiple, source_type=st, receiver_type=rt,
                             inversion=bool(requires_grad), requires_grad=requires_grad,
-                            dtype=dtype)
+                            boundary_saving=boundary_saving and bool(requires_grad), dtype=dtype)
+        # the reverse sweep's class-level state (checkpoint_new.py:111-112,
+        # checkpoint.py:110-111) starts fresh for every case
+        for ck in (ref.checkpoint_new.CheckpointFunction, ref.checkpoint.CheckpointFunction):
+            ck.counts = 0
+            ck.wavefields = []
         rnn, y = RL.run_wavernn(ref, geom, eqmod._time_step, eqmod._time_step_backward, w, src, rec)
         return geom, rnn, y
 
@@ -124,6 +133,7 @@ def run_case(ref, equation, models_int, *, order=2, width=20, multiple=False, ns
         for n in names:
             out["obsmodel_" + n] = obs_padded[n]
     meta = dict(equation=equation, order=order, width=width, multiple=multiple, nt=nt, dt=dt,
+                boundary_saving=boundary_saving,
                 h=h, fm=fm, habc=habc, src=np.array(src), nshots=nshots,
                 rec_z=np.array([r[0] for r in rec]), rec_x=np.array([r[1] for r in rec]),
                 wavelet=w, d=np.asarray(d.numpy() if torch.is_tensor(d) else d),
@@ -196,6 +206,15 @@ def cases():
                                   multiple=True, nt=240)
     C["grad_rho_habc_zeroobs"] = dict(equation="acoustic_rho_habc", models_int=rho, order=2, width=50, habc=True,
                                       nt=200, grad=["vp", "rho"], obs_models=None)
+    # the reference's per-step boundary-saving gradient (cell.py:71-72; 1-cell
+    # strips at index 49, so a 50-cell boundary)
+    C["grad_bs_acoustic_pml_o2_zeroobs"] = dict(equation="acoustic", models_int=ah, order=2, width=50, nt=160,
+                                                grad=["vp"], obs_models=None, boundary_saving=True)
+    C["grad_bs_acoustic_habc_o2_zeroobs"] = dict(equation="acoustic_habc", models_int=ah, order=2, width=50,
+                                                 habc=True, nt=160, grad=["vp"], obs_models=None,
+                                                 boundary_saving=True)
+    C["grad_bs_elastic_zeroobs"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0, width=50,
+                                        nt=160, grad=["vp", "vs", "rho"], obs_models=None, boundary_saving=True)
     C["grad_elastic_zeroobs"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,
                                      nt=200, grad=["vp", "vs", "rho"], obs_models=None)
     C["grad_elastic"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,

@@ -24,7 +24,8 @@ import os
 import sys
 import types
 
-REF_ROOT = os.environ.get("SEISTORCH_REF_ROOT", "/root/reference")
+# the reference checkout must be named explicitly (no machine-specific default)
+REF_ROOT = os.environ.get("SEISTORCH_REF_ROOT", "")
 PKG_DIR = os.path.join(REF_ROOT, "seistorch")
 
 _STUB_ROOTS = ["yaml", "h5py", "geomloss", "torchvision", "torchaudio", "segyio",
@@ -108,6 +109,8 @@ def _exec_patched(modname, path, device, line_patches=()):
 
 def load(device="cpu"):
     """Return a namespace with the reference hot-path modules."""
+    if not REF_ROOT or not os.path.isdir(PKG_DIR):
+        raise RuntimeError("set SEISTORCH_REF_ROOT to a seistorch checkout (the directory holding seistorch/)")
     _install_stubs()
     _install_package()
     ns = types.SimpleNamespace()
@@ -132,6 +135,8 @@ def load(device="cpu"):
     ns.source = importlib.import_module("seistorch.source")
     ns.probe = importlib.import_module("seistorch.probe")
     ns.cell = importlib.import_module("seistorch.cell")
+    ns.checkpoint = importlib.import_module("seistorch.checkpoint")
+    ns.checkpoint_new = importlib.import_module("seistorch.checkpoint_new")
     ns.rnn = importlib.import_module("seistorch.rnn")
     ns.rutils = importlib.import_module("seistorch.utils")
     ns.type = importlib.import_module("seistorch.type")

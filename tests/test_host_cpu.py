@@ -308,3 +308,84 @@ def test_every_registered_equation_has_the_reference_entry_points():
         assert eq in paras and len(Wavefield(eq).wavefields) in (2, 4), eq
     assert paras["acoustic_lsrtm_habc"] == ["vp", "m"]
     assert Wavefield("vti_habc2").wavefields == ["p1", "p2"]
+
+
+def test_cfl_check_limits_and_refusal(lib):
+    """sgb_cfl_check: the leapfrog limit 2/sqrt(max eig(-h^2 L)) per order,
+    1/sqrt(2) for the staggered elastic grid, and SGB_ERR_CFL above it
+    (host only).  The workloads' Courant numbers (about 0.38 for 128x256 at
+    4th order, 0.45 for 400x1000 at 8th order, 0.5 for the elastic 300x800
+    grid) sit below their limits."""
+    from seistorch_gb300 import _native as N
+    want = {2: 1 / np.sqrt(2), 4: 1 / np.sqrt(8 / 3), 6: 1 / np.sqrt(2 * (1.5 + 1 / 90)),
+            8: 1 / np.sqrt(2 * (8 / 5 + 8 / 315))}
+    for order, lim in want.items():
+        c, got = N.cfl_check(N.SCHEME_ACOUSTIC, order, 1000.0, 0.001, 10.0)
+        assert abs(got - lim) < 1e-5 and abs(c - 0.1) < 1e-6
+    assert abs(N.cfl_check(N.SCHEME_ELASTIC, 2, 1000.0, 0.0005, 5.0)[1] - 1 / np.sqrt(2)) < 1e-6
+    assert N.cfl_check(N.SCHEME_ACOUSTIC, 4, 3800.0, 0.001, 10.0)[0] < want[4]
+    assert N.cfl_check(N.SCHEME_ACOUSTIC, 8, 4500.0, 0.001, 10.0)[0] < want[8]
+    assert N.cfl_check(N.SCHEME_ELASTIC, 2, 5000.0, 0.0005, 5.0)[0] < 1 / np.sqrt(2)
+    # a bad dt: 4500 m/s at 10 m needs dt below 1.23 ms at 8th order
+    with pytest.raises(N.NativeError, match="CFL"):
+        N.cfl_check(N.SCHEME_ACOUSTIC, 8, 4500.0, 0.0013, 10.0)
+    with pytest.raises(N.NativeError, match="CFL"):
+        N.cfl_check(N.SCHEME_ELASTIC, 2, 5000.0, 0.0008, 5.0)
+    out = ctypes.c_float(0.0)
+    assert lib.sgb_cfl_check(0, 2, 2000.0, 0.004, 10.0, ctypes.byref(out), None) == 9
+    assert abs(out.value - 0.8) < 1e-6
+    assert lib.sgb_status_string(9).startswith(b"CFL")
+    assert lib.sgb_cfl_check(0, 3, 2000.0, 0.001, 10.0, None, None) == 5   # order
+    assert lib.sgb_cfl_check(1, 4, 2000.0, 0.001, 10.0, None, None) == 5   # elastic is 2nd order
+    assert lib.sgb_cfl_check(0, 2, 2000.0, -0.001, 10.0, None, None) == 1  # dt
+    assert lib.sgb_cfl_check(2, 2, 2000.0, 0.001, 10.0, None, None) == 1   # scheme
+
+
+def test_cfl_limit_is_the_stencil_stability_edge():
+    """The acoustic limit is where the leapfrog recursion's amplification at
+    the worst wavenumber reaches 1: just below it a plane wave of that
+    wavenumber stays bounded over many steps, just above it it grows."""
+    from oracle import fd2d
+    from seistorch_gb300 import _native as N
+    for order in (2, 4, 8):
+        lim = N.cfl_check(N.SCHEME_ACOUSTIC, order, 0.1, 1.0, 1.0)[1]
+        c = fd2d.fd_coefficients(order)
+        th = np.linspace(0, np.pi, 4097)
+        s1 = np.max(2 * sum(cj * (1 - np.cos((j + 1) * th)) for j, cj in enumerate(c)))
+        for fac, bounded in ((0.999, True), (1.001, False)):
+            a = (fac * lim) ** 2 * 2 * s1  # C^2 * max eig of -h^2 L
+            u0, u1 = 1.0, 1.0
+            for _ in range(20000):
+                u0, u1 = u1, (2 - a) * u1 - u0
+            assert (abs(u1) < 1e3) == bounded, (order, fac, u1)
+
+
+@pytest.mark.parametrize("name", ["acoustic_habc_o2", "acoustic_habc_o2_multiple", "elastic"])
+def test_save_restore_boundaries_match_reference(name):
+    """save_boundaries / restore_boundaries (equations2d/utils.py:50-90) on
+    the fields the step goldens hold: the strips the reference saved from
+    one state, and the reference's restore of another state's strips into
+    it (with and without ``multiple``)."""
+    from seistorch_gb300.equations2d.utils import restore_boundaries, save_boundaries
+    z = np.load(os.path.join(ROOT, "tests", "golden", f"steps_{name}.npz"))
+    f0 = str(z["field_names"][0])
+    tgt = torch.tensor(z["restore_target"], dtype=torch.float64)
+    for got, k in zip(save_boundaries(tgt), "tblr"):
+        assert np.array_equal(got.numpy(), z[f"strip_{f0}_{k}"].astype(np.float64))
+    strips = save_boundaries(torch.tensor(z["in_" + f0], dtype=torch.float64))
+    assert np.array_equal(restore_boundaries(tgt.clone(), strips).numpy(), z["restored"].astype(np.float64))
+    assert np.array_equal(restore_boundaries(tgt.clone(), strips, multiple=True).numpy(),
+                          z["restored_multiple"].astype(np.float64))
+
+
+def test_diff_using_roll_edge_rule():
+    """Only dim 1 and dim 2 (the last axis) get the padding value at the
+    wrapped edge (equations2d/utils.py:17-23,37-43); other dims keep the wrap."""
+    from seistorch_gb300.equations2d.utils import diff_using_roll
+    x = torch.arange(24.0).reshape(2, 3, 4) ** 2
+    f1 = diff_using_roll(x, 1)
+    assert torch.all(f1[:, 0] == 0) and torch.equal(f1[:, 1:], x[:, 1:] - x[:, :-1])
+    b2 = diff_using_roll(x, 2, False)
+    assert torch.all(b2[..., -1] == 0) and torch.equal(b2[..., :-1], x[..., 1:] - x[..., :-1])
+    wrap = diff_using_roll(x, -1)  # not 1 or 2: the roll's wrap stays
+    assert torch.equal(wrap, x - torch.roll(x, 1, -1))

@@ -8,7 +8,9 @@ library.  Two calls in a row through the C ABI must give the gradient of the
 regular entry point (which takes caller-allocated scratch) within the
 gradient tolerance of the other tests (relative L2 1e-4); the second call
 also shows that what the first call left in the shared array does not leak
-into the next.  This file is named to be collected last.
+into the next, and the device's free memory (cudaMemGetInfo) is the same
+before and after it: the call allocates nothing.  This file is named to be
+collected last.
 """
 import ctypes
 
@@ -45,7 +47,7 @@ def test_noalloc_adjoint_matches_allocating_entry_point_twice():
     want = prop.backward(state, acq, resid).cpu().numpy()
     assert np.isfinite(want).all() and np.abs(want).max() > 0
 
-    for _ in range(2):
+    for call in range(2):
         rec, state = _forward_state(g, dev, prop, acq)
         resid = (2.0 * rec).contiguous()
         res = torch.zeros(acq.nt, acq.nrec, 1, dtype=torch.float32, device=dev)
@@ -54,8 +56,14 @@ def test_noalloc_adjoint_matches_allocating_entry_point_twice():
         gr = prop.grid(acq.nshots)
         q = acq.struct(res, 1)
         ub = N.PTR3(*[b.data_ptr() for b in state.buf])
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info(dev)[0]
         N.call("sgb_acoustic_backward_noalloc", ctypes.byref(gr), ctypes.byref(state.model), ctypes.byref(q),
                ctypes.byref(state.bs), ub, state.cur, state.prev, N.ptr(grad), N.stream_handle())
+        torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info(dev)[0]
+        if call == 1:  # the first call may load the kernels' module; the second must not allocate
+            assert free_after == free_before, (free_before, free_after)
         got = grad[:, :nx].cpu().numpy()
         assert rel_l2(got, want) < 1e-4
 
