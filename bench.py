@@ -189,12 +189,16 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="acoustic_gradient",
                     choices=["acoustic_gradient", "elastic_gradient", "uneven_forward", "learned_fwi", "learned_net",
-                             "born_gradient", "vti_gradient", "rho_gradient"],
+                             "born_gradient", "vti_gradient", "rho_gradient", "forward_small", "habc_gradient"],
                     help="acoustic_gradient (default, the headline line); elastic_gradient: 300x800 + 50 PML "
                          "elastic forward+adjoint; uneven_forward: 4 grid sizes x 64 shots in one launch per step; "
                          "born_gradient: least-squares RTM gradient (Born modelling, HABC); "
                          "vti_gradient: VTI (vti_habc2) vp / eps / delta gradient; "
-                         "rho_gradient: variable-density (acoustic_rho_habc) vp / rho gradient")
+                         "rho_gradient: variable-density (acoustic_rho_habc) vp / rho gradient; "
+                         "forward_small: 128x256 + 50 PML, 4th order, 8 shots, 1000 steps, forward only "
+                         "(L2-resident); habc_gradient: the headline grid and model with the hybrid absorbing "
+                         "boundary (acoustic_habc), --order 2 (default) or 4")
+    ap.add_argument("--order", type=int, default=0, help="habc_gradient: spatial order (2 or 4)")
     ap.add_argument("--pairs", type=int, default=2000, help="learned_fwi: training pairs")
     ap.add_argument("--epochs", type=int, default=12, help="learned_fwi: training epochs")
     ap.add_argument("--iters", type=int, default=20, help="learned_fwi: FWI iterations")
@@ -214,6 +218,10 @@ def main():
         return bench_vti(args)
     if args.workload == "rho_gradient":
         return bench_rho(args)
+    if args.workload == "forward_small":
+        return bench_forward_small(args)
+    if args.workload == "habc_gradient":
+        return bench_habc(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -388,6 +396,235 @@ def e2e_through_api(args, dev, vp_init, obs_host, wav, sources, receivers, world
     return {"value": len(sources) * nz * nx * NT * world / wall / 1e9, "unit": "Gpts/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(grad_host.numel() * 4 + 4),
             "ms_per_step": wall * 1e3, "api": "build_model -> WaveRNN.forward -> loss.backward"}
+
+
+# ------------------------------------------------- small forward (C1) ---
+# 128 x 256 interior + 50-cell PML (228 x 356), dx = 10 m, dt = 1 ms, 1000
+# steps, 4th order, fp32; vp: 3 horizontal layers 1500 / 2500 / 3500 m/s plus
+# a Gaussian anomaly (+300 m/s, sigma = 10 cells, centre drawn from the seed);
+# 8 shots on row 2 spaced 32 cells, 10 Hz Ricker, receivers on every cell of
+# row 2.  One step = one forward modelling of the 8 shots (records).  The
+# working set (three 2.6 MB fields) lives in L2, so the figure is reported
+# against the HBM roofline for reference only.
+FS_NZI, FS_NXI, FS_NT, FS_ORDER, FS_FM, FS_SHOTS = 128, 256, 1000, 4, 10.0, 8
+
+
+def forward_small_case(seed=0):
+    rng = np.random.default_rng(seed)
+    vp = np.zeros((FS_NZI, FS_NXI))
+    b = np.linspace(0, FS_NZI, 4).astype(int)
+    for v, z0, z1 in zip((1500.0, 2500.0, 3500.0), b[:-1], b[1:]):
+        vp[z0:z1] = v
+    zz, xx = np.mgrid[0:FS_NZI, 0:FS_NXI]
+    cz, cx = rng.uniform(0.3, 0.7) * FS_NZI, rng.uniform(0.3, 0.7) * FS_NXI
+    vp += 300.0 * np.exp(-((zz - cz) ** 2 + (xx - cx) ** 2) / (2 * 10.0 ** 2))
+    vp = np.pad(vp, WIDTH, mode="edge")
+    sources = [[(WIDTH + 2, WIDTH + 16 + 32 * k)] for k in range(FS_SHOTS)]
+    receivers = [([WIDTH + 2] * FS_NXI, list(range(WIDTH, WIDTH + FS_NXI)))] * FS_SHOTS
+    return vp, sources, receivers
+
+
+def cpu_forward_rate(vp, d, wav, sources, receivers, procs=None):
+    """The oracle port (numpy fp32) of the same forward, one process per shot."""
+    import multiprocessing as mp
+    from oracle import baseline
+    procs = max(1, min(procs or os.cpu_count() or 1, len(sources)))
+    jobs = [(vp, d, DT, H, wav, sources[i], receivers[i], FS_ORDER) for i in range(len(sources))]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        pool.map(baseline.forward_one_shot, [(vp, d, DT, H, wav[:2], sources[0], receivers[0], FS_ORDER)] * procs)
+        t0 = time.perf_counter()
+        pool.map(baseline.forward_one_shot, jobs)
+        wall = time.perf_counter() - t0
+    return len(sources) * vp.size * len(wav) / wall / 1e9, wall, procs
+
+
+def bench_forward_small(args):
+    from oracle import fd2d
+    vp, sources, receivers = forward_small_case()
+    nz, nx = vp.shape
+    d = fd2d.pml_profile_2d((nz, nx), WIDTH).astype(np.float32)
+    wav = fd2d.ricker(FS_FM, DT, FS_NT, delay=int(1.0 / FS_FM / DT))
+    metric, unit = "Gpts/s fwd", "Gpts/s"
+    config = {"workload": "acoustic_forward_128x256_pml50_o4_nt1000_8shots", "grid": [nz, nx], "shots": FS_SHOTS,
+              "nt": FS_NT, "order": FS_ORDER, "l2": "L2-resident (2.6 MB per field); not an HBM-bound case"}
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return 0
+        vals = [cpu_forward_rate(vp, d, wav, sources, receivers) for _ in range(max(1, args.steps))]
+        rate = float(np.median([v[0] for v in vals]))
+        cb = {"value": rate, "unit": unit, "cores": vals[-1][2], "kind": "port",
+              "sample": f"the whole workload ({FS_SHOTS} shots x {FS_NT} steps), numpy fp32, one process per shot"}
+        print(json.dumps({"impl": "reference", "metric": metric, "value": rate, "unit": unit, "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": FS_SHOTS * nz * nx * FS_NT / (rate * 1e9) * 1e3,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                          "data": "synthetic", "config": config, "cpu_baseline": cb,
+                          "e2e": {"value": rate, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return 0
+    import torch
+    from seistorch_gb300 import _native, build_model, engine
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _native.load(build_if_missing=False)
+    prop = engine.AcousticPropagator(nz, nx, DT, H, FS_ORDER, "pml", WIDTH, False, dev)
+    acq = engine.Acquisition(nz, nx, sources, receivers, wav, dev)
+    vpt = torch.tensor(vp, dtype=torch.float32, device=dev)
+    dt_ = torch.tensor(d, device=dev)
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    with torch.no_grad():
+        for _ in range(max(3, args.warmup)):
+            engine.acoustic_loop(vpt, prop, dt_, acq)
+        torch.cuda.synchronize()
+        with ClockSampler(0) as clocks:
+            t0, t1 = ev(), ev()
+            t0.record(stream)
+            for _ in range(args.steps):
+                engine.acoustic_loop(vpt, prop, dt_, acq)
+            t1.record(stream)
+            torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    pts = FS_SHOTS * nz * nx * FS_NT
+    peak, kind = measured_peaks()
+    gbs = (FS_SHOTS * nz * nx * BYTES_FWD + nz * nx * BYTES_COEF) * FS_NT / (ms * 1e-3) / 1e9
+    # end to end: build_model -> WaveRNN.forward with the model copied in and the records copied out
+    cfg = {"equation": "acoustic", "dtype": "float32",
+           "geom": {"dt": DT, "h": H, "nt": FS_NT, "boundary": {"type": "pml", "width": WIDTH}, "multiple": False,
+                    "source_type": ["h1"], "receiver_type": ["h1"], "spatial_order": FS_ORDER}}
+    _, model = build_model(cfg, device=dev, mode="forward", models={"vp": vp[WIDTH:-WIDTH, WIDTH:-WIDTH]})
+    srcs = [[x - WIDTH, z - WIDTH] for [(z, x)] in sources]
+    recs = [[[x - WIDTH for x in xs], [z - WIDTH for z in zs]] for zs, xs in receivers]
+    model.reset_geom(list(range(FS_SHOTS)), srcs, recs, cfg)
+    vp_host = torch.tensor(vp, dtype=torch.float32).pin_memory()
+    wav_host = torch.tensor(wav)[None].pin_memory()
+    rec_host = torch.empty(FS_SHOTS, FS_NT, FS_NXI).pin_memory()
+    param = model.cell.geom.vp
+
+    def api_step():
+        with torch.no_grad():
+            param.copy_(vp_host.to(dev, non_blocking=True))
+            y = model(wav_host.to(dev, non_blocking=True))
+            rec_host.copy_(torch.stack([t[..., 0] for t in y.data]), non_blocking=True)
+
+    for _ in range(max(3, args.warmup)):
+        api_step()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        api_step()
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - w0) / args.steps
+    line = {"metric": metric, "value": pts / (ms * 1e-3) / 1e9, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+            "shots_per_s": FS_SHOTS / (ms * 1e-3),
+            "roofline": {"kernel": "acoustic_fwd_tile_kernel", "bound": "hbm", "achieved": gbs, "peak": peak,
+                         "peak_kind": kind, "unit": "GB/s", "frac": gbs / peak, "traffic": None,
+                         "note": "working set in L2: the HBM bound does not apply; shown for comparison"},
+            "gpu_launches": args.steps * (FS_NT + 1), "clocks": clocks.summary(),
+            "e2e": {"value": pts / wall / 1e9, "unit": unit, "h2d_bytes_per_step": int(vp_host.numel() * 4 +
+                                                                                          wav_host.numel() * 4),
+                    "d2h_bytes_per_step": int(rec_host.numel() * 4), "ms_per_step": wall * 1e3,
+                    "api": "build_model -> WaveRNN.forward (records to host)"}}
+    if not args.no_cpu_baseline:
+        rate, wall_c, procs = cpu_forward_rate(vp, d, wav, sources, receivers)
+        line["cpu_baseline"] = {"value": rate, "unit": unit, "cores": procs, "kind": "port",
+                                "sample": f"the whole workload ({FS_SHOTS} shots x {FS_NT} steps), numpy fp32, "
+                                          f"one process per shot ({wall_c:.1f} s wall)"}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------- HABC ---
+# acoustic_habc gradient: the headline grid, model and acquisition (400 x
+# 1000 interior + 50-cell hybrid absorbing boundary, dx = 10 m, dt = 1 ms,
+# 3000 steps, 64 shots, 8 Hz, 1000 receivers on row 2), 2nd order (the
+# reference's default) or 4th.  One step = forward + L2 residual against data
+# from the true model + HABC adjoint (tiled interior + frame kernels) + dJ/dvp.
+HB_BYTES_FWD, HB_BYTES_REV, HB_BYTES_COEF = 12, 32, 8
+
+
+def bench_habc(args):
+    import torch
+    from seistorch_gb300 import _native, engine
+    from seistorch_gb300.habc import generate_habc_coefficients_2d
+    from seistorch_gb300.postprocess import L2
+    from seistorch_gb300.utils import ricker_wave
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm is timed on the acoustic "
+                          "gradient workload only"}))
+        return 0
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _native.load(build_if_missing=False)
+    order = args.order or 2
+    nt, shots = args.nt, args.shots
+    vp_true, vp_init = make_models(seed=0)
+    nz, nx = vp_true.shape
+    b = generate_habc_coefficients_2d((nz, nx), WIDTH).to(device=dev, dtype=torch.float32)
+    wav = ricker_wave(FM, DT, nt, delay=int(1.2 / FM / DT), dtype="numpy")
+    sources, receivers = acquisition_lists()
+    sources, receivers = sources[:shots], receivers[:shots]
+    prop = engine.AcousticPropagator(nz, nx, DT, H, order, "habc", WIDTH, False, dev)
+    acq = engine.Acquisition(nz, nx, sources, receivers, wav, dev)
+    t = lambda a, rg=False: torch.tensor(a, dtype=torch.float32, device=dev, requires_grad=rg)
+    ck = engine.default_ckpt_every(nt)
+    with torch.no_grad():
+        obs, _ = engine.acoustic_loop(t(vp_true), prop, b, acq)
+    obs = obs.contiguous()
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def step(timing=None):
+        vp = t(vp_init, True)
+        e0, e1, e2 = ev(), ev(), ev()
+        e0.record(stream)
+        r, _ = engine.acoustic_loop(vp, prop, b, acq, False, ck)
+        e1.record(stream)
+        loss = L2()(r, obs)
+        loss.backward()
+        e2.record(stream)
+        if timing is not None:
+            timing.append((e0, e1, e2))
+        return loss
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    timing = []
+    with ClockSampler(0) as clocks:
+        t0, t1 = ev(), ev()
+        t0.record(stream)
+        for _ in range(args.steps):
+            step(timing)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    fwd_ms = float(np.median([a.elapsed_time(c) for a, c, _ in timing]))
+    rev_ms = float(np.median([c.elapsed_time(e) for _, c, e in timing]))
+    npts = nz * nx
+    rev_bytes = shots * npts * HB_BYTES_REV + npts * HB_BYTES_COEF
+    fwd_bytes = shots * npts * HB_BYTES_FWD + npts * HB_BYTES_COEF
+    peak, kind = measured_peaks()
+    rev_gbs = rev_bytes / (rev_ms / (nt - 1) * 1e-3) / 1e9
+    fwd_gbs = fwd_bytes / (fwd_ms / nt * 1e-3) / 1e9
+    line = {"metric": "Gpts/s fwd+adjoint", "value": shots * npts * nt / (ms * 1e-3) / 1e9, "unit": "Gpts/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"acoustic_habc_l2_gradient_{NZI}x{NXI}_habc{WIDTH}_o{order}_nt{nt}_{shots}shots",
+                       "grid": [nz, nx], "shots": shots, "nt": nt, "order": order, "ckpt_every": ck,
+                       "l2": "inputs larger than L2 (141 MB per field)"},
+            "shots_per_s": shots / (ms * 1e-3), "phases_ms": {"forward": fwd_ms, "adjoint": rev_ms},
+            "roofline": {"kernel": "habc_bwd_interior_kernel + habc_bwd_kernel", "bound": "hbm", "achieved": rev_gbs,
+                         "peak": peak, "peak_kind": kind, "unit": "GB/s", "frac": rev_gbs / peak, "traffic": None,
+                         "bytes_per_launch": rev_bytes, "launch_ms": rev_ms / (nt - 1)},
+            "roofline_forward": {"kernel": "acoustic_fwd_tile_kernel<HABC>", "achieved": fwd_gbs,
+                                 "frac": fwd_gbs / peak, "unit": "GB/s", "launch_ms": fwd_ms / nt},
+            # per step: NT forward, 2 (NT-1) reverse, coefficients, misfit, reduction
+            "gpu_launches": args.steps * (nt + 2 * (nt - 1) + 3), "clocks": clocks.summary()}
+    print(json.dumps(line))
+    return 0
 
 
 # ------------------------------------------------------------ elastic ---
@@ -976,7 +1213,8 @@ def bench_learned(args):
     _native.load(build_if_missing=False)
     log = lambda m: print(m, file=sys.stderr, flush=True)
     t0 = time.perf_counter()
-    train_sv = fwi.Survey(256, 512, shots=8, nt=1500, fm=8.0, device=dev)
+    # pairs on the inversion's own survey (32 shots, 3000 steps, 8 Hz)
+    train_sv = fwi.Survey(256, 512, shots=32, nt=3000, fm=8.0, device=dev)
     X, Y = fwi.make_pairs(args.pairs, train_sv, seed=0, log=log)
     torch.cuda.synchronize()
     t_pairs = time.perf_counter() - t0
@@ -1001,7 +1239,7 @@ def bench_learned(args):
     if args.save_net:
         np.savez(args.save_net, **net.state_dict())
     # held-out inversion
-    sv = fwi.Survey(256, 512, shots=32, nt=3000, fm=8.0, device=dev)
+    sv = train_sv
     rng = np.random.default_rng(12345)
     vt = fwi.random_model(rng, 256, 512)
     v0 = fwi.smooth(vt)
@@ -1012,6 +1250,7 @@ def bench_learned(args):
     t_plain = plain["time"][-1]
     reach = next((t for m, t in zip(learned["misfit"], learned["time"]) if m <= target), None)
     ratio = reach / t_plain if reach is not None else None
+    # model error relative to the starting model's (1 = no better than the start)
     model_err = lambda r: float(torch.linalg.norm(r["model"] - torch.as_tensor(vt, device=dev, dtype=torch.float32))
                                 / np.linalg.norm(vt - v0))
     peak = None
@@ -1024,7 +1263,10 @@ def bench_learned(args):
             "higher_is_better": False, "n_gpus": 1, "steps": 1, "warmup": 0, "vs_baseline": None,
             "dtype": "bf16 weights / fp32 accumulate (network), f32 (solver)", "data": "synthetic",
             "config": {"workload": "learned_preconditioner_fwi_256x512_32shots_nt3000", "pairs": args.pairs,
-                       "pair_survey": "8 shots x 1500 steps", "epochs": args.epochs, "iters": args.iters,
+                       "pair_survey": "the inversion's: 32 shots x 3000 steps, 8 Hz",
+                       "start": f"true model Gaussian-smoothed, sigma {fwi.START_SIGMA:g} cells",
+                       "plain_method": "illumination-preconditioned PR conjugate gradient + parabolic line search",
+                       "epochs": args.epochs, "iters": args.iters,
                        "params": n_params()},
             "plain": {"final_misfit": target, "wall_s": t_plain, "misfit": plain["misfit"],
                       "time": plain["time"], "model_error": model_err(plain)},

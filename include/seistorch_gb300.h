@@ -181,6 +181,8 @@ typedef struct {
   const float *born_u; /* Born: the background field U_n of the m k L(U) source   */
   float *born_gu;      /* Born: out dJ/d(background U_n) through the source       */
   float *born_gm;      /* Born: out dJ/dm (plane)                                 */
+  float *wi_out;       /* out: each cell's interior share wi = 1 - b sum of its
+                          sides' shares (plane), or NULL                          */
 } sgb_habc_vjp_io;
 
 /* Vector-Jacobian product of one step of the HABC family (autograd of
@@ -249,6 +251,35 @@ int sgb_acoustic_backward_noalloc(const sgb_grid *grid, const sgb_acoustic_model
                                   const sgb_acquisition *acq, const sgb_bs_store *bs,
                                   float *const ubuf[3], int32_t ucur, int32_t uprev, float *grad_vp,
                                   sgb_stream_t stream);
+
+/* ---------------------------------------------------- viscoacoustic --- */
+
+/* The viscoacoustic equation with the HABC (vacoustic_habc.py:74-115):
+ *   y = HABC(2U - U- + kv L(U) + a_neg K(U - U-)) + sources,
+ * K(x) = real(ifft2(|k| fft2(x))) over the padded grid, |k| =
+ * sqrt(fz^2 + fx^2) with fz / fx = fftfreq(nz / nx, h), kv =
+ * vp^2 dt^2 (1 - (1 - sqrt(Q^2 + 1)) / Q^2) / h^2 and a_neg = -dt t vp / 2
+ * with the reference's t(Q, omega) (the caller computes both planes;
+ * model->coef = [g = 2][kv]).  Scratch (caller-allocated):
+ * sgb_vacoustic_work_size floats of complex work and twiddles. */
+int sgb_vacoustic_work_size(const sgb_grid *grid, int64_t *work_floats, int64_t *tw_floats);
+
+/* out[b] = post * K(pre * (u1[b] - u2[b])) for every shot; pre, u2, post may
+ * be NULL (1, 0, 1).  Two shots share one complex transform (K is real and
+ * even); mixed-radix transforms, nz, nx <= 8192.  out must not alias u1/u2. */
+int sgb_vacoustic_kterm(const sgb_grid *grid, const float *pre, const float *u1, const float *u2,
+                        const float *post, float *out, float *work, float *tw, sgb_stream_t stream);
+
+/* One step of vacoustic_habc._time_step (no sources): unext = step(u, um);
+ * extra receives a_neg K(u - um). */
+int sgb_vacoustic_step(const sgb_grid *grid, const sgb_acoustic_model *model, const float *a_neg, const float *u,
+                       const float *um, float *unext, float *extra, float *work, float *tw, sgb_stream_t stream);
+
+/* Whole forward loop of vacoustic_habc (records; as sgb_acoustic_forward
+ * with the damping term; no boundary store).  extra: one field of scratch. */
+int sgb_vacoustic_forward(const sgb_grid *grid, const sgb_acoustic_model *model, const float *a_neg,
+                          const sgb_acquisition *acq, float *const buf[3], float *extra, float *work, float *tw,
+                          int32_t *cur_out, int32_t *prev_out, sgb_stream_t stream);
 
 /* ---------------------------------------------------------------- VTI --- */
 
@@ -501,6 +532,16 @@ int sgb_grad_smooth(int32_t nz, int32_t nx, int32_t pitch, const float *weights_
  * uint32. */
 int sgb_sd_step(int64_t n, float *param, const float *grad, float lr, int32_t clamp, float lo, float hi,
                 uint32_t *scratch, sgb_stream_t stream);
+
+/* Non-linear conjugate-gradient step (optimizer.py:144-224, class Cg): d =
+ * grad clamped to [lo, hi] when clamp != 0 (the caller's clip_value
+ * quantiles); beta = (d - prev_grad) . d / |prev_grad|^2 (beta_type 0,
+ * Polak-Ribiere) or |d|^2 / |prev_grad|^2 (1, Fletcher-Reeves), 0 while
+ * prev_grad is all zero; direction = -d + beta direction; param += lr *
+ * direction / max|direction|; prev_grad = d.  prev_grad starts at zeros.
+ * scratch: 4 device doubles.  No host synchronisation. */
+int sgb_ncg_step(int64_t n, float *param, const float *grad, float *prev_grad, float *direction, float lr,
+                 int32_t beta_type, int32_t clamp, float lo, float hi, double *scratch, sgb_stream_t stream);
 
 /* Zero-phase IIR filtering of records (scipy.signal.filtfilt with its
  * default odd padding, as SeisSignal.filter applies it to each shot,

@@ -32,6 +32,15 @@ def _one_shot(args):
     return time.perf_counter() - t0
 
 
+def forward_one_shot(args):
+    """Forward modelling of one shot (records), the oracle in float32."""
+    vp, d, dt, h, wavelet, src, rec, order = args
+    from oracle import fd2d
+    t0 = time.perf_counter()
+    fd2d.forward("acoustic", {"vp": vp}, d, dt, h, wavelet, [src], [rec], order=order, dtype=np.float32)
+    return time.perf_counter() - t0
+
+
 def acoustic_gradient_rate(vp, d, dt, h, wavelet, sources, receivers, order, nsteps, procs=None):
     """Run ``procs`` shots of ``nsteps`` steps in parallel processes.
 

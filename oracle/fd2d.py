@@ -268,6 +268,34 @@ def born_habc_step(vp, m, h1, h2, sh1, sh2, dt, h, b, order, multiple=False, dty
     return p0, np.asarray(h1, dtype), s0, np.asarray(sh1, dtype)
 
 
+def vacoustic_habc_step(vp, Q, h1, h2, dt, h, b, order=2, multiple=False, omega=16.5, dtype=np.float64):
+    """Viscoacoustic step with HABC (vacoustic_habc.py:74-115):
+    y = 2 h1 - h2 + vp^2 dt^2 (1 - (1 - sqrt(Q^2 + 1)) / Q^2) lap(h1)
+        - (dt^2 t vp / 2) real(ifft2(|k| fft2((h1 - h2) / dt))),
+    |k| = sqrt(kz^2 + kx^2) from fftfreq(nz, h) and fftfreq(nx, h); t from Q
+    and omega: t_sigma = (sqrt(1 + Q^-2) - 1/Q) / omega, t_eps =
+    1 / (omega^2 t_sigma), t = t_eps / (t_sigma - 1e-8) - 1; then the HABC
+    blend.  Returns (y, h1)."""
+    vp = np.asarray(vp, dtype)
+    Q = np.asarray(Q, dtype)
+    h1 = np.asarray(h1, dtype)
+    h2 = np.asarray(h2, dtype)
+    dt_ = dtype(dt)
+    t_sigma = (np.sqrt(1 + Q ** -2) - Q ** -1) / omega
+    t_eps = 1.0 / (omega ** 2 * t_sigma)
+    t = t_eps / (t_sigma - 1e-8) - 1.0
+    lap = laplacian(h1, order, h, dtype)
+    y = 2 * h1 - h2 + vp ** 2 * dt_ ** 2 * (1 - (1 - np.sqrt(Q ** 2 + 1)) * Q ** -2) * lap
+    nz, nx = h1.shape[-2:]
+    kz, kx = np.meshgrid(np.fft.fftfreq(nz, d=h), np.fft.fftfreq(nx, d=h), indexing="ij")
+    k = np.sqrt(kz ** 2 + kx ** 2)
+    dy = (h1 - h2) / dt_
+    temp = np.real(np.fft.ifft2(k * np.fft.fft2(dy, axes=(-2, -1)), axes=(-2, -1)))
+    y = y - (dt_ ** 2 * t * vp / 2) * temp
+    y = habc_apply(y, h1, h2, vp, b, dt, h, 50, multiple, dtype)
+    return y, h1
+
+
 def second_difference(u, axis, h, dtype=np.float64):
     """Zero-padded 1-D second difference / h^2 along `axis` of (B, Nz, Nx)
     fields (convkernel.py kernelx / kernely at spatial order 2: [1, -2, 1])."""
@@ -381,11 +409,11 @@ def elastic_step(vp, vs, rho, vx, vz, txx, tzz, txz, dt, h, d, dtype=np.float64)
 
 WAVEFIELDS = {"acoustic": ["h1", "h2"], "acoustic_habc": ["h1", "h2"],
               "acoustic_lsrtm_habc": ["h1", "h2", "sh1", "sh2"], "vti_habc2": ["p1", "p2"],
-              "acoustic_rho_habc": ["h1", "h2"],
+              "acoustic_rho_habc": ["h1", "h2"], "vacoustic_habc": ["h1", "h2"],
               "elastic": ["vx", "vz", "txx", "tzz", "txz"]}
 MODEL_PARAMS = {"acoustic": ["vp"], "acoustic_habc": ["vp"], "acoustic_lsrtm_habc": ["vp", "m"],
                 "vti_habc2": ["vp", "epsilon", "delta"], "acoustic_rho_habc": ["vp", "rho"],
-                "elastic": ["vp", "vs", "rho"]}
+                "vacoustic_habc": ["vp", "Q"], "elastic": ["vp", "vs", "rho"]}
 
 
 def forward(equation, models, d, dt, h, wavelet, sources, receivers, *,
@@ -433,6 +461,10 @@ def forward(equation, models, d, dt, h, wavelet, sources, receivers, *,
             fields = dict(zip(names, out))
         elif equation == "acoustic_rho_habc":
             y, h1 = rho_habc_step(models["vp"], models["rho"], fields["h1"], fields["h2"], dt, h, d, multiple, dtype)
+            fields["h1"], fields["h2"] = y, h1
+        elif equation == "vacoustic_habc":
+            y, h1 = vacoustic_habc_step(models["vp"], models["Q"], fields["h1"], fields["h2"], dt, h, d, order,
+                                        multiple, dtype=dtype)
             fields["h1"], fields["h2"] = y, h1
         elif equation == "vti_habc2":
             y, p1 = vti_habc_step(models["vp"], models["epsilon"], models["delta"], fields["p1"], fields["p2"],

@@ -21,7 +21,7 @@ LIB_NAME = "libseistorch_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 SOURCES = ["acoustic.cu", "acoustic_stream.cu", "acoustic_stream_fwd.cu", "acoustic_stream_bwd.cu",
            "elastic.cu", "capi.cu", "capi_elastic.cu", "capi_batch.cu", "noalloc.cu",
-           "nn_gemm.cu", "nn_ops.cu", "capi_nn.cu", "habc_bwd.cu", "postproc.cu"]
+           "nn_gemm.cu", "nn_ops.cu", "capi_nn.cu", "habc_bwd.cu", "postproc.cu", "fft.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -94,7 +94,7 @@ class AcousticModel(ctypes.Structure):
 class HabcVjpIO(ctypes.Structure):
     _fields_ = [("u", c_ptr), ("um", c_ptr), ("gy", c_ptr), ("gu", c_ptr), ("gum", c_ptr), ("gparam", c_ptr),
                 ("gvp_oneway", c_ptr), ("kz", c_ptr), ("rho_c", c_ptr), ("born_m", c_ptr), ("born_u", c_ptr),
-                ("born_gu", c_ptr), ("born_gm", c_ptr)]
+                ("born_gu", c_ptr), ("born_gm", c_ptr), ("wi_out", c_ptr)]
 
 
 class BsStore(ctypes.Structure):
@@ -207,6 +207,17 @@ SIGNATURES = {
     "sgb_nn_adam": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_f32, c_f32, c_f32, c_f32, c_i32,
                                    c_f32, c_ptr]),
     "sgb_nn_mse": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr]),
+    "sgb_ncg_step": (ctypes.c_int, [ctypes.c_int64, c_ptr, c_ptr, c_ptr, c_ptr, c_f32, c_i32, c_i32, c_f32, c_f32,
+                                    c_ptr, c_ptr]),
+    "sgb_vacoustic_work_size": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(ctypes.c_int64),
+                                               ctypes.POINTER(ctypes.c_int64)]),
+    "sgb_vacoustic_kterm": (ctypes.c_int, [ctypes.POINTER(Grid), c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+                                           c_ptr]),
+    "sgb_vacoustic_step": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel), c_ptr, c_ptr,
+                                          c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr]),
+    "sgb_vacoustic_forward": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(AcousticModel), c_ptr,
+                                             ctypes.POINTER(Acquisition), PTR3, c_ptr, c_ptr, c_ptr,
+                                             ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_ptr]),
     "sgb_cfl_check": (ctypes.c_int, [c_i32, c_i32, c_f32, c_f32, c_f32, ctypes.POINTER(c_f32),
                                      ctypes.POINTER(c_f32)]),
     "sgb_debug_wait_probe": (ctypes.c_int, [ctypes.c_uint32, c_i32, c_ptr]),

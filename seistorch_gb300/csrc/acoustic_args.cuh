@@ -99,6 +99,19 @@ struct AcStreamArgs {
   const float* __restrict__ ring_src;
   float* __restrict__ ring_dst;
   int* status;
+  // HABC family (single-grid launches of the HABC instantiation only): the
+  // input field for strip neighbours outside the staged box, the blend
+  // (acoustic_habc.py:79-204), and the equation variants of AcStepArgs
+  const float* __restrict__ u;
+  const float* __restrict__ vp;
+  const float* __restrict__ hb;
+  float lamf, muf;
+  int hw, multiple;
+  const float* __restrict__ kz;
+  const float* __restrict__ rho_c;
+  const float* __restrict__ born_m;
+  float* __restrict__ born_out;
+  const float* __restrict__ born_in;
 };
 
 // Forward steps of up to MAXG grids in one launch (tiles numbered group

@@ -2,9 +2,51 @@
 // stream_common.cuh): u+ = g (u - u-) + u- + k L(u) (acoustic.py:73-86),
 // with source injection (source.py:47-57), receiver sampling (probe.py:42-44),
 // the illumination sum and the saving of the input's boundary ring fused in.
+#include "habc_blend.cuh"
 #include "stream_common.cuh"
 
 namespace sgb {
+
+// Strip neighbours of the HABC blend: the current field from the staged
+// stencil box where the cell lies in it, else from global memory; the
+// previous field from global memory (L2).
+struct StageField {
+  const float* su;  // staged box: rows [zt, zt + rows), columns [xt, xt + w)
+  int zt, xt, rows, w;
+  const float* u;
+  const float* um;
+  long long base;
+  int pitch;
+  __device__ __forceinline__ float U(int z, int x) const {
+    const int r = z - zt, c = x - xt;
+    if (r >= 0 && r < rows && c >= 0 && c < w) return su[r * w + c];
+    return __ldg(u + base + (long long)z * pitch + x);
+  }
+  __device__ __forceinline__ float P(int z, int x) const { return __ldg(um + base + (long long)z * pitch + x); }
+};
+
+// Cross-stencil x and z parts (1-D second differences, centre -2 sum c) of
+// the 4 columns of a lane, as lap_row.
+template <int R>
+__device__ __forceinline__ void lap_row_xz(const float4 (&win)[2 * R + 1], const float* srow, int lane,
+                                           const FdWeights& w, float4& Lx, float4& Lz) {
+  const float4 l = lds4(srow + Row<R>::LO - 4 + 4 * lane);
+  const float4 r = lds4(srow + Row<R>::LO + 4 + 4 * lane);
+  const float4 c = win[R];
+  const float a[12] = {l.x, l.y, l.z, l.w, c.x, c.y, c.z, c.w, r.x, r.y, r.z, r.w};
+  const float c0 = 0.5f * w.c[0];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    float sx = c0 * a[4 + m], sz = c0 * a[4 + m];
+#pragma unroll
+    for (int j = 1; j <= R; ++j) {
+      sx = fmaf(w.c[j], a[4 + m + j] + a[4 + m - j], sx);
+      sz = fmaf(w.c[j], comp(win[R + j], m) + comp(win[R - j], m), sz);
+    }
+    set_comp(Lx, m, sx);
+    set_comp(Lz, m, sz);
+  }
+}
 
 // PT: the previous field travels through the TMA stage (prefetched S-1
 // tiles ahead) instead of a global load issued before the stage wait.
@@ -57,7 +99,7 @@ struct FwdMany {
 
 // per group: map_u = U_n [nshots][nz][nx], box {W, TZ+2R, 1};
 //            map_um = U_{n-1}, box {128, TZ, 1} (used when PT)
-template <int R, int TZ, int NWP, int S, bool PT, int SB, class P>
+template <int R, int TZ, int NWP, int S, bool PT, int SB, class P, bool HB = false>
 __device__ __forceinline__ void fwd_tiles(const P& prov) {
   static_assert(SB == 1 || PT, "several shots per tile need the previous field in the stage");
   using Lay = FwdTileLayout<R, TZ, S, PT, SB>;
@@ -152,13 +194,60 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
         const int lr = lr0 + i;
         const int z = zw + i;
         win[2 * R] = lds4(su + (lr + 2 * R) * UW + LO + 4 * lane);
-        const float4 L = lap_row<R>(win, su + (lr + R) * UW, lane, a.w);
+        const float* srow = su + (lr + R) * UW;
         const float4 c = win[R];
         float4 y;
-        y.x = fmaf(vk[i].x, L.x, fmaf(vg[i].x, c.x - vm[i].x, vm[i].x));
-        y.y = fmaf(vk[i].y, L.y, fmaf(vg[i].y, c.y - vm[i].y, vm[i].y));
-        y.z = fmaf(vk[i].z, L.z, fmaf(vg[i].z, c.z - vm[i].z, vm[i].z));
-        y.w = fmaf(vk[i].w, L.w, fmaf(vg[i].w, c.w - vm[i].w, vm[i].w));
+        if (HB && R == 1 && a.rho_c != nullptr) {  // variable density: g (u - u-) + u- + C D(u)
+          const long long po = (long long)z * a.pitch + x, pl = (long long)a.nz * a.pitch;
+          const bool in = xin && z < a.nz;
+          const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 C4 = in ? ldg4(a.rho_c + po) : z4, bxp = in ? ldg4(a.rho_c + pl + po) : z4;
+          const float4 bxn = in ? ldg4(a.rho_c + 2 * pl + po) : z4, bzp = in ? ldg4(a.rho_c + 3 * pl + po) : z4;
+          const float4 bzn = in ? ldg4(a.rho_c + 4 * pl + po) : z4;
+          const float xs[6] = {srow[LO - 1 + 4 * lane], c.x, c.y, c.z, c.w, srow[LO + 4 + 4 * lane]};
+#pragma unroll
+          for (int m = 0; m < 4; ++m) {
+            const float cc = xs[m + 1];
+            const float D = comp(bxp, m) * (xs[m + 2] - cc) - comp(bxn, m) * (cc - xs[m]) +
+                            comp(bzp, m) * (comp(win[R + 1], m) - cc) - comp(bzn, m) * (cc - comp(win[R - 1], m));
+            set_comp(y, m, fmaf(comp(C4, m), D, fmaf(comp(vg[i], m), cc - comp(vm[i], m), comp(vm[i], m))));
+          }
+        } else if (HB && a.kz != nullptr) {  // VTI: k Lx + kz Lz
+          float4 Lx, Lz;
+          lap_row_xz<R>(win, srow, lane, a.w, Lx, Lz);
+          const float4 vz = (xin && z < a.nz) ? ldg4(a.kz + (long long)z * a.pitch + x) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int m = 0; m < 4; ++m)
+            set_comp(y, m, fmaf(comp(vk[i], m), comp(Lx, m), fmaf(comp(vz, m), comp(Lz, m),
+                                                                 fmaf(comp(vg[i], m), comp(c, m) - comp(vm[i], m),
+                                                                      comp(vm[i], m)))));
+        } else {
+          const float4 L = lap_row<R>(win, srow, lane, a.w);
+          y.x = fmaf(vk[i].x, L.x, fmaf(vg[i].x, c.x - vm[i].x, vm[i].x));
+          y.y = fmaf(vk[i].y, L.y, fmaf(vg[i].y, c.y - vm[i].y, vm[i].y));
+          y.z = fmaf(vk[i].z, L.z, fmaf(vg[i].z, c.z - vm[i].z, vm[i].z));
+          y.w = fmaf(vk[i].w, L.w, fmaf(vg[i].w, c.w - vm[i].w, vm[i].w));
+          if (HB && (a.born_out != nullptr || a.born_in != nullptr) && xin && z < a.nz) {
+            const long long po = (long long)z * a.pitch + x;
+            if (a.born_out != nullptr) {  // m k L(u): the scattered field's source (Born)
+              const float4 mm = ldg4(a.born_m + po);
+              *reinterpret_cast<float4*>(a.born_out + fbase + po) =
+                  make_float4(mm.x * (vk[i].x * L.x), mm.y * (vk[i].y * L.y), mm.z * (vk[i].z * L.z),
+                              mm.w * (vk[i].w * L.w));
+            }
+            if (a.born_in != nullptr) {
+              const float4 sb4 = ldg4(a.born_in + fbase + po);
+              y = make_float4(y.x + sb4.x, y.y + sb4.y, y.z + sb4.z, y.w + sb4.w);
+            }
+          }
+        }
+        if (HB && z < a.nz && xin && (z < a.hw || z >= a.nz - a.hw || x < a.hw || x + 3 >= a.nx - a.hw)) {
+          // the one-way blend on strip cells; one copy of its code, not unrolled
+          const StageField T{su, g.z0 - R, g.x0 - LO, TZ + 2 * R, UW, a.u, a.um, fbase, a.pitch};
+#pragma unroll 1
+          for (int m = 0; m < 4; ++m)
+            if (x + m < a.nx) set_comp(y, m, habc_point(T, a, z, x + m, comp(y, m)));
+        }
         if (src.mask) apply_sources(src, i, lane, 1.f, y);
         if (z < a.nz && xin) {
           *reinterpret_cast<float4*>(outp) = y;
@@ -198,11 +287,11 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
       if ((int)blockIdx.x + q * G < ntiles) mbar_wait(&bars[q % S], (q / S) & 1, nullptr);
 }
 
-template <int R, int TZ, int NWP, int S, bool PT, int SB>
+template <int R, int TZ, int NWP, int S, bool PT, int SB, bool HB = false>
 __global__ void __launch_bounds__(32 * NWP) acoustic_fwd_tile_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                                      const __grid_constant__ CUtensorMap tm_um,
                                                                      const AcStreamArgs a) {
-  fwd_tiles<R, TZ, NWP, S, PT, SB>(FwdOne<SB>{&tm_u, &tm_um, a});
+  fwd_tiles<R, TZ, NWP, S, PT, SB, FwdOne<SB>, HB>(FwdOne<SB>{&tm_u, &tm_um, a});
   // the input field's boundary ring for the adjoint, spread over the CTAs'
   // tails (the input is read-only in this launch)
   if (a.ring_dst != nullptr)
@@ -225,13 +314,13 @@ static const FwdCfg FWD_TILE_CFGS[] = {{16, 4, 3, 1}, {16, 4, 3, 1}, {8, 4, 4, 1
 // Launches the variant on batch b; with s == nullptr and prepare_only it
 // only sets the kernel's shared-memory attribute (done once per variant, and
 // before any stream capture).
-template <int R, int TZ, int NWP, int S, bool PT, int MAXG, int SB = 1>
+template <int R, int TZ, int NWP, int S, bool PT, int MAXG, int SB = 1, bool HB = false>
 static cudaError_t fwd_tile_t(const AcFwdBatch<MAXG>& b, cudaStream_t s, bool prepare_only) {
   using Lay = FwdTileLayout<R, TZ, S, PT, MAXG == 1 ? SB : 1>;
   const size_t smem = Lay::BYTES + 128;  // + alignment slack
   static int blocks = 0;
   if constexpr (MAXG == 1) {
-    auto kern = acoustic_fwd_tile_kernel<R, TZ, NWP, S, PT, SB>;
+    auto kern = acoustic_fwd_tile_kernel<R, TZ, NWP, S, PT, SB, HB>;
     if (blocks == 0) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
@@ -285,7 +374,13 @@ int fwd_tile_rows() { return FWD_TILE_CFGS[g_fwd_cfg].tz; }
 int fwd_tile_shots() { return FWD_TILE_CFGS[g_fwd_cfg].sb; }
 int stencil_box_width(int R) { return (R % 2 == 0) ? TX + 8 : TX + 16; }
 
-cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s) {
+// The HABC family's forward: one variant (HT-row tiles, 4 warps, HS stages,
+// previous field by global loads, which the blend's strip neighbours share).
+constexpr int HT = 8, HS = 4;
+int habc_tile_rows() { return HT; }
+
+cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s,
+                                       bool habc) {
   AcFwdBatch<1> b;
   b.tm_u[0] = maps[0];
   b.tm_um[0] = maps[1];
@@ -293,7 +388,14 @@ cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcS
   b.ngroups = 1;
   b.tile0[0] = 0;
   b.tile0[1] = a.nshots * a.ntx * a.nzc;
-  return fwd_dispatch<1>(R, b, s, false);
+  if (!habc) return fwd_dispatch<1>(R, b, s, false);
+  switch (R) {
+    case 1: return fwd_tile_t<1, HT, 4, HS, false, 1, 1, true>(b, s, false);
+    case 2: return fwd_tile_t<2, HT, 4, HS, false, 1, 1, true>(b, s, false);
+    case 3: return fwd_tile_t<3, HT, 4, HS, false, 1, 1, true>(b, s, false);
+    case 4: return fwd_tile_t<4, HT, 4, HS, false, 1, 1, true>(b, s, false);
+  }
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_acoustic_fwd_batch(int R, const AcFwdBatch<MAX_BATCH_GROUPS>& b, cudaStream_t s) {

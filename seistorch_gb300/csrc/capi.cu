@@ -67,7 +67,21 @@ cudaError_t launch_acoustic_grad_reduce(const sgb_grid& gr, const float* grad_sh
                                         const Ring& ring, float* grad_vp, cudaStream_t s);
 int pick_tz(int nz, int nx, int nshots, int tz_max);
 // streaming kernels in acoustic_stream.cu
-cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s);
+cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s,
+                                       bool habc = false);
+int habc_tile_rows();
+int vacoustic_kterm(const sgb_grid& g, const float* pre, const float* u1, const float* u2, const float* post,
+                    float* out, float* work, float* tw, cudaStream_t s);
+
+// Viscoacoustic extras of a forward loop: before each step the damping term
+// extra = a_neg * K(U_n - U_{n-1}) is formed and added to the interior
+// update (vacoustic_habc.py:86-111).
+struct VacParams {
+  const float* a_neg;
+  float* extra;
+  float* work;
+  float* tw;
+};
 cudaError_t launch_acoustic_bwd_stream(int R, const CUtensorMap* maps, const AcBwdStreamArgs& a,
                                        cudaStream_t s);
 int field_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int nshots, int boxw, int rb,
@@ -168,7 +182,43 @@ AcStepArgs base_step_args(const sgb_grid* g, const sgb_acoustic_model* m) {
 
 int acoustic_forward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                           float* const buf[3], float* illum, const sgb_bs_store* bs, int32_t* cur_out,
-                          int32_t* prev_out, const float* kz, cudaStream_t s, const float* rho_c = nullptr);
+                          int32_t* prev_out, const float* kz, cudaStream_t s, const float* rho_c = nullptr,
+                          const VacParams* vac = nullptr);
+
+// Arguments of the TMA tile pipeline from those of the tile kernel.
+void fill_stream_args(AcStreamArgs& sa, const AcStepArgs& a, const sgb_acquisition* acq, int tzr) {
+  sa.nz = a.nz; sa.nx = a.nx; sa.pitch = a.pitch; sa.nshots = a.nshots; sa.ntx = a.ntx;
+  sa.zc = tzr;
+  sa.nzc = (a.nz + tzr - 1) / tzr;
+  sa.nseg = sa.nzc;
+  sa.tpu = 1;
+  sa.g = a.g;
+  sa.k = a.k;
+  sa.src_zr = acq->src_zr;
+  sa.rec_zr = acq->rec_zr;
+  sa.sstride = a.sstride;
+  sa.w = a.w;
+  sa.src_ptr = a.src_ptr; sa.src_z = a.src_z; sa.src_x = a.src_x; sa.src_wrow = a.src_wrow;
+  sa.wavelet = a.wavelet; sa.nt = a.nt;
+  sa.rec_row_ptr = a.rec_row_ptr; sa.rec_x = a.rec_x; sa.rec_col = a.rec_col;
+  sa.nrec = a.nrec; sa.nch = a.nch;
+  sa.ring = a.ring;
+  sa.status = a.status;
+}
+
+void fill_stream_habc(AcStreamArgs& sa, const AcStepArgs& a) {
+  sa.vp = a.vp;
+  sa.hb = a.hb;
+  sa.lamf = a.lamf;
+  sa.muf = a.muf;
+  sa.hw = a.hw;
+  sa.multiple = a.multiple;
+  sa.kz = a.kz;
+  sa.rho_c = a.rho_c;
+  sa.born_m = a.born_m;
+  sa.born_out = a.born_out;
+  sa.born_in = a.born_in;
+}
 
 }  // namespace
 
@@ -345,13 +395,65 @@ int sgb_rho_forward(const sgb_grid* grid, const sgb_acoustic_model* model, const
                                rho_c);
 }
 
+int sgb_vacoustic_work_size(const sgb_grid* grid, int64_t* work_floats, int64_t* tw_floats) {
+  if (int e = check_grid(grid)) return e;
+  if (work_floats == nullptr || tw_floats == nullptr) return SGB_ERR_ARG;
+  *work_floats = 2LL * ((grid->nshots + 1) / 2) * grid->nz * grid->nx;
+  *tw_floats = 2LL * (grid->nz + grid->nx);
+  return SGB_OK;
+}
+
+int sgb_vacoustic_kterm(const sgb_grid* grid, const float* pre, const float* u1, const float* u2, const float* post,
+                        float* out, float* work, float* tw, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (u1 == nullptr || out == nullptr || work == nullptr || tw == nullptr) return SGB_ERR_ARG;
+  if (out == u1 || out == u2) return SGB_ERR_ARG;
+  return vacoustic_kterm(*grid, pre, u1, u2, post, out, work, tw, (cudaStream_t)stream);
+}
+
+int sgb_vacoustic_step(const sgb_grid* grid, const sgb_acoustic_model* model, const float* a_neg, const float* u,
+                       const float* um, float* unext, float* extra, float* work, float* tw, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (int e = check_model(grid, model)) return e;
+  if (model->boundary != 1) return SGB_ERR_UNSUPPORTED;
+  if (a_neg == nullptr || u == nullptr || um == nullptr || unext == nullptr || extra == nullptr || work == nullptr ||
+      tw == nullptr)
+    return SGB_ERR_ARG;
+  if (!aligned16(u) || !aligned16(um) || !aligned16(unext) || !aligned16(extra)) return SGB_ERR_ALIGN;
+  if (unext == u || unext == um || extra == u || extra == um || extra == unext) return SGB_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (int e = vacoustic_kterm(*grid, nullptr, u, um, a_neg, extra, work, tw, s)) return e;
+  AcStepArgs a = base_step_args(grid, model);
+  a.u = u;
+  a.um = um;
+  a.un = unext;
+  a.born_in = extra;
+  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 32);
+  SGB_CUDA_CHECK(launch_acoustic_fwd(model->order / 2, true, tz, a, s));
+  return SGB_OK;
+}
+
+int sgb_vacoustic_forward(const sgb_grid* grid, const sgb_acoustic_model* model, const float* a_neg,
+                          const sgb_acquisition* acq, float* const buf[3], float* extra, float* work, float* tw,
+                          int32_t* cur_out, int32_t* prev_out, sgb_stream_t stream) {
+  if (int e = check_grid(grid)) return e;
+  if (model == nullptr || a_neg == nullptr || extra == nullptr || work == nullptr || tw == nullptr)
+    return SGB_ERR_ARG;
+  if (model->boundary != 1) return SGB_ERR_UNSUPPORTED;  // vacoustic_habc: HABC
+  if (!aligned16(extra)) return SGB_ERR_ALIGN;
+  const VacParams vac{a_neg, extra, work, tw};
+  return acoustic_forward_impl(grid, model, acq, buf, nullptr, nullptr, cur_out, prev_out, nullptr,
+                               (cudaStream_t)stream, nullptr, &vac);
+}
+
 }  // extern "C"
 
 namespace {
 
 int acoustic_forward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                           float* const buf[3], float* illum, const sgb_bs_store* bs, int32_t* cur_out,
-                          int32_t* prev_out, const float* kz, cudaStream_t s, const float* rho_c) {
+                          int32_t* prev_out, const float* kz, cudaStream_t s, const float* rho_c,
+                          const VacParams* vac) {
   if (int e = check_grid(grid)) return e;
   if (int e = check_model(grid, model)) return e;
   if (int e = check_acq(grid, acq)) return e;
@@ -387,67 +489,44 @@ int acoustic_forward_impl(const sgb_grid* grid, const sgb_acoustic_model* model,
     if (a.ring.size != bs->ring_size) return SGB_ERR_SHAPE;
     if (bs->ckpt_every > 0 && bs->ckpt_store == nullptr) return SGB_ERR_ARG;
   }
-  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 32);
   const int R = model->order / 2;
   const bool habc = model->boundary == 1;
-  // PML: TMA tile pipeline; HABC: tile kernel (needs the strip neighbours)
+  // TMA tile pipeline for both boundaries (the HABC instantiation adds the
+  // strip blend and the equation variants)
   CUtensorMap mu[3], mum[3];
   AcStreamArgs sa;
   std::memset(&sa, 0, sizeof(sa));
-  if (!habc) {
-    const int tzr = fwd_tile_rows();
-    const int tsb = fwd_tile_shots();
-    const int bw = stencil_box_width(R);
-    for (int i = 0; i < 3; ++i)
-      if (field_map(&mu[i], buf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R, tsb) ||
-          field_map(&mum[i], buf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr, tsb))
-        return SGB_ERR_CUDA;
-    sa.nz = a.nz; sa.nx = a.nx; sa.pitch = a.pitch; sa.nshots = a.nshots; sa.ntx = a.ntx;
-    sa.zc = tzr;
-    sa.nzc = (grid->nz + tzr - 1) / tzr;
-    sa.nseg = sa.nzc;
-    sa.tpu = 1;
-    sa.g = a.g;
-    sa.k = a.k;
-    sa.src_zr = acq->src_zr;
-    sa.rec_zr = acq->rec_zr;
-    sa.sstride = a.sstride;
-    sa.w = a.w;
-    sa.src_ptr = a.src_ptr; sa.src_z = a.src_z; sa.src_x = a.src_x; sa.src_wrow = a.src_wrow;
-    sa.wavelet = a.wavelet; sa.nt = a.nt;
-    sa.rec_row_ptr = a.rec_row_ptr; sa.rec_x = a.rec_x; sa.rec_col = a.rec_col;
-    sa.nrec = a.nrec; sa.nch = a.nch;
-    sa.illum = illum;
-    sa.ring = a.ring;
-    sa.status = a.status;
-    if ((a.src_ptr != nullptr && acq->src_zr == nullptr) || (acq->records != nullptr && acq->rec_zr == nullptr))
-      return SGB_ERR_ARG;
-  }
+  const int tzr = habc ? habc_tile_rows() : fwd_tile_rows();
+  const int tsb = habc ? 1 : fwd_tile_shots();
+  const int bw = stencil_box_width(R);
+  for (int i = 0; i < 3; ++i)
+    if (field_map(&mu[i], buf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R, tsb) ||
+        field_map(&mum[i], buf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr, tsb))
+      return SGB_ERR_CUDA;
+  fill_stream_args(sa, a, acq, tzr);
+  sa.illum = illum;
+  if (habc) fill_stream_habc(sa, a);
+  if ((a.src_ptr != nullptr && acq->src_zr == nullptr) || (acq->records != nullptr && acq->rec_zr == nullptr))
+    return SGB_ERR_ARG;
   int cur = 0, prev = 1, nxt = 2;
   for (int t = 0; t < acq->nt; ++t) {
-    a.u = buf[cur];
-    a.um = buf[prev];
-    a.un = buf[nxt];
-    a.t = t;
-    a.records = acq->records ? acq->records + (long long)t * acq->nrec * acq->nch : nullptr;
-    if (habc) {
-      SGB_CUDA_CHECK(launch_acoustic_fwd(R, habc, tz, a, s));
-    } else {
-      sa.un = buf[nxt];
-      sa.um = buf[prev];
-      sa.t = t;
-      sa.records = a.records;
-      // the step saves the ring of its input U_t into slot t-1 (the adjoint
-      // reads the rings of U_1 .. U_{nt-2})
-      sa.ring_src = buf[cur];
-      sa.ring_dst = (bs != nullptr && t >= 1) ? bs->ring_store + (long long)(t - 1) * grid->nshots * a.ring.size
-                                              : nullptr;
-      const CUtensorMap maps[2] = {mu[cur], mum[prev]};
-      SGB_CUDA_CHECK(launch_acoustic_fwd_stream(R, maps, sa, s));
+    sa.un = buf[nxt];
+    sa.um = buf[prev];
+    sa.u = buf[cur];
+    sa.t = t;
+    sa.records = acq->records ? acq->records + (long long)t * acq->nrec * acq->nch : nullptr;
+    // the step saves the ring of its input U_t into slot t-1 (the adjoint
+    // reads the rings of U_1 .. U_{nt-2})
+    sa.ring_src = buf[cur];
+    sa.ring_dst = (bs != nullptr && t >= 1) ? bs->ring_store + (long long)(t - 1) * grid->nshots * a.ring.size
+                                            : nullptr;
+    const CUtensorMap maps[2] = {mu[cur], mum[prev]};
+    if (vac != nullptr) {
+      if (int e = vacoustic_kterm(*grid, nullptr, buf[cur], buf[prev], vac->a_neg, vac->extra, vac->work, vac->tw, s))
+        return e;
+      sa.born_in = vac->extra;
     }
-    if (habc && bs != nullptr)  // ring of U_{t+1} into slot t
-      SGB_CUDA_CHECK(launch_ring_copy(*grid, a.ring, buf[nxt], bs->ring_store + (long long)t * grid->nshots * a.ring.size,
-                                      false, s));
+    SGB_CUDA_CHECK(launch_acoustic_fwd_stream(R, maps, sa, s, habc));
     if (bs != nullptr && bs->ckpt_every > 0 && (t + 1) % bs->ckpt_every == 0) {
       float* slot = bs->ckpt_store + (long long)((t + 1) / bs->ckpt_every - 1) * 2 * field;
       SGB_CUDA_CHECK(cudaMemcpyAsync(slot, buf[nxt], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
@@ -514,33 +593,52 @@ int sgb_born_forward(const sgb_grid* grid, const sgb_acoustic_model* model, cons
     if (ring.size != bs->ring_size) return SGB_ERR_SHAPE;
     if (bs->ckpt_every > 0 && bs->ckpt_store == nullptr) return SGB_ERR_ARG;
   }
-  const int tz = pick_tz(grid->nz, grid->nx, grid->nshots, 32);
   const int R = model->order / 2;
+  ap.ring = ring;
+  const int tzr = habc_tile_rows();
+  const int bw = stencil_box_width(R);
+  CUtensorMap pu[3], pum[3], su3[3], sum3[3];
+  for (int i = 0; i < 3; ++i)
+    if (field_map(&pu[i], pbuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R) ||
+        field_map(&pum[i], pbuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr) ||
+        field_map(&su3[i], sbuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R) ||
+        field_map(&sum3[i], sbuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr))
+      return SGB_ERR_CUDA;
+  AcStreamArgs sp, ss;
+  std::memset(&sp, 0, sizeof(sp));
+  std::memset(&ss, 0, sizeof(ss));
+  fill_stream_args(sp, ap, acq, tzr);
+  fill_stream_habc(sp, ap);
+  fill_stream_args(ss, as, acq, tzr);
+  fill_stream_habc(ss, as);
+  if ((ap.src_ptr != nullptr && acq->src_zr == nullptr) || (acq->records != nullptr && acq->rec_zr == nullptr))
+    return SGB_ERR_ARG;
   for (int i = 0; i < 3; ++i) {
     SGB_CUDA_CHECK(cudaMemsetAsync(pbuf[i], 0, field * sizeof(float), s));
     SGB_CUDA_CHECK(cudaMemsetAsync(sbuf[i], 0, field * sizeof(float), s));
   }
   int cur = 0, prev = 1, nxt = 2;
   for (int t = 0; t < acq->nt; ++t) {
-    ap.u = pbuf[cur];
-    ap.um = pbuf[prev];
-    ap.un = pbuf[nxt];
-    ap.t = t;
-    SGB_CUDA_CHECK(launch_acoustic_fwd(R, true, tz, ap, s));
-    as.u = sbuf[cur];
-    as.um = sbuf[prev];
-    as.un = sbuf[nxt];
-    as.t = t;
-    as.records = acq->records ? acq->records + (long long)t * acq->nrec * acq->nch : nullptr;
-    SGB_CUDA_CHECK(launch_acoustic_fwd(R, true, tz, as, s));
-    if (bs != nullptr) {
-      SGB_CUDA_CHECK(launch_ring_copy(*grid, ring, pbuf[nxt], bs->ring_store + (long long)t * grid->nshots * ring.size,
-                                      false, s));
-      if (bs->ckpt_every > 0 && (t + 1) % bs->ckpt_every == 0) {
-        float* slot = bs->ckpt_store + (long long)((t + 1) / bs->ckpt_every - 1) * 2 * field;
-        SGB_CUDA_CHECK(cudaMemcpyAsync(slot, pbuf[nxt], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
-        SGB_CUDA_CHECK(cudaMemcpyAsync(slot + field, pbuf[cur], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
-      }
+    sp.u = pbuf[cur];
+    sp.um = pbuf[prev];
+    sp.un = pbuf[nxt];
+    sp.t = t;
+    // the background step saves the ring of its input U_t into slot t-1
+    sp.ring_src = pbuf[cur];
+    sp.ring_dst = (bs != nullptr && t >= 1) ? bs->ring_store + (long long)(t - 1) * grid->nshots * ring.size : nullptr;
+    const CUtensorMap mp[2] = {pu[cur], pum[prev]};
+    SGB_CUDA_CHECK(launch_acoustic_fwd_stream(R, mp, sp, s, true));
+    ss.u = sbuf[cur];
+    ss.um = sbuf[prev];
+    ss.un = sbuf[nxt];
+    ss.t = t;
+    ss.records = acq->records ? acq->records + (long long)t * acq->nrec * acq->nch : nullptr;
+    const CUtensorMap ms[2] = {su3[cur], sum3[prev]};
+    SGB_CUDA_CHECK(launch_acoustic_fwd_stream(R, ms, ss, s, true));
+    if (bs != nullptr && bs->ckpt_every > 0 && (t + 1) % bs->ckpt_every == 0) {
+      float* slot = bs->ckpt_store + (long long)((t + 1) / bs->ckpt_every - 1) * 2 * field;
+      SGB_CUDA_CHECK(cudaMemcpyAsync(slot, pbuf[nxt], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      SGB_CUDA_CHECK(cudaMemcpyAsync(slot + field, pbuf[cur], field * sizeof(float), cudaMemcpyDeviceToDevice, s));
     }
     prev = cur;
     cur = nxt;

@@ -574,6 +574,7 @@ struct HabcVjpArgs {
   const float* __restrict__ born_u;
   float* __restrict__ born_gu;
   float* __restrict__ born_gm;
+  float* __restrict__ wi_out;
 };
 
 template <int R, int EQ>
@@ -715,7 +716,248 @@ __global__ void __launch_bounds__(256) habc_step_vjp_kernel(const HabcVjpArgs a)
     for (int q = 0; q < np; ++q) a.gparam[q * pl + o] = pacc[q];
     if (a.gc != nullptr) a.gc[o] = cacc;
     if (born) a.born_gm[o] = macc;
+    if (a.wi_out != nullptr) a.wi_out[o] = wq.wi;
   }
+}
+
+
+// ------------------------------------------- line walkers + all-cell tiles ---
+// The plain / VTI / Born reverse step in two kinds of launch.  The one-way
+// transposes are gathered along each strip's inward normal by one thread per
+// (shot, line) (habc_oneway_tb_kernel: top and bottom lines, one per column;
+// habc_oneway_lr_kernel: left and right lines, one per row), which evaluate
+// each cell's side share once and carry the previous two cells' terms in
+// registers.  They write their sums into the output adjoint La_j for the
+// cells within hw of an edge (the only ones they reach).  The tiled kernel
+// (habc_bwd_tile_kernel) then computes every cell: the interior-share
+// weighted transpose 2 wi La1 + L(k wi La1) - wi La2 from shared-memory tiles
+// of k wi La1 and U_{j-1}, plus the one-way sum for band cells, plus the
+// receiver residuals; and the gradient term and the reconstruction inside the
+// box, the saved ring (or 0) outside it.
+
+// The one-way line of side `side` through the edge cell (ze, xe) with inward
+// step (sz, sx): the transposes of the strip cells at depths 0 .. hw-1 into
+// the cells at depths 0 .. hw (lines of one shot, fields offset by fb).
+// `keep(z, x)` says whether the cell already holds a partial sum to add to.
+template <class Keep>
+__device__ __forceinline__ void oneway_line(const HabcBwdArgs& a, long long fb, int ze, int xe, int sz, int sx,
+                                            int side, Keep keep) {
+  const int hw = a.hw;
+  const bool mult = a.multiple != 0;
+  const float* l1 = a.la1 + fb;
+  const float* l2 = a.la2 + fb;
+  float* out = a.lout + fb;
+  const long long step = (long long)sz * a.pitch + sx;
+  long long o = (long long)ze * a.pitch + xe;
+  // terms of the cells one and two steps back: C l1 - D l2 and -E l1
+  float c1 = 0.f, e2 = 0.f, e1 = 0.f;
+  float acc0 = 0.f, wrap = 0.f;
+  for (int k = 0; k <= hw; ++k, o += step) {
+    const int z = ze + k * sz, x = xe + k * sx;
+    float v = c1 + e2;
+    float cn = 0.f, en = 0.f;
+    if (k < hw) {
+      const HabcW w = habc_weights(z, x, a.nz, a.nx, hw, mult, __ldg(a.hb + (long long)z * a.pitch + x));
+      const float ws = side == 0 ? w.wt : side == 1 ? w.wb : side == 2 ? w.wl : w.wr;
+      if (ws != 0.f) {
+        const float c = __ldg(a.vp + (long long)z * a.pitch + x);
+        const float lam = c * a.lamf, mu = c * c * a.muf;
+        const float u1 = l1[o], u2 = l2[o];
+        v += ws * ((2.f - lam - mu) * u1 + (lam - 1.f) * u2);
+        cn = ws * ((lam + 2.f * mu) * u1 - lam * u2);
+        en = -ws * mu * u1;
+        if (k == hw - 1) wrap = en;  // its second neighbour is the edge cell
+      }
+    }
+    // the depth-(k-2) cell's p2 is this cell unless it wrapped (k - 2 = hw - 1)
+    e2 = e1;
+    e1 = (k + 1 < hw) ? en : 0.f;
+    c1 = cn;
+    if (k == 0) {
+      acc0 = v;
+    } else {
+      out[o] = keep(z, x) ? out[o] + v : v;
+    }
+  }
+  o = (long long)ze * a.pitch + xe;
+  out[o] = keep(ze, xe) ? out[o] + acc0 + wrap : acc0 + wrap;
+}
+
+__global__ void __launch_bounds__(128) habc_oneway_tb_kernel(const HabcBwdArgs a) {
+  const long long n = (long long)a.nshots * a.nx;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(i / a.nx), x = (int)(i - (long long)b * a.nx);
+    const long long fb = (long long)b * a.sstride;
+    const int hw = a.hw;
+    oneway_line(a, fb, 0, x, 1, 0, 0, [](int, int) { return false; });
+    oneway_line(a, fb, a.nz - 1, x, -1, 0, 1, [&](int z, int) { return z <= hw; });
+  }
+}
+
+__global__ void __launch_bounds__(128) habc_oneway_lr_kernel(const HabcBwdArgs a) {
+  const long long n = (long long)a.nshots * a.nz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(i / a.nz), z = (int)(i - (long long)b * a.nz);
+    const long long fb = (long long)b * a.sstride;
+    const int hw = a.hw, nz = a.nz;
+    const bool tb = z <= hw || z >= nz - 1 - hw;  // written by the top / bottom lines
+    oneway_line(a, fb, z, 0, 0, 1, 2, [&](int, int) { return tb; });
+    oneway_line(a, fb, z, a.nx - 1, 0, -1, 3, [&](int, int x) { return tb || x <= hw; });
+  }
+}
+
+// All cells of a reverse step, tile 8 x 128 with block (32, 8) (lane: four
+// columns).  La_j = 2 wi La1 + L(k wi La1) - wi La2 (VTI: x neighbours by
+// kx, z neighbours by kz) + one-way sums (band cells, from lout) + residuals.
+template <int R, bool VTI>
+__global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a) {
+  constexpr int ROWS = HT_Z + 2 * R, W = HT_X + 2 * HT_H;
+  __shared__ __align__(16) float s_kl[ROWS][W];             // k wi La1 (VTI: kx wi La1)
+  __shared__ __align__(16) float s_kzl[VTI ? ROWS : 1][W];  // VTI: kz wi La1
+  __shared__ __align__(16) float s_u[ROWS][W];
+  const int b = blockIdx.z;
+  const int z0 = blockIdx.y * HT_Z, x0 = blockIdx.x * HT_X;
+  const long long fb = (long long)b * a.sstride;
+  const float* l1 = a.la1 + fb;
+  const float* u1 = a.ujm1 + fb;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const int hw = a.hw;
+  const bool mult = a.multiple != 0;
+  // does any cell of the tile or its halo have an interior share below 1?
+  const bool near = hw > 0 && ((!mult && z0 - R < hw) || z0 + HT_Z + R > a.nz - hw || x0 - HT_H < hw ||
+                                x0 + HT_X + HT_H > a.nx - hw);
+  auto wi_at = [&](int z, int x) -> float {
+    return near ? habc_weights(z, x, a.nz, a.nx, hw, mult, __ldg(a.hb + (long long)z * a.pitch + x)).wi : 1.f;
+  };
+  for (int c = tid; c < ROWS * (W / 4); c += 256) {
+    const int rr = c / (W / 4), cc = c - rr * (W / 4);
+    const int z = z0 - R + rr, x = x0 - HT_H + 4 * cc;
+    float kl[4] = {0.f, 0.f, 0.f, 0.f}, kzl[4] = {0.f, 0.f, 0.f, 0.f}, uu[4] = {0.f, 0.f, 0.f, 0.f};
+    if (z >= 0 && z < a.nz && x >= 0 && x < a.nx) {
+      const long long o = (long long)z * a.pitch + x;
+      const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
+      const float4 l4 = *reinterpret_cast<const float4*>(l1 + o);
+      const float4 q4 = VTI ? __ldg(reinterpret_cast<const float4*>(a.kz + o)) : k4;
+      const float4 v4 = *reinterpret_cast<const float4*>(u1 + o);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        if (x + m < a.nx) {
+          const float w = wi_at(z, x + m);
+          kl[m] = comp(k4, m) * w * comp(l4, m);
+          if (VTI) kzl[m] = comp(q4, m) * w * comp(l4, m);
+          uu[m] = comp(v4, m);
+        }
+      }
+    }
+    *reinterpret_cast<float4*>(&s_kl[rr][4 * cc]) = make_float4(kl[0], kl[1], kl[2], kl[3]);
+    if (VTI) *reinterpret_cast<float4*>(&s_kzl[rr][4 * cc]) = make_float4(kzl[0], kzl[1], kzl[2], kzl[3]);
+    *reinterpret_cast<float4*>(&s_u[rr][4 * cc]) = make_float4(uu[0], uu[1], uu[2], uu[3]);
+  }
+  __syncthreads();
+  const int z = z0 + threadIdx.y, x = x0 + 4 * threadIdx.x;
+  if (z >= a.nz || x >= a.nx) return;
+  const int rr = R + threadIdx.y, cx = HT_H + 4 * threadIdx.x;
+  const long long o = (long long)z * a.pitch + x;
+  const float4 l2v = *reinterpret_cast<const float4*>(a.la2 + fb + o);
+  const float4 l1c = *reinterpret_cast<const float4*>(l1 + o);
+  const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
+  const float4 kz4 = VTI ? __ldg(reinterpret_cast<const float4*>(a.kz + o)) : k4;
+  // band cells (within hw of an edge) carry the one-way sums in lout
+  const bool band_rows = hw > 0 && (z <= hw || z >= a.nz - 1 - hw);
+  const float4 ow4 = (band_rows || (hw > 0 && (x <= hw || x + 3 >= a.nx - 1 - hw)))
+                         ? *reinterpret_cast<const float4*>(a.lout + fb + o) : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float ch = 0.5f * a.w.c[0];
+  float v[4], L[4], Lz[4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int xm = x + m;
+    const float wq = (xm < a.nx) ? wi_at(z, xm) : 0.f;
+    const bool band = band_rows || (hw > 0 && (xm <= hw || xm >= a.nx - 1 - hw));
+    float lap, lu, luz = 0.f;
+    if (VTI) {
+      float lx = ch * s_kl[rr][cx + m], lz = ch * s_kzl[rr][cx + m];
+      float ux = ch * s_u[rr][cx + m], uz = ch * s_u[rr][cx + m];
+#pragma unroll
+      for (int j = 1; j <= R; ++j) {
+        lx += a.w.c[j] * (s_kl[rr][cx + m - j] + s_kl[rr][cx + m + j]);
+        lz += a.w.c[j] * (s_kzl[rr - j][cx + m] + s_kzl[rr + j][cx + m]);
+        ux += a.w.c[j] * (s_u[rr][cx + m - j] + s_u[rr][cx + m + j]);
+        uz += a.w.c[j] * (s_u[rr - j][cx + m] + s_u[rr + j][cx + m]);
+      }
+      lap = lx + lz;
+      lu = ux;
+      luz = uz;
+    } else {
+      lap = a.w.c[0] * s_kl[rr][cx + m];
+      lu = a.w.c[0] * s_u[rr][cx + m];
+#pragma unroll
+      for (int j = 1; j <= R; ++j) {
+        lap += a.w.c[j] * (s_kl[rr - j][cx + m] + s_kl[rr + j][cx + m] + s_kl[rr][cx + m - j] + s_kl[rr][cx + m + j]);
+        lu += a.w.c[j] * (s_u[rr - j][cx + m] + s_u[rr + j][cx + m] + s_u[rr][cx + m - j] + s_u[rr][cx + m + j]);
+      }
+    }
+    v[m] = (xm < a.nx) ? 2.f * wq * comp(l1c, m) + lap - wq * comp(l2v, m) + (band ? comp(ow4, m) : 0.f) : 0.f;
+    L[m] = lu;
+    Lz[m] = luz;
+  }
+  // residuals of the records of step j-1 in this row
+  if (a.resid != nullptr) {
+    const int* rp = a.rec_row_ptr + (long long)b * a.nz;
+    int lo = rp[z], hi = rp[z + 1];
+    const int end = hi;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (a.rec_x[mid] < x) lo = mid + 1; else hi = mid;
+    }
+    for (int q = lo; q < end && a.rec_x[q] < x + 4; ++q) {
+      const int dx = a.rec_x[q] - x;
+      const float rv = a.resid[(long long)a.rec_col[q] * a.nch];
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+        if (dx == m) v[m] += rv;
+    }
+  }
+  *reinterpret_cast<float4*>(a.lout + fb + o) = make_float4(v[0], v[1], v[2], v[3]);
+  // gradient and reconstruction inside the box; the saved ring (or 0) outside
+  const bool row_in = z >= a.ring.iz0 && z < a.ring.iz1;
+  float uo[4] = {0.f, 0.f, 0.f, 0.f};
+  float ujv[4] = {0.f, 0.f, 0.f, 0.f};
+  if (a.uout != nullptr && row_in) {
+    const float4 uj = *reinterpret_cast<const float4*>(a.uj + fb + o);
+    ujv[0] = uj.x; ujv[1] = uj.y; ujv[2] = uj.z; ujv[3] = uj.w;
+    if (a.src_ptr != nullptr) {
+      for (int q = a.src_ptr[b]; q < a.src_ptr[b + 1]; ++q) {
+        const int dx = a.src_x[q] - x;
+        if (a.src_z[q] == z && dx >= 0 && dx < 4) {
+          const float wv = a.wavelet[(long long)a.src_wrow[q] * a.nt + a.t_src];
+#pragma unroll
+          for (int m = 0; m < 4; ++m)
+            if (dx == m) ujv[m] -= wv;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int xm = x + m;
+    if (xm >= a.nx) break;
+    const long long om = o + m;
+    if (row_in && xm >= a.ring.ix0 && xm < a.ring.ix1) {
+      const float kk = comp(k4, m);
+      if (VTI) {
+        a.grad[fb + om] += v[m] * L[m];
+        a.grad2[fb + om] += v[m] * Lz[m];
+        uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + kk * L[m] + comp(kz4, m) * Lz[m];
+      } else {
+        a.grad[fb + om] += v[m] * kk * L[m];
+        uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + kk * L[m];
+      }
+    } else if (a.uout != nullptr) {
+      const int ri = a.ring.index(z, xm);
+      uo[m] = (ri >= 0 && a.ring_in != nullptr) ? a.ring_in[(long long)b * a.ring.size + ri] : 0.f;
+    }
+  }
+  if (a.uout != nullptr) *reinterpret_cast<float4*>(a.uout + fb + o) = make_float4(uo[0], uo[1], uo[2], uo[3]);
 }
 
 }  // namespace
@@ -765,13 +1007,36 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
   a.rec_col = q.rec_col;
   a.nch = q.nch;
   a.resid = resid;
-  // interior region of the tiled kernel (plain equation only)
   const int R = a.R, far = a.hw + R;
+  const bool vti = kz != nullptr;
+  if (rho_c == nullptr && R <= HT_H) {
+    // plain / VTI / Born: one-way sums along the strip lines, then every cell in tiles
+    a.tz0 = a.tz1 = a.tx0 = a.tx1 = 0;
+    if (a.hw > 0) {
+      const long long ntb = (long long)g.nshots * g.nx, nlr = (long long)g.nshots * g.nz;
+      habc_oneway_tb_kernel<<<(unsigned)((ntb + 127) / 128), 128, 0, s>>>(a);
+      habc_oneway_lr_kernel<<<(unsigned)((nlr + 127) / 128), 128, 0, s>>>(a);
+    }
+    const dim3 grid((unsigned)((g.nx + HT_X - 1) / HT_X), (unsigned)((g.nz + HT_Z - 1) / HT_Z), (unsigned)g.nshots);
+    switch (R * 2 + (vti ? 1 : 0)) {
+      case 2: habc_bwd_tile_kernel<1, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+      case 3: habc_bwd_tile_kernel<1, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+      case 4: habc_bwd_tile_kernel<2, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+      case 5: habc_bwd_tile_kernel<2, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+      case 6: habc_bwd_tile_kernel<3, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+      case 7: habc_bwd_tile_kernel<3, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+      case 8: habc_bwd_tile_kernel<4, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+      case 9: habc_bwd_tile_kernel<4, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+      default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+  }
+  // variable density: the tiled interior kernel does not apply (rho_c set),
+  // so the per-cell kernel takes every cell
   a.tz0 = a.multiple ? R : far;
   a.tz1 = g.nz - far;
   a.tx0 = (far + 3) / 4 * 4;
   a.tx1 = (g.nx - far) / 4 * 4;
-  const bool vti = kz != nullptr;
   const bool tiled = rho_c == nullptr && R <= HT_H && a.tz1 > a.tz0 && a.tx1 > a.tx0 && a.tz0 >= R &&
                      a.tz1 + R <= g.nz;
   if (!tiled) a.tz0 = a.tz1 = a.tx0 = a.tx1 = 0;
@@ -845,6 +1110,7 @@ cudaError_t launch_habc_step_vjp(const sgb_grid& g, const sgb_acoustic_model& m,
   a.born_u = io.born_u;
   a.born_gu = io.born_gu;
   a.born_gm = io.born_gm;
+  a.wi_out = io.wi_out;
   const long long cells = (long long)g.nz * g.nx;
   long long blocks = (cells + 255) / 256;
   if (blocks > 152 * 8) blocks = 152 * 8;

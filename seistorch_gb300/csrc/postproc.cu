@@ -92,6 +92,59 @@ __global__ void sd_kernel(long long n, float* p, const float* g, int clamp, floa
   }
 }
 
+// Non-linear conjugate gradient (optimizer.py:144-224).  d = grad clamped to
+// [lo, hi] when clamp.  sums: [0] |d|^2, [1] (d - gp) . d, [2] |gp|^2
+// (float64 atomics), then beta (PR or FR; 0 when |gp| = 0), the direction
+// dir = -d + beta dir, gp = d, max |dir| (bits in slot 3), and the update
+// param += lr / max|dir| * dir.
+__device__ __forceinline__ float clamp_to(float v, int clamp, float lo, float hi) {
+  return clamp ? fminf(fmaxf(v, lo), hi) : v;
+}
+
+__global__ void ncg_dots_kernel(long long n, const float* g, const float* gp, int clamp, float lo, float hi,
+                                double* sums) {
+  double a = 0.0, b = 0.0, c = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double d = clamp_to(g[i], clamp, lo, hi), p = gp[i];
+    a += d * d;
+    b += (d - p) * d;
+    c += p * p;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(sums, a);
+    atomicAdd(sums + 1, b);
+    atomicAdd(sums + 2, c);
+  }
+}
+
+__global__ void ncg_dir_kernel(long long n, const float* g, int clamp, float lo, float hi, float* gp, float* dir,
+                               int fletcher_reeves, const double* sums, unsigned* maxbits) {
+  const double pn = sums[2];
+  const float beta = pn == 0.0 ? 0.f : (float)((fletcher_reeves ? sums[0] : sums[1]) / pn);
+  float m = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float d = clamp_to(g[i], clamp, lo, hi);
+    const float v = -d + beta * dir[i];
+    dir[i] = v;
+    gp[i] = d;
+    m = fmaxf(m, fabsf(v));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxbits, __float_as_uint(m));
+}
+
+__global__ void ncg_update_kernel(long long n, float* p, const float* dir, float lr, const unsigned* maxbits) {
+  const float mx = __uint_as_float(*maxbits);
+  const float alpha = mx > 0.f ? lr / mx : 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] += alpha * dir[i];
+}
+
 // Zero-phase IIR filter of every trace (scipy.signal.filtfilt's default
 // method as SeisSignal._filter_ calls it, signal.py:39-40): odd extension
 // by padlen samples at both ends, a forward direct-form-II-transposed pass
@@ -179,6 +232,23 @@ int sgb_sd_step(int64_t n, float* param, const float* grad, float lr, int32_t cl
   SGB_CUDA_CHECK(cudaMemsetAsync(scratch, 0, sizeof(uint32_t), s));
   maxabs_kernel<<<blocks_for(n), 256, 0, s>>>(n, grad, clamp, lo, hi, scratch);
   sd_kernel<<<blocks_for(n), 256, 0, s>>>(n, param, grad, clamp, lo, hi, lr, scratch);
+  SGB_CUDA_CHECK(cudaGetLastError());
+  return SGB_OK;
+}
+
+int sgb_ncg_step(int64_t n, float* param, const float* grad, float* prev_grad, float* direction, float lr,
+                 int32_t beta_type, int32_t clamp, float lo, float hi, double* scratch, sgb_stream_t stream) {
+  if (param == nullptr || grad == nullptr || prev_grad == nullptr || direction == nullptr || scratch == nullptr)
+    return SGB_ERR_ARG;
+  if (n <= 0) return SGB_ERR_SHAPE;
+  if (beta_type != 0 && beta_type != 1) return SGB_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  SGB_CUDA_CHECK(cudaMemsetAsync(scratch, 0, 4 * sizeof(double), s));
+  unsigned* maxbits = reinterpret_cast<unsigned*>(scratch + 3);
+  ncg_dots_kernel<<<blocks_for(n), 256, 0, s>>>(n, grad, prev_grad, clamp, lo, hi, scratch);
+  ncg_dir_kernel<<<blocks_for(n), 256, 0, s>>>(n, grad, clamp, lo, hi, prev_grad, direction, beta_type, scratch,
+                                               maxbits);
+  ncg_update_kernel<<<blocks_for(n), 256, 0, s>>>(n, param, direction, lr, maxbits);
   SGB_CUDA_CHECK(cudaGetLastError());
   return SGB_OK;
 }

@@ -12,7 +12,7 @@ import ctypes
 import torch
 
 from . import _native as N
-from .engine import check_cfl, grid_struct, interior_box, pitch_of, require_cuda, to_pitched
+from .engine import check_cfl, grid_struct, interior_box, pitch_of, require_cuda, to_pitched, unpitched
 
 FIELDS = ("vx", "vz", "txx", "tzz", "txz")  # Wavefield('elastic') order (eqconfigure.py:45-127)
 
@@ -87,7 +87,7 @@ class ElasticPropagator:
         g = self.grid(inp[0].shape[0])
         N.call("sgb_elastic_step", ctypes.byref(g), ctypes.byref(m), N.PTR5(*[t.data_ptr() for t in inp]),
                N.PTR5(*[t.data_ptr() for t in out]), N.stream_handle())
-        return tuple(o[..., :self.nx] for o in out)
+        return tuple(unpitched(o, self.nx) for o in out)
 
     def step_vjp(self, vp, vs, rho, damp, fields_in, stresses_out, grads_out):
         """(dJ/d inputs[5], dJ/dvp, dJ/dvs, dJ/drho) of one step."""

@@ -52,6 +52,12 @@ def check_cfl(vel, scheme, order, dt, h, vmax_of=None):
     _CFL_LAST[key] = (weakref.ref(vel), vel._version)
 
 
+def unpitched(t, nx):
+    """The first nx columns of a pitched tensor as a tensor of its own (not a
+    view), so callers may modify a step's output in place."""
+    return t if t.shape[-1] == nx else t[..., :nx].contiguous()
+
+
 def to_pitched(a, pitch, dtype=torch.float32):
     """(..., nz, nx) -> contiguous (..., nz, pitch) float32 with zero pad columns."""
     a = a.to(dtype)
@@ -223,7 +229,7 @@ class AcousticPropagator:
         g = self.grid(B)
         N.call("sgb_acoustic_step", ctypes.byref(g), ctypes.byref(m), N.ptr(up), N.ptr(ump), N.ptr(out),
                N.stream_handle())
-        return out[..., :self.nx]
+        return unpitched(out, self.nx)
 
     def step_vjp(self, vp, damp, u, gy, gh1):
         m, keep = self.model(vp, damp)
@@ -239,7 +245,7 @@ class AcousticPropagator:
                N.ptr(gh1p), N.ptr(gu), N.ptr(gum), N.ptr(gvp), N.stream_handle())
         return gu[..., :self.nx], gum[..., :self.nx], gvp[:, :self.nx]
 
-    def habc_vjp(self, m, u, um, gy, kz=None, rho_c=None, born=None):
+    def habc_vjp(self, m, u, um, gy, kz=None, rho_c=None, born=None, want_wi=False):
         """sgb_habc_step_vjp on pitched copies: dict of gu, gum (fields),
         gparam (1, 2 or 5 planes), gc (one-way velocity term) and, with
         ``born = (m plane, background U_n)``, born_gu and born_gm."""
@@ -257,9 +263,11 @@ class AcousticPropagator:
             bu = pit(born[1])
             out["born_gu"] = torch.empty_like(up)
             out["born_gm"] = torch.empty(self.nz, self.pitch, dtype=torch.float32, device=dev)
+        if want_wi:
+            out["wi"] = torch.empty(self.nz, self.pitch, dtype=torch.float32, device=dev)
         io = N.HabcVjpIO(N.ptr(up), N.ptr(ump), N.ptr(gyp), N.ptr(out["gu"]), N.ptr(out["gum"]),
                          N.ptr(out["gparam"]), N.ptr(out["gc"]), N.ptr(kz), N.ptr(rho_c), N.ptr(bm), N.ptr(bu),
-                         N.ptr(out.get("born_gu")), N.ptr(out.get("born_gm")))
+                         N.ptr(out.get("born_gu")), N.ptr(out.get("born_gm")), N.ptr(out.get("wi")))
         g = self.grid(B)
         N.call("sgb_habc_step_vjp", ctypes.byref(g), ctypes.byref(m), ctypes.byref(io), N.stream_handle())
         nx = self.nx
@@ -444,7 +452,7 @@ class BornPropagator(AcousticPropagator):
         g = self.grid(B)
         N.call("sgb_born_step", ctypes.byref(g), ctypes.byref(m), N.ptr(mp), N.ptr(pp), N.ptr(ppm), N.ptr(ps),
                N.ptr(psm), N.ptr(pn), N.ptr(sn), N.ptr(src), N.stream_handle())
-        return pn[..., :self.nx], sn[..., :self.nx]
+        return unpitched(pn, self.nx), unpitched(sn, self.nx)
 
     def backward_born(self, state, acq, grad_records):
         """dJ/dm (nz, nx) from dJ/d(records) of the scattered field."""
@@ -560,7 +568,7 @@ class VTIPropagator(AcousticPropagator):
         g = self.grid(u.shape[0])
         N.call("sgb_vti_step", ctypes.byref(g), ctypes.byref(m), N.ptr(up), N.ptr(ump), N.ptr(out),
                N.stream_handle())
-        return out[..., :self.nx]
+        return unpitched(out, self.nx)
 
     def forward_vti(self, vp, eps, delta, damp, acq, *, save_for_adjoint=False, ckpt_every=0):
         m, keep = self.model_vti(vp, eps, delta, damp)
@@ -691,7 +699,7 @@ class RhoPropagator(AcousticPropagator):
         g = self.grid(u.shape[0])
         N.call("sgb_rho_step", ctypes.byref(g), ctypes.byref(m), N.ptr(rc), N.ptr(up), N.ptr(ump), N.ptr(out),
                N.stream_handle())
-        return out[..., :self.nx]
+        return unpitched(out, self.nx)
 
     def forward_rho(self, vp, rho, damp, acq, *, save_for_adjoint=False, ckpt_every=0):
         m, keep = self.model(vp, damp)
@@ -771,6 +779,158 @@ class _RhoLoop(torch.autograd.Function):
 def rho_loop(vp, rho, prop, damp, acq, ckpt_every=0):
     """Records (nt, nrec, 1) of the variable-density loop; differentiable in vp and rho."""
     return _RhoLoop.apply(vp, rho, prop, damp, acq, ckpt_every)
+
+
+def vacoustic_coefficients(vp, Q, dt, h, omega=16.5):
+    """Planes of vacoustic_habc._time_step (vacoustic_habc.py:74-111): the
+    Laplacian coefficient kv = vp^2 dt^2 (1 - (1 - sqrt(Q^2 + 1)) / Q^2) / h^2
+    (wave term plus phase correction) and the damping coefficient
+    a_neg = -dt t vp / 2 of K(U - U-) with t_sigma = (sqrt(1 + Q^-2) - 1/Q) /
+    omega, t_eps = 1 / (omega^2 t_sigma), t = t_eps / (t_sigma - 1e-8) - 1.
+    The reference uses omega = 16.5 in its forward step and 5.0 in its
+    reverse steps.  Differentiable in vp and Q (float64)."""
+    vp, Q = vp.double(), Q.double()
+    t_sigma = (torch.sqrt(1.0 + Q ** -2) - Q ** -1) / omega
+    t_eps = (omega ** 2 * t_sigma) ** -1
+    t = t_eps / (t_sigma - 1e-8) - 1.0
+    kv = vp ** 2 * float(dt) ** 2 / float(h) ** 2 * (1.0 - (1.0 - torch.sqrt(Q ** 2 + 1.0)) * Q ** -2)
+    return kv, -(float(dt) * t * vp / 2.0)
+
+
+class VacousticPropagator(AcousticPropagator):
+    """Viscoacoustic equation with the HABC (vacoustic_habc.py): the acoustic
+    HABC step with the Laplacian coefficient kv and the spectral damping term
+    a_neg K(U - U-), K = real(ifft2(|k| fft2(.))) (sgb_vacoustic_kterm)."""
+
+    def __init__(self, nz, nx, dt, h, order=2, bwidth=50, multiple=False, device=None):
+        super().__init__(nz, nx, dt, h, order, "habc", bwidth, multiple, device)
+
+    def model_vac(self, vp, Q, damp, blend=True, omega=16.5):
+        require_cuda(vp, "VacousticPropagator.model_vac")
+        kv, an = vacoustic_coefficients(vp.detach(), Q.detach(), self.dt, self.h, omega)
+        check_cfl(vp, N.SCHEME_ACOUSTIC, self.order, self.dt, self.h,
+                  lambda _: float(kv.clamp_min(0).max().sqrt()) * self.h / self.dt)
+        coef = torch.empty(2, self.nz, self.pitch, dtype=torch.float32, device=vp.device)
+        coef[0] = 2.0
+        coef[1] = to_pitched(kv.float(), self.pitch)
+        a_neg = to_pitched(an.float(), self.pitch).contiguous()
+        vpp = to_pitched(vp.detach().float(), self.pitch).contiguous()
+        dp = to_pitched(damp.detach().to(vp.device).float(), self.pitch).contiguous()
+        m = N.AcousticModel(self.order, BOUNDARY_HABC, 50 if blend else 0, int(self.multiple), N.ptr(coef), N.ptr(vpp),
+                            N.ptr(dp))
+        return m, (vpp, dp, coef, a_neg)
+
+    def scratch(self, nshots, dev):
+        g = self.grid(nshots)
+        wf, tf = ctypes.c_int64(0), ctypes.c_int64(0)
+        N.call("sgb_vacoustic_work_size", ctypes.byref(g), ctypes.byref(wf), ctypes.byref(tf))
+        return (torch.empty(wf.value, dtype=torch.float32, device=dev),
+                torch.empty(tf.value, dtype=torch.float32, device=dev))
+
+    def kterm(self, u1, u2=None, pre=None, post=None):
+        """post * K(pre * (u1 - u2)) per shot (pitched planes / fields)."""
+        B = u1.shape[0]
+        work, tw = self.scratch(B, u1.device)
+        out = torch.empty_like(u1)
+        g = self.grid(B)
+        N.call("sgb_vacoustic_kterm", ctypes.byref(g), N.ptr(pre), N.ptr(u1), N.ptr(u2), N.ptr(post), N.ptr(out),
+               N.ptr(work), N.ptr(tw), N.stream_handle())
+        return out
+
+    def step_vac(self, vp, Q, damp, u, um, blend=True, omega=16.5):
+        m, keep = self.model_vac(vp, Q, damp, blend, omega)
+        pit = lambda t: to_pitched(t.to(torch.float32), self.pitch).contiguous()
+        up, ump = pit(u), pit(um)
+        out, extra = torch.empty_like(up), torch.empty_like(up)
+        work, tw = self.scratch(u.shape[0], up.device)
+        g = self.grid(u.shape[0])
+        N.call("sgb_vacoustic_step", ctypes.byref(g), ctypes.byref(m), N.ptr(keep[3]), N.ptr(up), N.ptr(ump),
+               N.ptr(out), N.ptr(extra), N.ptr(work), N.ptr(tw), N.stream_handle())
+        return unpitched(out, self.nx)
+
+    def step_vjp_vac(self, vp, Q, damp, u, um, gy, blend=True, omega=16.5):
+        """VJP of one step: dJ/du, dJ/dum, dJ/d(vp, Q).  The blended interior
+        update wi (2u - um + kv L(u) + a_neg K(u - um)) + one-way terms: the
+        HABC transposes (sgb_habc_step_vjp) plus K(a_neg wi gy) (K is
+        symmetric) into dJ/du and minus it into dJ/dum, and
+        dJ/da_neg = sum_b wi gy K(u - um)."""
+        m, keep = self.model_vac(vp, Q, damp, blend, omega)
+        r = self.habc_vjp(m, u, um, gy, want_wi=True)
+        pit = lambda t: to_pitched(t.to(torch.float32), self.pitch).contiguous()
+        wi = to_pitched(r["wi"], self.pitch).contiguous()
+        F = self.kterm(pit(gy), pre=(keep[3] * wi).contiguous())[..., :self.nx]
+        Kd = self.kterm(pit(u), pit(um))[..., :self.nx]
+        g_an = (r["wi"][None] * gy.to(torch.float32) * Kd).sum(0)
+        with torch.enable_grad():
+            ins = [t.detach().requires_grad_(True) for t in (vp, Q)]
+            kv, an = vacoustic_coefficients(*ins, self.dt, self.h, omega)
+            grads = torch.autograd.grad((kv, an), ins, (r["gparam"][0].double(), g_an.double()), allow_unused=True)
+        grads = [torch.zeros_like(t, dtype=torch.float64) if g_ is None else g_ for g_, t in zip(grads, ins)]
+        if blend:
+            grads[0] = grads[0] + r["gc"].double()
+        return r["gu"] + F, r["gum"] - F, grads
+
+    def forward_vac(self, vp, Q, damp, acq):
+        """Records (nt, nrec, 1) of the whole loop (no adjoint state)."""
+        m, keep = self.model_vac(vp, Q, damp)
+        B = acq.nshots
+        dev = vp.device
+        field = (B, self.nz, self.pitch)
+        buf = [torch.zeros(field, dtype=torch.float32, device=dev) for _ in range(3)]
+        extra = torch.empty(field, dtype=torch.float32, device=dev)
+        work, tw = self.scratch(B, dev)
+        records = torch.empty(acq.nt, max(acq.nrec, 1), 1, dtype=torch.float32, device=dev)
+        cur, prev = ctypes.c_int32(0), ctypes.c_int32(0)
+        g = self.grid(B)
+        q = acq.struct(records if acq.nrec else None, 1)
+        N.call("sgb_vacoustic_forward", ctypes.byref(g), ctypes.byref(m), N.ptr(keep[3]), ctypes.byref(q),
+               N.PTR3(*[b_.data_ptr() for b_ in buf]), N.ptr(extra), N.ptr(work), N.ptr(tw), ctypes.byref(cur),
+               ctypes.byref(prev), N.stream_handle())
+        self._last = (buf, cur.value, prev.value)
+        return records[:, :acq.nrec]
+
+
+class VacousticStep(torch.autograd.Function):
+    """One native viscoacoustic step with its native VJP (the per-step op of
+    vacoustic_habc._time_step and of its reverse steps)."""
+
+    @staticmethod
+    def forward(ctx, vp, Q, h1, h2, damp, prop, blend, omega):
+        ctx.prop, ctx.blend, ctx.omega = prop, blend, omega
+        ctx.save_for_backward(vp, Q, h1, h2, damp)
+        return prop.step_vac(vp, Q, damp, h1, h2, blend, omega)
+
+    @staticmethod
+    def backward(ctx, gy):
+        vp, Q, h1, h2, damp = ctx.saved_tensors
+        gu, gum, gm = ctx.prop.step_vjp_vac(vp, Q, damp, h1, h2, gy.contiguous().to(torch.float32), ctx.blend,
+                                            ctx.omega)
+        return (gm[0].to(vp.dtype), gm[1].to(Q.dtype), gu.to(h1.dtype), gum.to(h2.dtype), None, None, None, None)
+
+
+def vacoustic_records(vp, Q, prop, damp, acq):
+    """Records (nt, nrec, 1) of the viscoacoustic loop.  Without gradients:
+    the native whole loop (sgb_vacoustic_forward).  With gradients: the loop
+    step by step under autograd (native steps and VJPs), which is what the
+    reference differentiates -- its spectral damping term has no explicit
+    time reversal, so no boundary-saving reconstruction applies."""
+    if not (torch.is_grad_enabled() and (vp.requires_grad or Q.requires_grad)):
+        with torch.no_grad():
+            return prop.forward_vac(vp, Q, damp, acq)
+    B, dev = acq.nshots, vp.device
+    sp = acq.src_ptr.cpu().tolist()
+    sb = torch.as_tensor(np.repeat(np.arange(B), np.diff(sp)), device=dev)
+    sz, sx, sw = acq.src_z.long(), acq.src_x.long(), acq.src_wrow.long()
+    h1 = torch.zeros(B, prop.nz, prop.nx, device=dev)
+    h2 = torch.zeros_like(h1)
+    recs = []
+    for t in range(acq.nt):
+        y = VacousticStep.apply(vp, Q, h1, h2, damp, prop, True, 16.5)
+        if acq.nsrc:
+            y = y.index_put((sb, sz, sx), acq.wavelet[sw, t], accumulate=True)
+        h2, h1 = h1, y
+        recs.append(y[acq.rec_b, acq.rec_z, acq.rec_xs])
+    return torch.stack(recs)[..., None]
 
 
 class UnevenBatch:

@@ -11,11 +11,13 @@ class Parameters:
                 "acoustic_lsrtm_habc": ["vp", "m"],
                 "vti_habc2": ["vp", "epsilon", "delta"],
                 "acoustic_rho_habc": ["vp", "rho"],
+                "vacoustic_habc": ["vp", "Q"],
                 "elastic": ["vp", "vs", "rho"]}
 
     @staticmethod
     def secondorder_equations():
-        return ["acoustic", "acoustic_habc", "acoustic_rho_habc", "acoustic_lsrtm_habc", "vti_habc2"]
+        return ["acoustic", "acoustic_habc", "acoustic_rho_habc", "vacoustic_habc", "acoustic_lsrtm_habc",
+                "vti_habc2"]
 
 
 class Wavefield:
@@ -24,6 +26,7 @@ class Wavefield:
                "acoustic_lsrtm_habc": ["h1", "h2", "sh1", "sh2"],
                "vti_habc2": ["p1", "p2"],
                "acoustic_rho_habc": ["h1", "h2"],
+               "vacoustic_habc": ["h1", "h2"],
                "elastic": ["vx", "vz", "txx", "tzz", "txz"]}
 
     def __init__(self, equation="acoustic"):

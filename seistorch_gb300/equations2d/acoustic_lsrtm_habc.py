@@ -72,9 +72,9 @@ def _backward(args, multiple):
     h_bd, _, sh_bd, _ = args[-2]
     src_type, src_func, src_values = args[-1]
     p0, h1, s0, sh1 = _step(args[:9], multiple, blend=False)
-    with torch.no_grad():
-        p0 = restore_boundaries(p0, h_bd, multiple=multiple)
-        s0 = restore_boundaries(s0, sh_bd, multiple=multiple)
+    # tracked by autograd, as acoustic_lsrtm_habc.py:54-55 (no no_grad there)
+    p0 = restore_boundaries(p0, h_bd, multiple=multiple)
+    s0 = restore_boundaries(s0, sh_bd, multiple=multiple)
     p0 = src_func(p0, src_values, 1)
     return p0, h1, s0, sh1
 

@@ -66,8 +66,9 @@ def _backward(args, multiple):
     h_bd, _ = args[-2]
     src_type, src_func, src_values = args[-1]
     y, p1 = _step(args[:8], multiple, blend=False)
-    with torch.no_grad():
-        y = restore_boundaries(y, h_bd, multiple=multiple)
+    # tracked by autograd, as vti_habc2.py:99 (no no_grad there): the
+    # restored cells take their values, and their gradients, from the strips
+    y = restore_boundaries(y, h_bd, multiple=multiple)
     y = src_func(y, src_values, 1)
     return y, p1
 

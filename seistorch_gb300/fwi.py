@@ -1,21 +1,23 @@
 """Full-waveform inversion driver: the plain illumination-preconditioned
-gradient method and the learned-preconditioner method, both on the native
-solver.
+method and the learned-preconditioner method, both on the native solver.
 
-Plain (the reference's preconditioning, process.py:115-118 + a normalised
-steepest-descent step, optimizer.py:124-142): d = -g / (P + eps max P),
-scaled to a maximum update of ``alpha`` m/s, accepted only if the data
-misfit decreases (halving ``alpha`` otherwise).
+Plain: the reference's illumination preconditioning (process.py:115-118),
+p = g / (P + eps max P), with Polak-Ribiere conjugate directions (the beta of
+optimizer.py:144-224, restarted whenever the direction is not a descent
+direction) normalised to max |d| = 1, and a parabolic line search on the data
+misfit that uses the known slope g . d at the current model: one trial
+step, the minimiser of the parabola through (0, J0) with slope g . d and the
+trial, and a shorter step if neither lowers the misfit.
 
 Learned: the network maps [g / max|g|, P / max P] to a model update; the
-update is accepted only if the true data misfit decreases (at full, half or
-quarter length), else the plain step is taken -- the misfit stays the judge of the
-network's error and the plain gradient its fallback.
+same line search runs along it, and the update is accepted only if it lowers
+the true data misfit, else the plain step is taken -- the misfit stays the
+judge of the network's error and the plain method its fallback.
 
-Training pairs come from the solver itself: random layered + anomaly
-models, a starting point between the smoothed model and the truth, and the
-L2 gradient and source illumination there; the target is the model error
-(true - start) / 1000 m/s.
+Training pairs come from the solver itself on the inversion's own survey:
+random layered + anomaly models, a starting point between the smoothed model
+and the truth, and the L2 gradient and source illumination there; the
+target is the model error (true - start) / 1000 m/s.
 """
 import time
 
@@ -28,6 +30,7 @@ from .postprocess import L2
 from .utils import ricker_wave
 
 TARGET_SCALE = 1000.0  # m/s per unit of network output
+START_SIGMA = 10.0     # cells: starting models are the true model Gaussian-smoothed by this much
 
 
 def random_model(rng, nz=256, nx=512, vmin=1500.0, vmax=4500.0):
@@ -50,7 +53,7 @@ def random_model(rng, nz=256, nx=512, vmin=1500.0, vmax=4500.0):
     return np.clip(v, vmin, vmax)
 
 
-def smooth(v, sigma=20.0):
+def smooth(v, sigma=START_SIGMA):
     from scipy.ndimage import gaussian_filter
     return gaussian_filter(v, sigma, mode="nearest")
 
@@ -153,7 +156,32 @@ def train(net, X, Y, epochs=10, batch=8, lr=1e-3, seed=0, log=None):
     return hist
 
 
-def invert(survey, obs, v0, iters=20, net=None, alpha=100.0, vmin=1500.0, vmax=4500.0, log=None):
+def line_search(survey, obs, v, J0, g, d, a0, vmin, vmax):
+    """Step length along d (max |d| = 1, in m/s) from the misfit J0 with the
+    slope s0 = g . d: a trial step a0, then the minimiser of the parabola
+    J0 + s0 a + c a^2 through the trial (clipped to [a0/10, 4 a0]), then a
+    quarter of the shorter step.  Returns (model, misfit, step) of the best
+    step that lowers the misfit, or None."""
+    s0 = float((g * d).sum())
+    if not s0 < 0:
+        return None
+    clampv = lambda a: (v + a * d).clamp(vmin, vmax)
+    tried = []
+    J1 = survey.misfit(survey.pad(clampv(a0)), obs)
+    tried.append((J1, a0))
+    c = (J1 - J0 - s0 * a0) / (a0 * a0)
+    a2 = min(max(-s0 / (2 * c), 0.1 * a0), 4 * a0) if c > 0 else (2 * a0 if J1 < J0 else 0.25 * a0)
+    tried.append((survey.misfit(survey.pad(clampv(a2)), obs), a2))
+    if min(t[0] for t in tried) >= J0:
+        a3 = 0.25 * min(a0, a2)
+        tried.append((survey.misfit(survey.pad(clampv(a3)), obs), a3))
+    J, a = min(tried)
+    if J >= J0:
+        return None
+    return clampv(a), J, a
+
+
+def invert(survey, obs, v0, iters=20, net=None, step0=50.0, vmin=1500.0, vmax=4500.0, log=None):
     """FWI from interior model v0.  Returns dict(misfit=[...], time=[...],
     learned_steps=k, model=final interior model).  misfit[i] / time[i]: data
     misfit and elapsed wall time after i iterations (i = 0: start)."""
@@ -165,30 +193,38 @@ def invert(survey, obs, v0, iters=20, net=None, alpha=100.0, vmin=1500.0, vmax=4
     J, g, P = survey.gradient(survey.pad(v), obs)
     hist_m.append(J)
     hist_t.append(time.perf_counter() - t0)
+    p_prev = d_prev = None
+    a_plain, a_net = step0, 1.0
     for it in range(iters):
-        accepted = False
+        res = None
         if net is not None:
             dv = net.predict(features(g, P)[None])[0] * TARGET_SCALE
-            for beta in (1.0, 0.5, 0.25):
-                cand = (v + beta * dv).clamp(vmin, vmax)
-                Jc = survey.misfit(survey.pad(cand), obs)
-                if Jc < J:
-                    v, accepted = cand, True
-                    learned_steps += 1
-                    break
-        if not accepted:
-            d = plain_direction(g, P)
-            a = alpha
-            for _ in range(4):
-                cand = (v + a * d).clamp(vmin, vmax)
-                Jc = survey.misfit(survey.pad(cand), obs)
-                if Jc < J:
-                    v, accepted = cand, True
-                    alpha = a * 1.5 if a == alpha else a
-                    break
-                a *= 0.5
-            if not accepted:
-                alpha *= 0.25
+            scale = float(dv.abs().max().clamp_min(1e-30))
+            res = line_search(survey, obs, v, J, g, dv / scale, a_net * scale, vmin, vmax)
+            if res is not None:
+                a_net = res[2] / scale
+                learned_steps += 1
+                p_prev = d_prev = None  # the conjugate directions restart after a learned step
+        if res is None:
+            p = g / (P + 1e-3 * P.max())
+            d = -p
+            if p_prev is not None:
+                beta = float(((p - p_prev) * p).sum() / (p_prev * p_prev).sum().clamp_min(1e-30))
+                d = -p + max(beta, 0.0) * d_prev
+                if not float((g * d).sum()) < 0:
+                    d = -p
+            d = d / d.abs().max().clamp_min(1e-30)
+            res = line_search(survey, obs, v, J, g, d, a_plain, vmin, vmax)
+            if res is None and p_prev is not None:  # restart along the preconditioned gradient
+                d = -p / p.abs().max().clamp_min(1e-30)
+                res = line_search(survey, obs, v, J, g, d, a_plain, vmin, vmax)
+            p_prev, d_prev = p, d
+            if res is not None:
+                a_plain = res[2]
+            else:
+                a_plain *= 0.25
+        if res is not None:
+            v = res[0]
         J, g, P = survey.gradient(survey.pad(v), obs)
         hist_m.append(J)
         torch.cuda.synchronize()

@@ -129,6 +129,53 @@ class Steepestdescent(torch.optim.Optimizer):
         return loss
 
 
+class Cg(torch.optim.Optimizer):
+    """Non-linear conjugate gradient (optimizer.py:144-224): d = grad clamped
+    to its clip_value / 1 - clip_value quantiles when ``grad_clamp``; beta =
+    Polak-Ribiere ('PR') or Fletcher-Reeves ('FR'), 0 on the first step;
+    direction = -d + beta direction; param += lr direction / max|direction|.
+    One native call per parameter (sgb_ncg_step), no host synchronisation
+    besides the quantiles."""
+
+    name = "ncg"
+
+    def __init__(self, params, lr=1.0, beta_type="PR", grad_clamp=True, clip_value=0.02, **kwargs):
+        if beta_type not in ("PR", "FR"):
+            raise ValueError("Invalid beta_type. Must be 'FR' or 'PR'")
+        super().__init__(params, dict(lr=lr, beta_type=beta_type, grad_clamp=grad_clamp, clip_value=clip_value))
+        self._scratch = {}
+
+    @torch.no_grad()
+    def step(self, closure=None):
+        loss = closure() if closure is not None else None
+        for group in self.param_groups:
+            for p in group["params"]:
+                if p.grad is None:
+                    continue
+                if p.dtype != torch.float32 or not p.is_contiguous():
+                    raise TypeError("Cg updates contiguous float32 parameters")
+                g = p.grad.contiguous().to(torch.float32)
+                lo = hi = 0.0
+                if group["grad_clamp"]:
+                    c = float(group["clip_value"])
+                    q = torch.quantile(g.reshape(-1), torch.tensor([c, 1.0 - c], device=g.device))
+                    lo, hi = float(q[0]), float(q[1])
+                state = self.state[p]
+                if len(state) == 0:
+                    state["step"] = 0
+                    state["prev_grad"] = torch.zeros_like(g)
+                    state["direction"] = torch.zeros_like(g)
+                s = self._scratch.get(p.device)
+                if s is None:
+                    s = self._scratch[p.device] = torch.zeros(4, dtype=torch.float64, device=p.device)
+                N.call("sgb_ncg_step", p.numel(), N.ptr(p), N.ptr(g), N.ptr(state["prev_grad"]),
+                       N.ptr(state["direction"]), ctypes.c_float(group["lr"]),
+                       0 if group["beta_type"] == "PR" else 1, int(group["grad_clamp"]), ctypes.c_float(lo),
+                       ctypes.c_float(hi), N.ptr(s), N.stream_handle())
+                state["step"] += 1
+        return loss
+
+
 def filter_mode(freqs):
     """SeisSignal.decide_filter_type: a number or [f] -> lowpass, [f1, f2] -> bandpass."""
     if freqs == "all":

@@ -131,6 +131,15 @@ class WaveRNN(torch.nn.Module):
             ck = geom.ckpt_every or engine.default_ckpt_every(acq.nt)
             rec = engine.vti_loop(*[m_.to(torch.float32) for m_ in models[:3]], prop, d, acq, ck)
             self._fields = prop
+        elif eq == "vacoustic_habc":
+            if list(geom.source_type) != ["h1"] or list(geom.receiver_type) != ["h1"]:
+                raise NotImplementedError("vacoustic_habc injects into and records h1")
+            if not geom.use_habc:
+                raise NotImplementedError("vacoustic_habc runs with the HABC boundary")
+            prop = engine.VacousticPropagator(nz, nx, geom.dt, float(geom.h), geom.spatial_order, geom.bwidth,
+                                              geom.multiple, device)
+            rec = engine.vacoustic_records(models[0].to(torch.float32), models[1].to(torch.float32), prop, d, acq)
+            self._fields = prop
         elif eq == "elastic":
             from . import elastic_engine
             rec, illum, fields = elastic_engine.elastic_loop(models, geom, d, acq,

@@ -55,7 +55,8 @@ def run_case(ref, equation, models_int, *, order=2, width=20, multiple=False, ns
     torch.set_default_dtype(dtype)
     eqmod = {"acoustic": ref.acoustic, "acoustic_habc": ref.acoustic_habc,
              "acoustic_lsrtm_habc": ref.acoustic_lsrtm_habc, "vti_habc2": ref.vti_habc2,
-             "acoustic_rho_habc": ref.acoustic_rho_habc, "elastic": ref.elastic}[equation]
+             "acoustic_rho_habc": ref.acoustic_rho_habc, "vacoustic_habc": ref.vacoustic_habc,
+             "elastic": ref.elastic}[equation]
     if equation == "acoustic_rho_habc":
         # its one-cell difference / averaging kernels (convkernel.py:79-89) in the run's dtype
         for n in ("kernelx_gc_pos", "kernelx_gc_neg", "kernely_gc_pos", "kernely_gc_neg", "kernelx_gc_pos2",
@@ -215,6 +216,12 @@ def cases():
                                                  boundary_saving=True)
     C["grad_bs_elastic_zeroobs"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0, width=50,
                                         nt=160, grad=["vp", "vs", "rho"], obs_models=None, boundary_saving=True)
+    vac = {"vp": ah["vp"], "Q": layered(16, 24, [25.0, 60.0], 8, anomaly=10.0)}
+    C["vacoustic_habc"] = dict(equation="vacoustic_habc", models_int=vac, order=2, width=50, habc=True, nt=240)
+    C["vacoustic_habc_multiple"] = dict(equation="vacoustic_habc", models_int=vac, order=2, width=50, habc=True,
+                                        multiple=True, nt=240)
+    C["grad_vacoustic_habc_zeroobs"] = dict(equation="vacoustic_habc", models_int=vac, order=2, width=50,
+                                            habc=True, nt=160, grad=["vp", "Q"], obs_models=None)
     C["grad_elastic_zeroobs"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,
                                      nt=200, grad=["vp", "vs", "rho"], obs_models=None)
     C["grad_elastic"] = dict(equation="elastic", models_int=e, dt=0.0005, h=5.0, fm=20.0,

@@ -42,6 +42,23 @@ def main():
     out["l2_obs"] = np.stack([o.numpy() for o in obs])
     out["l2_loss"] = np.array(loss.item())
     out["l2_grad"] = np.stack([s.grad.numpy() for s in syn_g])
+    # non-linear conjugate gradient (optimizer.py:144-224): four steps of a
+    # 40 x 70 parameter with a drawn gradient each, PR with the quantile
+    # clamp and FR without it
+    opt_mod = importlib.import_module("seistorch.optimizer")
+    r2 = np.random.default_rng(1)
+    p0 = (2000.0 + 100.0 * r2.standard_normal((40, 70))).astype(np.float32)
+    grads = (r2.standard_normal((4, 40, 70)) * np.linspace(1.0, 3.0, 70)).astype(np.float32)
+    out["ncg_p0"], out["ncg_grads"] = p0, grads
+    for tag, beta, clamp in (("pr", "PR", True), ("fr", "FR", False)):
+        prm = torch.nn.Parameter(torch.tensor(p0))
+        opt = opt_mod.Cg([prm], lr=10.0, beta_type=beta, grad_clamp=clamp, clip_value=0.02)
+        steps = []
+        for k in range(4):
+            prm.grad = torch.tensor(grads[k])
+            opt.step()
+            steps.append(prm.detach().numpy().copy())
+        out["ncg_" + tag] = np.stack(steps)
     np.savez_compressed(os.path.join(HERE, "postproc.npz"), **out)
     print({k: v.shape for k, v in out.items()})
 

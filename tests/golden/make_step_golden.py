@@ -63,13 +63,16 @@ CASES = {
     "born_habc_o2": dict(equation="acoustic_lsrtm_habc", order=2, habc=True, multiple=False),
     "born_habc_o4_multiple": dict(equation="acoustic_lsrtm_habc", order=4, habc=True, multiple=True),
     "elastic": dict(equation="elastic", order=2, habc=False, multiple=False),
+    "vacoustic_habc": dict(equation="vacoustic_habc", order=2, habc=True, multiple=False),
+    "vacoustic_habc_multiple": dict(equation="vacoustic_habc", order=2, habc=True, multiple=True),
 }
 
 
 def eq_module(ref, equation, order, dtype):
     mod = {"acoustic": ref.acoustic, "acoustic_habc": ref.acoustic_habc,
            "acoustic_lsrtm_habc": ref.acoustic_lsrtm_habc, "vti_habc2": ref.vti_habc2,
-           "acoustic_rho_habc": ref.acoustic_rho_habc, "elastic": ref.elastic}[equation]
+           "acoustic_rho_habc": ref.acoustic_rho_habc, "vacoustic_habc": ref.vacoustic_habc,
+           "elastic": ref.elastic}[equation]
     if equation == "acoustic_rho_habc":
         for n in ("kernelx_gc_pos", "kernelx_gc_neg", "kernely_gc_pos", "kernely_gc_neg", "kernelx_gc_pos2",
                   "kernelx_gc_neg2", "kernely_gc_pos2", "kernely_gc_neg2"):
@@ -95,6 +98,8 @@ def models_for(equation, nz, nx, rng):
                 "delta": f32(0.05 + 0.05 * layered(nz, nx, 0.0, 1.0, rng))}
     if equation == "acoustic_rho_habc":
         return {"vp": vp, "rho": layered(nz, nx, 1000.0, 2400.0, rng)}
+    if equation == "vacoustic_habc":
+        return {"vp": vp, "Q": layered(nz, nx, 20.0, 80.0, rng)}
     vpe = layered(nz, nx, 2000.0, 3600.0, rng)
     return {"vp": vpe, "vs": f32(vpe / 1.73), "rho": f32(310.0 * vpe ** 0.25)}
 
@@ -137,7 +142,8 @@ def run(ref, name, equation, order, habc, multiple, B=2, nzi=8, nxi=12, seed=0):
     ht = torch.tensor(h, dtype=dtype)
     # outputs that are new time levels (second-order equations return (y, h1) pairs)
     second = equation != "elastic"
-    outs_new = [0] if equation in ("acoustic", "acoustic_habc", "vti_habc2", "acoustic_rho_habc") else \
+    outs_new = [0] if equation in ("acoustic", "acoustic_habc", "vti_habc2", "acoustic_rho_habc",
+                                   "vacoustic_habc") else \
         ([0, 2] if equation == "acoustic_lsrtm_habc" else [0, 1, 2, 3, 4])
     G = [smooth_field(rng, (B, nz, nx), 1.0) for _ in outs_new]
     for i, g in zip(outs_new, G):

@@ -11,10 +11,10 @@ tensorboard, prettytable, ...).  Those are absent here, so this loader:
 * registers a bare ``seistorch`` package whose ``__path__`` is the reference
   package directory (so ``__init__`` never runs),
 * registers empty stub modules for the missing third-party names,
-* execs ``equations2d/acoustic.py``, ``acoustic_habc.py`` and
-  ``acoustic_lsrtm_habc.py`` from source with their module-level
-  ``device = "cuda"`` (acoustic.py:56, acoustic_habc.py:57,
-  acoustic_lsrtm_habc.py:7) replaced by ``"cpu"`` so the FD kernel can be built
+* execs ``equations2d/acoustic.py``, ``acoustic_habc.py``,
+  ``acoustic_lsrtm_habc.py`` and ``vacoustic_habc.py`` from source with their
+  module-level ``device = "cuda"`` (acoustic.py:56, acoustic_habc.py:57,
+  acoustic_lsrtm_habc.py:7, vacoustic_habc.py:57) replaced by ``"cpu"`` so the FD kernel can be built
   without a GPU, and lets the caller patch ``spatial_order``/``kernel``
   (module globals read at call time, acoustic.py:55-58).
 """
@@ -126,6 +126,8 @@ def load(device="cpu"):
         "seistorch.equations2d.convkernel", os.path.join(PKG_DIR, "equations2d", "convkernel.py"), device,
         [('device = "cuda" if torch.cuda.is_available() else Exception("No cuda device found")',
           f'device = "{device}"')])
+    ns.vacoustic_habc = _exec_patched("seistorch.equations2d.vacoustic_habc",
+                                      os.path.join(PKG_DIR, "equations2d", "vacoustic_habc.py"), device)
     ns.vti_habc2 = importlib.import_module("seistorch.equations2d.vti_habc2")
     ns.acoustic_rho_habc = importlib.import_module("seistorch.equations2d.acoustic_rho_habc")
     ns.elastic = importlib.import_module("seistorch.equations2d.elastic")

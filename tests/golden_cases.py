@@ -11,13 +11,14 @@ FORWARD_CASES = ["acoustic_pml_o2", "acoustic_pml_o4", "acoustic_pml_o8",
                  "acoustic_pml_o4_multiple", "acoustic_habc_o2", "acoustic_habc_o4",
                  "acoustic_habc_o2_multiple", "elastic", "elastic_multiple",
                  "born_habc_o2", "born_habc_o4", "born_habc_o2_multiple", "vti_habc2", "vti_habc2_multiple",
-                 "rho_habc", "rho_habc_multiple"]
+                 "rho_habc", "rho_habc_multiple", "vacoustic_habc", "vacoustic_habc_multiple"]
 GRAD_CASES = ["grad_acoustic_pml_o4", "grad_acoustic_pml_o8", "grad_elastic"]
 BORN_GRAD_CASES = ["grad_born_habc_o2_zeroobs", "grad_born_habc_o4"]
 VTI_GRAD_CASES = ["grad_vti_habc2_zeroobs"]
 RHO_GRAD_CASES = ["grad_rho_habc_zeroobs"]
 MODEL_PARAMS = {"acoustic": ["vp"], "acoustic_habc": ["vp"], "acoustic_lsrtm_habc": ["vp", "m"],
                 "vti_habc2": ["vp", "epsilon", "delta"], "acoustic_rho_habc": ["vp", "rho"],
+                "vacoustic_habc": ["vp", "Q"],
                 "elastic": ["vp", "vs", "rho"]}
 
 

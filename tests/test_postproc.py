@@ -94,3 +94,29 @@ def test_record_filter_matches_scipy_filtfilt(freqs):
     want = sps.filtfilt(b, a, d, axis=0).astype(np.float32)
     got = postprocess.filter_records(torch.tensor(d, device="cuda"), dt, freqs, 4).cpu().numpy()
     assert rel_l2(got, want) < 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag,beta,clamp", [("pr", "PR", True), ("fr", "FR", False)])
+def test_ncg_steps_match_reference(tag, beta, clamp):
+    """Four non-linear conjugate-gradient steps (sgb_ncg_step through
+    postprocess.Cg) against the reference's Cg optimizer (optimizer.py:144-224)
+    on the same parameter and gradients: Polak-Ribiere with the 2 % / 98 %
+    quantile clamp, Fletcher-Reeves without it.  The update is lr / max|dir|
+    times a float32 direction, so the parameters agree to float32 rounding
+    (relative L2 of the change 1e-5)."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    from seistorch_gb300 import _native
+    from seistorch_gb300.postprocess import Cg
+    _native.load(build_if_missing=False)
+    z = np.load(os.path.join(GOLDEN, "postproc.npz"))
+    dev = torch.device("cuda:0")
+    p = torch.nn.Parameter(torch.tensor(z["ncg_p0"], device=dev))
+    opt = Cg([p], lr=10.0, beta_type=beta, grad_clamp=clamp, clip_value=0.02)
+    for k in range(4):
+        p.grad = torch.tensor(z["ncg_grads"][k], device=dev)
+        opt.step()
+        want = z["ncg_" + tag][k]
+        got = p.detach().cpu().numpy()
+        assert rel_l2(got - z["ncg_p0"], want - z["ncg_p0"]) < 1e-5, k
