@@ -55,9 +55,10 @@ def _case(name):
 
 def _module(g):
     from seistorch_gb300.equations2d import (acoustic, acoustic_habc, acoustic_lsrtm_habc, acoustic_rho_habc,
-                                             elastic, vti_habc2)
+                                             elastic, vacoustic_habc, vti_habc2)
     mod = {"acoustic": acoustic, "acoustic_habc": acoustic_habc, "acoustic_lsrtm_habc": acoustic_lsrtm_habc,
-           "vti_habc2": vti_habc2, "acoustic_rho_habc": acoustic_rho_habc, "elastic": elastic}[g["equation"]]
+           "vti_habc2": vti_habc2, "acoustic_rho_habc": acoustic_rho_habc, "vacoustic_habc": vacoustic_habc,
+           "elastic": elastic}[g["equation"]]
     if hasattr(mod, "spatial_order"):
         mod.spatial_order = g["order"]
     return mod

@@ -389,3 +389,28 @@ def test_diff_using_roll_edge_rule():
     assert torch.all(b2[..., -1] == 0) and torch.equal(b2[..., :-1], x[..., 1:] - x[..., :-1])
     wrap = diff_using_roll(x, -1)  # not 1 or 2: the roll's wrap stays
     assert torch.equal(wrap, x - torch.roll(x, 1, -1))
+
+
+def test_hdf5_shot_gathers_round_trip(tmp_path):
+    """HDF5 shot gathers in the reference's layout (io.py:97-115): one float32
+    dataset ``shot_<i>`` of shape (nt, nrec, nch) per shot.  A file written
+    the way the reference's ``create_hdf5_file`` + per-shot writes lay it out
+    reads back through ``SeisIO.read_shot``, and ``SeisIO.write_shots``
+    produces that layout.  Runs wherever h5py is installed."""
+    h5py = pytest.importorskip("h5py")
+    from seistorch_gb300.io import SeisIO
+    rng = np.random.default_rng(0)
+    shots = [rng.standard_normal((50, 7 + i, 2)).astype(np.float32) for i in range(3)]
+    ref_path = str(tmp_path / "ref.hdf5")
+    with h5py.File(ref_path, "w") as f:
+        for i, s in enumerate(shots):
+            f.create_dataset(f"shot_{i}", s.shape, dtype="f", chunks=True)
+            f[f"shot_{i}"][...] = s
+    for i, s in enumerate(shots):
+        assert np.array_equal(SeisIO.read_shot(ref_path, i), s)
+    out = SeisIO.write_shots(str(tmp_path / "ours.hdf5"), shots)
+    with h5py.File(out, "r") as f:
+        assert sorted(f.keys()) == ["shot_0", "shot_1", "shot_2"]
+        for i, s in enumerate(shots):
+            assert f[f"shot_{i}"].dtype == np.float32
+            assert np.array_equal(f[f"shot_{i}"][...], s)
