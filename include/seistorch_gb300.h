@@ -100,6 +100,10 @@ typedef struct {
   float *ring_store;        /* [nt][nshots][ring_size]                      */
   int32_t ckpt_every;       /* 0: none                                      */
   float *ckpt_store;        /* [nt / ckpt_every][2][nshots][nz][pitch]      */
+  float *habc_planes;       /* HABC adjoints: [5][nz][pitch] scratch for each
+                               cell's interior share and its four sides'
+                               shares (filled once per backward call), or
+                               NULL (then evaluated on the fly each step)  */
 } sgb_bs_store;
 
 /* Library identification and diagnostics. */

@@ -100,7 +100,7 @@ class HabcVjpIO(ctypes.Structure):
 class BsStore(ctypes.Structure):
     _fields_ = [("iz0", c_i32), ("iz1", c_i32), ("ix0", c_i32), ("ix1", c_i32), ("ring", c_i32),
                 ("ring_size", c_i32), ("ring_store", c_ptr), ("ckpt_every", c_i32),
-                ("ckpt_store", c_ptr)]
+                ("ckpt_store", c_ptr), ("habc_planes", c_ptr)]
 
 
 class ElasticModel(ctypes.Structure):

@@ -25,6 +25,53 @@ struct StageField {
   __device__ __forceinline__ float P(int z, int x) const { return __ldg(um + base + (long long)z * pitch + x); }
 };
 
+// The one-way blend of four cells of a row that all take the same single
+// side (or none, where b = 0): v = one b + (1 - b) y with one = (2 - lam - mu)
+// U0 + (lam + 2 mu) U1 - mu U2 + (lam - 1) P0 - lam P1, lam = 2 c dt / h,
+// mu = c^2 dt^2 / h^2 (acoustic_habc.py:79-101), in habc_side's order.
+__device__ __forceinline__ float4 blend4(const float4& y, const float4& U0, const float4& U1, const float4& U2,
+                                         const float4& P0, const float4& P1, const float4& c, const float4& b,
+                                         float lamf, float muf) {
+  float4 v;
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const float cm = comp(c, m), bm = comp(b, m);
+    const float lam = cm * lamf;
+    const float mu = cm * cm * muf;
+    const float t1 = (2.f - lam - mu) * comp(U0, m);
+    const float t2 = (lam + 2.f * mu) * comp(U1, m);
+    const float t3 = -mu * comp(U2, m);
+    const float t4 = (lam - 1.f) * comp(P0, m);
+    const float t5 = -lam * comp(P1, m);
+    const float uo = t1 + t2 + t3 + t4 + t5;
+    set_comp(v, m, uo * bm + (1.f - bm) * comp(y, m));
+  }
+  return v;
+}
+
+// Which single side every cell of the group x..x+3 in row z takes, under the
+// mask precedence and corner diagonals of acoustic_habc.py:167-202 (cells of
+// no side have b = 0): 0 top, 1 bottom, 2 left, 3 right, or -1 when the
+// group holds a corner, a diagonal or cells of two sides.
+__device__ __forceinline__ int group_side(int z, int x, int nz, int nx, int hw, bool mult) {
+  const int dB = nz - 1 - z;
+  if ((z >= hw || mult) && dB >= hw) {      // rows without a top or bottom strip
+    if (x + 3 < nx - hw) return 2;
+    if (x >= hw) return 3;
+    return -1;
+  }
+  if (!mult && z < hw && dB >= hw) {
+    const int xd = nx - hw + z;              // top-right diagonal
+    if (x > z && x + 3 < nx - 1 - z && !(xd >= x && xd <= x + 3)) return 0;
+    return -1;
+  }
+  if (dB < hw && z >= hw) {
+    const int xd = hw - 1 - dB;              // bottom-left diagonal
+    if (x > dB && x + 3 < nx - 1 - dB && !(xd >= x && xd <= x + 3)) return 1;
+  }
+  return -1;
+}
+
 // Cross-stencil x and z parts (1-D second differences, centre -2 sum c) of
 // the 4 columns of a lane, as lap_row.
 template <int R>
@@ -242,11 +289,42 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
           }
         }
         if (HB && z < a.nz && xin && (z < a.hw || z >= a.nz - a.hw || x < a.hw || x + 3 >= a.nx - a.hw)) {
-          // the one-way blend on strip cells; one copy of its code, not unrolled
-          const StageField T{su, g.z0 - R, g.x0 - LO, TZ + 2 * R, UW, a.u, a.um, fbase, a.pitch};
+          // the one-way blend on strip cells: four cells of one side at once,
+          // else cell by cell (corners, diagonals, mixed groups; one copy of
+          // its code, not unrolled)
+          const int side = (x + 3 < a.nx) ? group_side(z, x, a.nz, a.nx, a.hw, a.multiple != 0) : -1;
+          const long long ro = (long long)z * a.pitch + x;
+          if (side >= 0) {
+            const float4 cv = ldg4(a.vp + ro), bv = ldg4(a.hb + ro);
+            float4 U1, U2, P1;
+            if (side <= 1) {
+              const int dz = side == 0 ? 1 : -1;
+              auto urow = [&](int zz) -> float4 {
+                const int r = zz - (g.z0 - R);
+                return (r >= 0 && r < TZ + 2 * R) ? lds4(su + r * UW + LO + 4 * lane)
+                                                  : ldg4(a.u + fbase + (long long)zz * a.pitch + x);
+              };
+              U1 = urow(z + dz);
+              U2 = urow(z + 2 * dz);
+              P1 = ldg4(a.um + fbase + ro + dz * (long long)a.pitch);
+            } else if (side == 2) {
+              const float4 r4 = lds4(srow + LO + 4 + 4 * lane);
+              U1 = make_float4(c.y, c.z, c.w, r4.x);
+              U2 = make_float4(c.z, c.w, r4.x, r4.y);
+              P1 = make_float4(vm[i].y, vm[i].z, vm[i].w, __ldg(a.um + fbase + ro + 4));
+            } else {
+              const float4 l4 = lds4(srow + LO - 4 + 4 * lane);
+              U1 = make_float4(l4.w, c.x, c.y, c.z);
+              U2 = make_float4(l4.z, l4.w, c.x, c.y);
+              P1 = make_float4(__ldg(a.um + fbase + ro - 1), vm[i].x, vm[i].y, vm[i].z);
+            }
+            y = blend4(y, c, U1, U2, vm[i], P1, cv, bv, a.lamf, a.muf);
+          } else {
+            const StageField T{su, g.z0 - R, g.x0 - LO, TZ + 2 * R, UW, a.u, a.um, fbase, a.pitch};
 #pragma unroll 1
-          for (int m = 0; m < 4; ++m)
-            if (x + m < a.nx) set_comp(y, m, habc_point(T, a, z, x + m, comp(y, m)));
+            for (int m = 0; m < 4; ++m)
+              if (x + m < a.nx) set_comp(y, m, habc_point(T, a, z, x + m, comp(y, m)));
+          }
         }
         if (src.mask) apply_sources(src, i, lane, 1.f, y);
         if (z < a.nz && xin) {

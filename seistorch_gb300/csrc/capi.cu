@@ -99,7 +99,8 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
                             const Ring& ring, const float* la1, const float* la2, float* lout, const float* uj,
                             const float* ujm1, float* uout, float* grad, const float* ring_in, int t_src,
                             const float* resid, const float* kz, float* grad2, const float* rho_c,
-                            float* grad_rho, cudaStream_t s);
+                            float* grad_rho, cudaStream_t s, const float* wpl = nullptr);
+cudaError_t launch_habc_shares(const sgb_grid& g, const sgb_acoustic_model& m, float* planes, cudaStream_t s);
 
 }  // namespace sgb
 
@@ -808,6 +809,13 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
     if ((acq->nsrc > 0 && acq->src_ptr == nullptr)) return SGB_ERR_ARG;
     int uj = ucur, ujm1 = uprev, ufree = 3 - ucur - uprev;
     int l1 = 0, l2 = 1, lfree = 2;
+    // the cells' static interior / side shares, once for the whole reverse loop
+    const float* wpl = nullptr;
+    if (bs->habc_planes != nullptr) {
+      if (!aligned16(bs->habc_planes)) return SGB_ERR_ALIGN;
+      SGB_CUDA_CHECK(launch_habc_shares(*grid, *model, bs->habc_planes, s));
+      wpl = bs->habc_planes;
+    }
     for (int j = nt; j >= 2; --j) {
       const int n = j - 1;
       const bool ck = K > 0 && n % K == 0 && n / K >= 1 && n / K <= nslots;
@@ -819,7 +827,7 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
       const float* resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
       SGB_CUDA_CHECK(launch_habc_bwd(*grid, *model, *acq, ring, lbuf[l1], lbuf[l2], lbuf[lfree], ubuf[uj],
                                      ubuf[ujm1], j >= 3 ? ubuf[ufree] : nullptr, grad_shot, ring_in, j - 1, resid,
-                                     kz, grad_shot2, rho_c, rho_c != nullptr ? grad_shot : nullptr, s));
+                                     kz, grad_shot2, rho_c, rho_c != nullptr ? grad_shot : nullptr, s, wpl));
       if (ck && j >= 3) {
         const float* slot = bs->ckpt_store + (long long)(n / K - 1) * 2 * field;
         SGB_CUDA_CHECK(

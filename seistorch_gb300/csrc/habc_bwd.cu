@@ -109,6 +109,8 @@ struct HabcBwdArgs {
   // cells [tz0, tz1) x [tx0, tx1) (tx0, tx1 multiples of 4) are done by
   // habc_bwd_interior_kernel; empty (tx1 = tx0) when that kernel is not used
   int tz0, tz1, tx0, tx1;
+  // [5][nz][pitch] static shares (wi, wt, wb, wl, wr) of every cell, or null
+  const float* __restrict__ wpl;
 };
 
 // Is the group of four columns at x0 (a multiple of 4) in row z one of the
@@ -721,100 +723,26 @@ __global__ void __launch_bounds__(256) habc_step_vjp_kernel(const HabcVjpArgs a)
 }
 
 
-// ------------------------------------------- line walkers + all-cell tiles ---
-// The plain / VTI / Born reverse step in two kinds of launch.  The one-way
-// transposes are gathered along each strip's inward normal by one thread per
-// (shot, line) (habc_oneway_tb_kernel: top and bottom lines, one per column;
-// habc_oneway_lr_kernel: left and right lines, one per row), which evaluate
-// each cell's side share once and carry the previous two cells' terms in
-// registers.  They write their sums into the output adjoint La_j for the
-// cells within hw of an edge (the only ones they reach).  The tiled kernel
-// (habc_bwd_tile_kernel) then computes every cell: the interior-share
-// weighted transpose 2 wi La1 + L(k wi La1) - wi La2 from shared-memory tiles
-// of k wi La1 and U_{j-1}, plus the one-way sum for band cells, plus the
-// receiver residuals; and the gradient term and the reconstruction inside the
-// box, the saved ring (or 0) outside it.
-
-// The one-way line of side `side` through the edge cell (ze, xe) with inward
-// step (sz, sx): the transposes of the strip cells at depths 0 .. hw-1 into
-// the cells at depths 0 .. hw (lines of one shot, fields offset by fb).
-// `keep(z, x)` says whether the cell already holds a partial sum to add to.
-template <class Keep>
-__device__ __forceinline__ void oneway_line(const HabcBwdArgs& a, long long fb, int ze, int xe, int sz, int sx,
-                                            int side, Keep keep) {
-  const int hw = a.hw;
-  const bool mult = a.multiple != 0;
-  const float* l1 = a.la1 + fb;
-  const float* l2 = a.la2 + fb;
-  float* out = a.lout + fb;
-  const long long step = (long long)sz * a.pitch + sx;
-  long long o = (long long)ze * a.pitch + xe;
-  // terms of the cells one and two steps back: C l1 - D l2 and -E l1
-  float c1 = 0.f, e2 = 0.f, e1 = 0.f;
-  float acc0 = 0.f, wrap = 0.f;
-  for (int k = 0; k <= hw; ++k, o += step) {
-    const int z = ze + k * sz, x = xe + k * sx;
-    float v = c1 + e2;
-    float cn = 0.f, en = 0.f;
-    if (k < hw) {
-      const HabcW w = habc_weights(z, x, a.nz, a.nx, hw, mult, __ldg(a.hb + (long long)z * a.pitch + x));
-      const float ws = side == 0 ? w.wt : side == 1 ? w.wb : side == 2 ? w.wl : w.wr;
-      if (ws != 0.f) {
-        const float c = __ldg(a.vp + (long long)z * a.pitch + x);
-        const float lam = c * a.lamf, mu = c * c * a.muf;
-        const float u1 = l1[o], u2 = l2[o];
-        v += ws * ((2.f - lam - mu) * u1 + (lam - 1.f) * u2);
-        cn = ws * ((lam + 2.f * mu) * u1 - lam * u2);
-        en = -ws * mu * u1;
-        if (k == hw - 1) wrap = en;  // its second neighbour is the edge cell
-      }
-    }
-    // the depth-(k-2) cell's p2 is this cell unless it wrapped (k - 2 = hw - 1)
-    e2 = e1;
-    e1 = (k + 1 < hw) ? en : 0.f;
-    c1 = cn;
-    if (k == 0) {
-      acc0 = v;
-    } else {
-      out[o] = keep(z, x) ? out[o] + v : v;
-    }
-  }
-  o = (long long)ze * a.pitch + xe;
-  out[o] = keep(ze, xe) ? out[o] + acc0 + wrap : acc0 + wrap;
-}
-
-__global__ void __launch_bounds__(128) habc_oneway_tb_kernel(const HabcBwdArgs a) {
-  const long long n = (long long)a.nshots * a.nx;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int b = (int)(i / a.nx), x = (int)(i - (long long)b * a.nx);
-    const long long fb = (long long)b * a.sstride;
-    const int hw = a.hw;
-    oneway_line(a, fb, 0, x, 1, 0, 0, [](int, int) { return false; });
-    oneway_line(a, fb, a.nz - 1, x, -1, 0, 1, [&](int z, int) { return z <= hw; });
-  }
-}
-
-__global__ void __launch_bounds__(128) habc_oneway_lr_kernel(const HabcBwdArgs a) {
-  const long long n = (long long)a.nshots * a.nz;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int b = (int)(i / a.nz), z = (int)(i - (long long)b * a.nz);
-    const long long fb = (long long)b * a.sstride;
-    const int hw = a.hw, nz = a.nz;
-    const bool tb = z <= hw || z >= nz - 1 - hw;  // written by the top / bottom lines
-    oneway_line(a, fb, z, 0, 0, 1, 2, [&](int, int) { return tb; });
-    oneway_line(a, fb, z, a.nx - 1, 0, -1, 3, [&](int, int x) { return tb || x <= hw; });
-  }
-}
-
-// All cells of a reverse step, tile 8 x 128 with block (32, 8) (lane: four
-// columns).  La_j = 2 wi La1 + L(k wi La1) - wi La2 (VTI: x neighbours by
-// kx, z neighbours by kz) + one-way sums (band cells, from lout) + residuals.
-template <int R, bool VTI>
+// --------------------------------------------------- all-cell tiles ---
+// The plain / VTI / Born reverse step in one launch, tile 8 x 128 with block
+// (32, 8) (lane: four columns).  La_j = 2 wi La1 + L(k wi La1) - wi La2 (VTI:
+// x neighbours by kx, z neighbours by kz) from shared-memory tiles of
+// k wi La1 and U_{j-1}; tiles within reach of a strip also stage La1 and La2
+// (two-row halo) and add the one-way transposes of the four sides, with each
+// cell's interior and side shares read from the five planes that
+// habc_shares_kernel fills once per reverse loop; then the receiver
+// residuals, the gradient term and the reconstruction inside the box, the
+// saved ring (or 0) outside it.
+template <int R, bool VTI, bool NEAR>
 __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a) {
-  constexpr int ROWS = HT_Z + 2 * R, W = HT_X + 2 * HT_H;
+  // row halo: the stencil's R, and 2 for the one-way lines (q - d, q - 2d)
+  constexpr int HR = R < 2 ? 2 : R;
+  constexpr int ROWS = HT_Z + 2 * HR, W = HT_X + 2 * HT_H;
   __shared__ __align__(16) float s_kl[ROWS][W];             // k wi La1 (VTI: kx wi La1)
   __shared__ __align__(16) float s_kzl[VTI ? ROWS : 1][W];  // VTI: kz wi La1
   __shared__ __align__(16) float s_u[ROWS][W];
+  __shared__ __align__(16) float s_l1[NEAR ? ROWS : 1][W];  // La1 and La2 (tiles near a strip only)
+  __shared__ __align__(16) float s_l2[NEAR ? ROWS : 1][W];
   const int b = blockIdx.z;
   const int z0 = blockIdx.y * HT_Z, x0 = blockIdx.x * HT_X;
   const long long fb = (long long)b * a.sstride;
@@ -823,22 +751,33 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const int hw = a.hw;
   const bool mult = a.multiple != 0;
-  // does any cell of the tile or its halo have an interior share below 1?
-  const bool near = hw > 0 && ((!mult && z0 - R < hw) || z0 + HT_Z + R > a.nz - hw || x0 - HT_H < hw ||
-                                x0 + HT_X + HT_H > a.nx - hw);
+  const long long pl = (long long)a.nz * a.pitch;
+  // does any cell of the tile or its halo have an interior share below 1, or
+  // lie within reach of a one-way line (depth <= hw)?
+  const bool near = hw > 0 && ((!mult && z0 - HR <= hw) || z0 + HT_Z + HR >= a.nz - 1 - hw ||
+                                x0 - HT_H <= hw || x0 + HT_X + HT_H >= a.nx - 1 - hw);
+  // two launches share the grid: the NEAR instantiation takes the tiles
+  // within reach of a strip, the other the rest (with none of the strip code)
+  if (near != NEAR) return;
   auto wi_at = [&](int z, int x) -> float {
-    return near ? habc_weights(z, x, a.nz, a.nx, hw, mult, __ldg(a.hb + (long long)z * a.pitch + x)).wi : 1.f;
+    if (!near) return 1.f;
+    const long long oo = (long long)z * a.pitch + x;
+    if (a.wpl != nullptr) return __ldg(a.wpl + oo);
+    const float bb = __ldg(a.hb + oo);  // b = 0: no side share, wi = 1
+    return bb == 0.f ? 1.f : habc_weights(z, x, a.nz, a.nx, hw, mult, bb).wi;
   };
   for (int c = tid; c < ROWS * (W / 4); c += 256) {
     const int rr = c / (W / 4), cc = c - rr * (W / 4);
-    const int z = z0 - R + rr, x = x0 - HT_H + 4 * cc;
+    const int z = z0 - HR + rr, x = x0 - HT_H + 4 * cc;
     float kl[4] = {0.f, 0.f, 0.f, 0.f}, kzl[4] = {0.f, 0.f, 0.f, 0.f}, uu[4] = {0.f, 0.f, 0.f, 0.f};
+    float r1[4] = {0.f, 0.f, 0.f, 0.f}, r2[4] = {0.f, 0.f, 0.f, 0.f};
     if (z >= 0 && z < a.nz && x >= 0 && x < a.nx) {
       const long long o = (long long)z * a.pitch + x;
       const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
       const float4 l4 = *reinterpret_cast<const float4*>(l1 + o);
       const float4 q4 = VTI ? __ldg(reinterpret_cast<const float4*>(a.kz + o)) : k4;
       const float4 v4 = *reinterpret_cast<const float4*>(u1 + o);
+      const float4 m4 = NEAR ? *reinterpret_cast<const float4*>(a.la2 + fb + o) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
         if (x + m < a.nx) {
@@ -846,33 +785,102 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
           kl[m] = comp(k4, m) * w * comp(l4, m);
           if (VTI) kzl[m] = comp(q4, m) * w * comp(l4, m);
           uu[m] = comp(v4, m);
+          r1[m] = comp(l4, m);
+          r2[m] = comp(m4, m);
         }
       }
     }
     *reinterpret_cast<float4*>(&s_kl[rr][4 * cc]) = make_float4(kl[0], kl[1], kl[2], kl[3]);
     if (VTI) *reinterpret_cast<float4*>(&s_kzl[rr][4 * cc]) = make_float4(kzl[0], kzl[1], kzl[2], kzl[3]);
     *reinterpret_cast<float4*>(&s_u[rr][4 * cc]) = make_float4(uu[0], uu[1], uu[2], uu[3]);
+    if constexpr (NEAR) {
+      *reinterpret_cast<float4*>(&s_l1[rr][4 * cc]) = make_float4(r1[0], r1[1], r1[2], r1[3]);
+      *reinterpret_cast<float4*>(&s_l2[rr][4 * cc]) = make_float4(r2[0], r2[1], r2[2], r2[3]);
+    }
   }
   __syncthreads();
   const int z = z0 + threadIdx.y, x = x0 + 4 * threadIdx.x;
   if (z >= a.nz || x >= a.nx) return;
-  const int rr = R + threadIdx.y, cx = HT_H + 4 * threadIdx.x;
+  const int rr = HR + threadIdx.y, cx = HT_H + 4 * threadIdx.x;
   const long long o = (long long)z * a.pitch + x;
   const float4 l2v = *reinterpret_cast<const float4*>(a.la2 + fb + o);
   const float4 l1c = *reinterpret_cast<const float4*>(l1 + o);
   const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
   const float4 kz4 = VTI ? __ldg(reinterpret_cast<const float4*>(a.kz + o)) : k4;
-  // band cells (within hw of an edge) carry the one-way sums in lout
-  const bool band_rows = hw > 0 && (z <= hw || z >= a.nz - 1 - hw);
-  const float4 ow4 = (band_rows || (hw > 0 && (x <= hw || x + 3 >= a.nx - 1 - hw)))
-                         ? *reinterpret_cast<const float4*>(a.lout + fb + o) : make_float4(0.f, 0.f, 0.f, 0.f);
+  // one-way transposes of side `sd` at cell (z, xm) of local column cxm:
+  // strip cells p = q, q - d, q - 2d (staged La1 / La2) and the wrap of the
+  // line's depth hw-1 cell into its edge cell (global)
+  auto share = [&](int sd, int pz, int px) -> float {
+    const long long oo = (long long)pz * a.pitch + px;
+    if (a.wpl != nullptr) return __ldg(a.wpl + (1 + sd) * pl + oo);
+    const float bb = __ldg(a.hb + oo);
+    if (bb == 0.f) return 0.f;
+    const HabcW w = habc_weights(pz, px, a.nz, a.nx, hw, mult, bb);
+    return sd == 0 ? w.wt : sd == 1 ? w.wb : sd == 2 ? w.wl : w.wr;
+  };
+  auto oneway = [&](int sd, int dq, int sz, int sx, int xm, int cxm) -> float {
+    if (dq > hw) return 0.f;
+    float acc = 0.f;
+    if (dq < hw) {
+      const float ws = share(sd, z, xm);
+      if (ws != 0.f) {
+        const float c = __ldg(a.vp + (long long)z * a.pitch + xm);
+        const float lam = c * a.lamf, mu = c * c * a.muf;
+        acc += ws * ((2.f - lam - mu) * s_l1[rr][cxm] + (lam - 1.f) * s_l2[rr][cxm]);
+      }
+    }
+    if (dq >= 1) {
+      const int pz = z - sz, px = xm - sx;
+      const float ws = share(sd, pz, px);
+      if (ws != 0.f) {
+        const float c = __ldg(a.vp + (long long)pz * a.pitch + px);
+        const float lam = c * a.lamf, mu = c * c * a.muf;
+        acc += ws * ((lam + 2.f * mu) * s_l1[rr - sz][cxm - sx] - lam * s_l2[rr - sz][cxm - sx]);
+      }
+    }
+    if (dq >= 2) {
+      const int pz = z - 2 * sz, px = xm - 2 * sx;
+      const float ws = share(sd, pz, px);
+      if (ws != 0.f) {
+        const float c = __ldg(a.vp + (long long)pz * a.pitch + px);
+        acc -= ws * c * c * a.muf * s_l1[rr - 2 * sz][cxm - 2 * sx];
+      }
+    }
+    if (dq == 0) {
+      const int pz = z + (hw - 1) * sz, px = xm + (hw - 1) * sx;
+      if (pz >= 0 && pz < a.nz && px >= 0 && px < a.nx) {
+        const float ws = share(sd, pz, px);
+        if (ws != 0.f) {
+          const long long oo = (long long)pz * a.pitch + px;
+          const float c = __ldg(a.vp + oo);
+          acc -= ws * c * c * a.muf * l1[oo];
+        }
+      }
+    }
+    return acc;
+  };
+  // the one-way sums of the four cells: one copy of the code for every
+  // (cell, side) pair (not unrolled, so the kernel stays small)
+  float4 ow4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if constexpr (NEAR) {
+#pragma unroll 1
+    for (int t = 0; t < 16; ++t) {
+      const int m = t >> 2, sd = t & 3;
+      const int xm = x + m;
+      if (xm >= a.nx) continue;
+      const int dq = sd == 0 ? z : sd == 1 ? a.nz - 1 - z : sd == 2 ? xm : a.nx - 1 - xm;
+      if (dq > hw) continue;
+      const int sz = sd == 0 ? 1 : sd == 1 ? -1 : 0, sx = sd == 2 ? 1 : sd == 3 ? -1 : 0;
+      set_comp(ow4, m, comp(ow4, m) + oneway(sd, dq, sz, sx, xm, cx + m));
+    }
+  }
   const float ch = 0.5f * a.w.c[0];
   float v[4], L[4], Lz[4];
 #pragma unroll
   for (int m = 0; m < 4; ++m) {
     const int xm = x + m;
     const float wq = (xm < a.nx) ? wi_at(z, xm) : 0.f;
-    const bool band = band_rows || (hw > 0 && (xm <= hw || xm >= a.nx - 1 - hw));
+    const float ow = NEAR ? comp(ow4, m) : 0.f;
     float lap, lu, luz = 0.f;
     if (VTI) {
       float lx = ch * s_kl[rr][cx + m], lz = ch * s_kzl[rr][cx + m];
@@ -896,7 +904,7 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
         lu += a.w.c[j] * (s_u[rr - j][cx + m] + s_u[rr + j][cx + m] + s_u[rr][cx + m - j] + s_u[rr][cx + m + j]);
       }
     }
-    v[m] = (xm < a.nx) ? 2.f * wq * comp(l1c, m) + lap - wq * comp(l2v, m) + (band ? comp(ow4, m) : 0.f) : 0.f;
+    v[m] = (xm < a.nx) ? 2.f * wq * comp(l1c, m) + lap - wq * comp(l2v, m) + ow : 0.f;
     L[m] = lu;
     Lz[m] = luz;
   }
@@ -937,6 +945,27 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
       }
     }
   }
+  if (row_in && x >= a.ring.ix0 && x + 3 < a.ring.ix1) {
+    // all four columns inside the box: vector gradient update and reconstruction
+    float4* gp = reinterpret_cast<float4*>(a.grad + fb + o);
+    const float4 g0 = *gp;
+    if (VTI) {
+      *gp = make_float4(g0.x + v[0] * L[0], g0.y + v[1] * L[1], g0.z + v[2] * L[2], g0.w + v[3] * L[3]);
+      float4* gq = reinterpret_cast<float4*>(a.grad2 + fb + o);
+      const float4 h0 = *gq;
+      *gq = make_float4(h0.x + v[0] * Lz[0], h0.y + v[1] * Lz[1], h0.z + v[2] * Lz[2], h0.w + v[3] * Lz[3]);
+    } else {
+      *gp = make_float4(g0.x + v[0] * k4.x * L[0], g0.y + v[1] * k4.y * L[1], g0.z + v[2] * k4.z * L[2],
+                        g0.w + v[3] * k4.w * L[3]);
+    }
+    if (a.uout != nullptr) {
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+        uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + comp(k4, m) * L[m] + (VTI ? comp(kz4, m) * Lz[m] : 0.f);
+      *reinterpret_cast<float4*>(a.uout + fb + o) = make_float4(uo[0], uo[1], uo[2], uo[3]);
+    }
+    return;
+  }
 #pragma unroll
   for (int m = 0; m < 4; ++m) {
     const int xm = x + m;
@@ -960,14 +989,39 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
   if (a.uout != nullptr) *reinterpret_cast<float4*>(a.uout + fb + o) = make_float4(uo[0], uo[1], uo[2], uo[3]);
 }
 
+
+// The static shares of every cell: wi and the four sides' b * share.
+__global__ void habc_shares_kernel(int nz, int nx, int pitch, int hw, int mult, const float* __restrict__ hb,
+                                   float* __restrict__ out) {
+  const long long pl = (long long)nz * pitch;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < pl; i += (long long)gridDim.x * blockDim.x) {
+    const int z = (int)(i / pitch), x = (int)(i - (long long)z * pitch);
+    HabcW w{1.f, 0.f, 0.f, 0.f, 0.f};
+    if (x < nx) w = habc_weights(z, x, nz, nx, hw, mult != 0, hb[i]);
+    out[i] = w.wi;
+    out[pl + i] = w.wt;
+    out[2 * pl + i] = w.wb;
+    out[3 * pl + i] = w.wl;
+    out[4 * pl + i] = w.wr;
+  }
+}
 }  // namespace
+
+cudaError_t launch_habc_shares(const sgb_grid& g, const sgb_acoustic_model& m, float* planes, cudaStream_t s) {
+  const long long pl = (long long)g.nz * g.pitch;
+  long long blocks = (pl + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  habc_shares_kernel<<<(unsigned)blocks, 256, 0, s>>>(g.nz, g.nx, g.pitch, m.habc_width, m.multiple, m.damp, planes);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
                             const Ring& ring, const float* la1, const float* la2, float* lout, const float* uj,
                             const float* ujm1, float* uout, float* grad, const float* ring_in, int t_src,
                             const float* resid, const float* kz, float* grad2, const float* rho_c,
-                            float* grad_rho, cudaStream_t s) {
+                            float* grad_rho, cudaStream_t s, const float* wpl) {
   HabcBwdArgs a;
+  a.wpl = wpl;
   a.kz = kz;
   a.grad2 = grad2;
   a.rho_c = rho_c;
@@ -1010,23 +1064,22 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
   const int R = a.R, far = a.hw + R;
   const bool vti = kz != nullptr;
   if (rho_c == nullptr && R <= HT_H) {
-    // plain / VTI / Born: one-way sums along the strip lines, then every cell in tiles
+    // plain / VTI / Born: every cell in tiles
     a.tz0 = a.tz1 = a.tx0 = a.tx1 = 0;
-    if (a.hw > 0) {
-      const long long ntb = (long long)g.nshots * g.nx, nlr = (long long)g.nshots * g.nz;
-      habc_oneway_tb_kernel<<<(unsigned)((ntb + 127) / 128), 128, 0, s>>>(a);
-      habc_oneway_lr_kernel<<<(unsigned)((nlr + 127) / 128), 128, 0, s>>>(a);
-    }
     const dim3 grid((unsigned)((g.nx + HT_X - 1) / HT_X), (unsigned)((g.nz + HT_Z - 1) / HT_Z), (unsigned)g.nshots);
     switch (R * 2 + (vti ? 1 : 0)) {
-      case 2: habc_bwd_tile_kernel<1, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-      case 3: habc_bwd_tile_kernel<1, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-      case 4: habc_bwd_tile_kernel<2, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-      case 5: habc_bwd_tile_kernel<2, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-      case 6: habc_bwd_tile_kernel<3, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-      case 7: habc_bwd_tile_kernel<3, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-      case 8: habc_bwd_tile_kernel<4, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-      case 9: habc_bwd_tile_kernel<4, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
+#define SGB_TILE2(RR, V)                                                    \
+  habc_bwd_tile_kernel<RR, V, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); \
+  if (a.hw > 0) habc_bwd_tile_kernel<RR, V, true><<<grid, dim3(32, HT_Z), 0, s>>>(a);
+      case 2: SGB_TILE2(1, false) break;
+      case 3: SGB_TILE2(1, true) break;
+      case 4: SGB_TILE2(2, false) break;
+      case 5: SGB_TILE2(2, true) break;
+      case 6: SGB_TILE2(3, false) break;
+      case 7: SGB_TILE2(3, true) break;
+      case 8: SGB_TILE2(4, false) break;
+      case 9: SGB_TILE2(4, true) break;
+#undef SGB_TILE2
       default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

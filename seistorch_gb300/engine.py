@@ -332,8 +332,11 @@ class AcousticPropagator:
         nslots = nt // K if K > 0 else 0
         state.ckpt_store = (torch.empty(max(nslots, 1), 2, *field, dtype=torch.float32, device=dev)
                             if K > 0 else None)
+        # the HABC adjoints read each cell's static interior / side shares from five planes
+        state.habc_planes = (torch.empty(5, self.nz, self.pitch, dtype=torch.float32, device=dev)
+                             if self.boundary == BOUNDARY_HABC else None)
         state.bs = N.BsStore(iz0, iz1, ix0, ix1, r, size.value, N.ptr(state.ring_store), K,
-                             N.ptr(state.ckpt_store))
+                             N.ptr(state.ckpt_store), N.ptr(state.habc_planes))
         return state.bs
 
     def backward(self, state, acq, grad_records):

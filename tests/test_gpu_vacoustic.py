@@ -93,5 +93,6 @@ def test_wavernn_dispatches_vacoustic(dev):
     with torch.no_grad():
         r1 = engine.vacoustic_records(t(g["models"]["vp"]), t(g["models"]["Q"]), prop, t(g["d"]), acq)
     r2 = engine.vacoustic_records(t(g["models"]["vp"], True), t(g["models"]["Q"]), prop, t(g["d"]), acq).detach()
-    # the native loop and the step-by-step autograd loop are the same arithmetic
-    assert rel_l2(r2.cpu().numpy(), r1.cpu().numpy()) < 1e-6
+    # the native loop (tile pipeline) and the step-by-step autograd loop (the
+    # per-step kernel) compute the same update in a different float order
+    assert rel_l2(r2.cpu().numpy(), r1.cpu().numpy()) < 1e-5
