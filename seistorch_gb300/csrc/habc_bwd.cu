@@ -21,14 +21,15 @@
 // dJ/dvp += La_j (2k / vp) L(U_{j-1}) there; the ring of order/2 cells
 // around the box comes from the forward's store.
 //
-// Two kernels share each reverse step: habc_bwd_interior_kernel takes the
-// cells at least hw + R from every strip side (there wi = 1 for the whole
-// stencil and no one-way line reaches), with k La1 and U_{j-1} tiles staged
-// in shared memory; habc_bwd_kernel takes the remaining frame of cells one
-// by one.  The same equations carry the VTI (k Lx + kz Lz, vti_habc2.py),
-// variable-density (C D(U), acoustic_rho_habc.py) and Born (the scattered
-// field's adjoint against the background's reconstruction,
-// acoustic_lsrtm_habc.py) gradients.
+// One kernel takes each reverse step (habc_bwd_tile_kernel, 8 x 128 tiles
+// staged in shared memory), in two instantiations: tiles out of reach of
+// every strip (wi = 1 over the whole stencil, no one-way line) and tiles
+// near a strip (static shares from planes filled once per reverse loop,
+// one-way transposes gathered from the staged La1 / La2).  The same
+// equations carry the VTI (k Lx + kz Lz, vti_habc2.py), variable-density
+// (C D(U), acoustic_rho_habc.py) and Born (the scattered field's adjoint
+// against the background's reconstruction, acoustic_lsrtm_habc.py)
+// gradients.
 #include "sgb_common.cuh"
 #include "acoustic_args.cuh"
 
@@ -106,18 +107,9 @@ struct HabcBwdArgs {
   const int* __restrict__ rec_col;
   int nch;
   const float* __restrict__ resid;
-  // cells [tz0, tz1) x [tx0, tx1) (tx0, tx1 multiples of 4) are done by
-  // habc_bwd_interior_kernel; empty (tx1 = tx0) when that kernel is not used
-  int tz0, tz1, tx0, tx1;
   // [5][nz][pitch] static shares (wi, wt, wb, wl, wr) of every cell, or null
   const float* __restrict__ wpl;
 };
-
-// Is the group of four columns at x0 (a multiple of 4) in row z one of the
-// interior kernel's?  The two kernels split the cells with this predicate.
-__device__ __forceinline__ bool in_tiled(const HabcBwdArgs& a, int z, int x0) {
-  return z >= a.tz0 && z < a.tz1 && x0 >= a.tx0 && x0 + 4 <= a.tx1;
-}
 
 __device__ __forceinline__ float ldz(const float* p, int z, int x, int nz, int nx, int pitch) {
   return (z >= 0 && z < nz && x >= 0 && x < nx) ? __ldg(p + (long long)z * pitch + x) : 0.f;
@@ -194,351 +186,8 @@ __device__ __forceinline__ float oneway_t(const Args& a, const float* l1, const 
   return acc;
 }
 
-// Cells of a shot outside the interior kernel's region, numbered rows
-// [0, tz0) in full, then rows [tz0, tz1) without columns [tx0, tx1), then
-// rows [tz1, nz) in full (all cells when the region is empty).
-struct FrameCells {
-  int nx, tz0, tz1, tx0, tx1, midw;
-  long long top, mid, plane;
-  __host__ __device__ FrameCells(const HabcBwdArgs& a)
-      : nx(a.nx), tz0(a.tz0), tz1(a.tz1), tx0(a.tx0), tx1(a.tx1), midw(a.tx0 + (a.nx - a.tx1)) {
-    top = (long long)tz0 * nx;
-    mid = (long long)(tz1 - tz0) * midw;
-    plane = top + mid + (long long)(a.nz - tz1) * nx;
-  }
-  __host__ __device__ void cell(long long r, int& z, int& x) const {
-    if (r < top) {
-      z = (int)(r / nx);
-      x = (int)(r % nx);
-    } else if (r < top + mid) {
-      const long long q = r - top;
-      const int c = (int)(q % midw);
-      z = tz0 + (int)(q / midw);
-      x = c < tx0 ? c : tx1 + (c - tx0);
-    } else {
-      const long long q = r - top - mid;
-      z = tz1 + (int)(q / nx);
-      x = (int)(q % nx);
-    }
-  }
-};
-
-// EQ: 0 plain (acoustic_habc, Born), 1 VTI, 2 variable density -- one
-// instantiation per equation, so each carries only its own branches.
-template <int R, int EQ>
-__global__ void __launch_bounds__(256, 4) habc_bwd_kernel(const HabcBwdArgs a) {
-  const FrameCells fc(a);
-  const long long plane = fc.plane;
-  const long long total = plane * a.nshots;
-  const bool mult = a.multiple != 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int b = (int)(i / plane);
-    int z, x;
-    fc.cell(i - (long long)b * plane, z, x);
-    const long long fb = (long long)b * a.sstride;
-    const long long o = (long long)z * a.pitch + x;
-    const float* l1 = a.la1 + fb;
-    const float* l2 = a.la2 + fb;
-    const float kq = __ldg(a.k + o);
-    // Cells at least hw + R from every strip side: every stencil neighbour
-    // lies in the grid with wi = 1 and no one-way line reaches them, so the
-    // transpose is the plain 2 La1 + L(k La1) - La2.  With `multiple` the
-    // top has no strip, but the stencil must still stay below row 0.
-    const int far = a.hw + R;
-    const bool interior =
-        z >= (mult ? R : far) && a.nz - 1 - z >= far && x >= far && a.nx - 1 - x >= far;
-    constexpr bool vti = EQ == 1;
-    constexpr bool rho = EQ == 2 && R == 1;
-    const float kzq = vti ? __ldg(a.kz + o) : 0.f;
-    const float ch = 0.5f * a.w.c[0];  // centre of the 1-D second difference
-    const long long pl = (long long)a.nz * a.pitch;
-    float v;
-    if (rho) {
-      // transpose of C D: the cell's own -(bx+ + bx- + bz+ + bz-) C w, plus
-      // bx+ C w of the left neighbour, bx- C w of the right one, bz+ C w of
-      // the row above and bz- C w of the row below (w = wi La1)
-      auto cw = [&](int zz, int xx, int q) -> float {  // C * coefficient q * wi * La1 at (zz, xx)
-        if (zz < 0 || zz >= a.nz || xx < 0 || xx >= a.nx) return 0.f;
-        const long long oo = (long long)zz * a.pitch + xx;
-        const float wi = interior ? 1.f : habc_weights(zz, xx, a.nz, a.nx, a.hw, mult, __ldg(a.hb + oo)).wi;
-        return __ldg(a.rho_c + oo) * __ldg(a.rho_c + q * pl + oo) * wi * l1[oo];
-      };
-      const float wq = interior ? 1.f : habc_weights(z, x, a.nz, a.nx, a.hw, mult, __ldg(a.hb + o)).wi;
-      const float sum = __ldg(a.rho_c + pl + o) + __ldg(a.rho_c + 2 * pl + o) + __ldg(a.rho_c + 3 * pl + o) +
-                        __ldg(a.rho_c + 4 * pl + o);
-      const float own = -sum * __ldg(a.rho_c + o) * wq * l1[o];
-      v = 2.f * wq * l1[o] + (own + cw(z, x - 1, 1) + cw(z, x + 1, 2) + cw(z - 1, x, 3) + cw(z + 1, x, 4)) -
-          wq * l2[o];
-      if (!interior) {
-        v += oneway_t<true, true>(a, l1, l2, z, x, z, 1, 0, 0);
-        v += oneway_t<true, true>(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
-        v += oneway_t<true, true>(a, l1, l2, z, x, x, 0, 1, 2);
-        v += oneway_t<true, true>(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
-      }
-    } else if (interior && vti) {
-      float lx = ch * kq * l1[o], lz = ch * kzq * l1[o];
-      for (int j = 1; j <= R; ++j) {
-        const long long up = o - (long long)j * a.pitch, dn = o + (long long)j * a.pitch;
-        lx += a.w.c[j] * (__ldg(a.k + o - j) * l1[o - j] + __ldg(a.k + o + j) * l1[o + j]);
-        lz += a.w.c[j] * (__ldg(a.kz + up) * l1[up] + __ldg(a.kz + dn) * l1[dn]);
-      }
-      v = 2.f * l1[o] + lx + lz - l2[o];
-    } else if (interior) {
-      float lap = a.w.c[0] * kq * l1[o];
-      for (int j = 1; j <= R; ++j) {
-        const long long up = o - (long long)j * a.pitch, dn = o + (long long)j * a.pitch;
-        lap += a.w.c[j] * (__ldg(a.k + up) * l1[up] + __ldg(a.k + dn) * l1[dn] + __ldg(a.k + o - j) * l1[o - j] +
-                           __ldg(a.k + o + j) * l1[o + j]);
-      }
-      v = 2.f * l1[o] + lap - l2[o];
-    } else if (vti) {
-      // x neighbours weighted by k, z neighbours by kz, each with its interior share
-      auto wl = [&](int zz, int xx, const float* kp) -> float {
-        if (zz < 0 || zz >= a.nz || xx < 0 || xx >= a.nx) return 0.f;
-        const long long oo = (long long)zz * a.pitch + xx;
-        const HabcW w = habc_weights(zz, xx, a.nz, a.nx, a.hw, mult, __ldg(a.hb + oo));
-        return __ldg(kp + oo) * w.wi * l1[oo];
-      };
-      const HabcW wq = habc_weights(z, x, a.nz, a.nx, a.hw, mult, __ldg(a.hb + o));
-      float lap = ch * (kq + kzq) * wq.wi * l1[o];
-      for (int j = 1; j <= R; ++j)
-        lap += a.w.c[j] * (wl(z, x - j, a.k) + wl(z, x + j, a.k) + wl(z - j, x, a.kz) + wl(z + j, x, a.kz));
-      v = 2.f * wq.wi * l1[o] + lap - wq.wi * l2[o];
-      v += oneway_t<true, true>(a, l1, l2, z, x, z, 1, 0, 0);
-      v += oneway_t<true, true>(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
-      v += oneway_t<true, true>(a, l1, l2, z, x, x, 0, 1, 2);
-      v += oneway_t<true, true>(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
-    } else {
-      // interior part: 2 wi La1 + L(k wi La1) - wi La2
-      auto kwl = [&](int zz, int xx) -> float {
-        if (zz < 0 || zz >= a.nz || xx < 0 || xx >= a.nx) return 0.f;
-        const long long oo = (long long)zz * a.pitch + xx;
-        const HabcW w = habc_weights(zz, xx, a.nz, a.nx, a.hw, mult, __ldg(a.hb + oo));
-        return __ldg(a.k + oo) * w.wi * l1[oo];
-      };
-      const HabcW wq = habc_weights(z, x, a.nz, a.nx, a.hw, mult, __ldg(a.hb + o));
-      float lap = a.w.c[0] * kq * wq.wi * l1[o];
-      for (int j = 1; j <= R; ++j)
-        lap += a.w.c[j] * (kwl(z - j, x) + kwl(z + j, x) + kwl(z, x - j) + kwl(z, x + j));
-      v = 2.f * wq.wi * l1[o] + lap - wq.wi * l2[o];
-      // one-way parts of the four sides
-      v += oneway_t<true, true>(a, l1, l2, z, x, z, 1, 0, 0);
-      v += oneway_t<true, true>(a, l1, l2, z, x, a.nz - 1 - z, -1, 0, 1);
-      v += oneway_t<true, true>(a, l1, l2, z, x, x, 0, 1, 2);
-      v += oneway_t<true, true>(a, l1, l2, z, x, a.nx - 1 - x, 0, -1, 3);
-    }
-    // residuals of the records of step j-1 (they sample U_j)
-    if (a.resid != nullptr) {
-      const int* rp = a.rec_row_ptr + (long long)b * a.nz;
-      int lo = rp[z], hi = rp[z + 1];  // receivers of the row, sorted by column
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (a.rec_x[mid] < x) lo = mid + 1; else hi = mid;
-      }
-      for (int q = lo; q < rp[z + 1] && a.rec_x[q] == x; ++q) v += a.resid[(long long)a.rec_col[q] * a.nch];
-    }
-    a.lout[fb + o] = v;
-    // gradient and reconstruction inside the undamped box
-    const bool inbox = a.ring.inside(z, x);
-    if (inbox) {
-      const float* u1 = a.ujm1 + fb;
-      float upd;  // k L(U_{j-1}) (VTI: k Lx + kz Lz; variable density: C D(U))
-      if (rho) {
-        const float u0 = u1[o];
-        const float dxp = ldz(u1, z, x + 1, a.nz, a.nx, a.pitch) - u0, dxn = u0 - ldz(u1, z, x - 1, a.nz, a.nx, a.pitch);
-        const float dzp = ldz(u1, z + 1, x, a.nz, a.nx, a.pitch) - u0, dzn = u0 - ldz(u1, z - 1, x, a.nz, a.nx, a.pitch);
-        const float bxp = __ldg(a.rho_c + pl + o), bxn = __ldg(a.rho_c + 2 * pl + o);
-        const float bzp = __ldg(a.rho_c + 3 * pl + o), bzn = __ldg(a.rho_c + 4 * pl + o);
-        const float D = bxp * dxp - bxn * dxn + bzp * dzp - bzn * dzn;
-        const float C = __ldg(a.rho_c + o);
-        const long long fs = (long long)a.nshots * a.sstride;  // one gradient field
-        float* gr = a.grad_rho + fb + o;
-        gr[0] += v * D;
-        gr[fs] += v * C * dxp;
-        gr[2 * fs] -= v * C * dxn;
-        gr[3 * fs] += v * C * dzp;
-        gr[4 * fs] -= v * C * dzn;
-        upd = C * D;
-      } else if (vti) {
-        float Lx = ch * u1[o], Lz = ch * u1[o];
-        for (int j = 1; j <= R; ++j) {
-          Lx += a.w.c[j] * (ldz(u1, z, x - j, a.nz, a.nx, a.pitch) + ldz(u1, z, x + j, a.nz, a.nx, a.pitch));
-          Lz += a.w.c[j] * (ldz(u1, z - j, x, a.nz, a.nx, a.pitch) + ldz(u1, z + j, x, a.nz, a.nx, a.pitch));
-        }
-        a.grad[fb + o] += v * Lx;  // dJ/dk
-        a.grad2[fb + o] += v * Lz;  // dJ/dkz
-        upd = kq * Lx + kzq * Lz;
-      } else {
-        float L = a.w.c[0] * u1[o];
-        for (int j = 1; j <= R; ++j)
-          L += a.w.c[j] * (ldz(u1, z - j, x, a.nz, a.nx, a.pitch) + ldz(u1, z + j, x, a.nz, a.nx, a.pitch) +
-                           ldz(u1, z, x - j, a.nz, a.nx, a.pitch) + ldz(u1, z, x + j, a.nz, a.nx, a.pitch));
-        a.grad[fb + o] += v * kq * L;  // times 2 / vp in the shot reduction (dJ/dvp)
-        upd = kq * L;
-      }
-      if (a.uout != nullptr) {
-        float ujv = a.uj[fb + o];
-        if (a.src_ptr != nullptr) {
-          for (int q = a.src_ptr[b]; q < a.src_ptr[b + 1]; ++q)
-            if (a.src_z[q] == z && a.src_x[q] == x) ujv -= a.wavelet[(long long)a.src_wrow[q] * a.nt + a.t_src];
-        }
-        a.uout[fb + o] = 2.f * u1[o] - ujv + upd;
-      }
-    } else {
-      if (rho) {
-        // the box's one-cell rim: the half-point buoyancy terms that reach
-        // into the box (their U values are the box's and the saved ring's),
-        // so that dJ/drho is complete at the box's edge cells
-        const bool xr = a.ring.inside(z, x + 1), xl = a.ring.inside(z, x - 1);
-        const bool zd = a.ring.inside(z + 1, x), zu = a.ring.inside(z - 1, x);
-        if (xr || xl || zd || zu) {
-          const float* u1 = a.ujm1 + fb;
-          const float u0 = u1[o], vC = v * __ldg(a.rho_c + o);
-          const long long fs = (long long)a.nshots * a.sstride;
-          float* gr = a.grad_rho + fb + o;
-          if (xr) gr[fs] += vC * (u1[o + 1] - u0);
-          if (xl) gr[2 * fs] -= vC * (u0 - u1[o - 1]);
-          if (zd) gr[3 * fs] += vC * (u1[o + a.pitch] - u0);
-          if (zu) gr[4 * fs] -= vC * (u0 - u1[o - a.pitch]);
-        }
-      }
-      if (a.uout != nullptr) {  // the saved ring around the box, 0 beyond it
-        const int ri = a.ring.index(z, x);
-        a.uout[fb + o] = (ri >= 0 && a.ring_in != nullptr) ? a.ring_in[(long long)b * a.ring.size + ri] : 0.f;
-      }
-    }
-  }
-}
-
-// Interior cells (at least hw + R from every strip side, inside the box;
-// plain or VTI equation, not variable density): the transpose
-// 2 La1 + L(k La1) - La2, the gradient term and the reconstruction, with
-// k La1 and U_{j-1} of an 8 x 128 tile plus its halo staged once in shared
-// memory.  Block (32, 8): warp w owns row z0 + w, lane l columns x0 + 4l.
-constexpr int HT_Z = 8, HT_X = 128, HT_H = 4;  // rows, columns, column halo (>= R)
-template <int R, bool VTI>
-__global__ void __launch_bounds__(256) habc_bwd_interior_kernel(const HabcBwdArgs a) {
-  constexpr int ROWS = HT_Z + 2 * R, W = HT_X + 2 * HT_H;
-  __shared__ __align__(16) float s_kl[ROWS][W];              // k La1 (VTI: kx La1)
-  __shared__ __align__(16) float s_kzl[VTI ? ROWS : 1][W];   // VTI: kz La1
-  __shared__ __align__(16) float s_u[ROWS][W];
-  const int b = blockIdx.z;
-  const int z0 = a.tz0 + blockIdx.y * HT_Z, x0 = a.tx0 + blockIdx.x * HT_X;
-  const long long fb = (long long)b * a.sstride;
-  const float* l1 = a.la1 + fb;
-  const float* u1 = a.ujm1 + fb;
-  const int tid = threadIdx.y * 32 + threadIdx.x;
-  // stage: rows z0-R .. z0+HT_Z+R-1, columns x0-4 .. x0+131 (zeros off the grid)
-  for (int c = tid; c < ROWS * (W / 4); c += 256) {
-    const int rr = c / (W / 4), cc = c - rr * (W / 4);
-    const int z = z0 - R + rr, x = x0 - HT_H + 4 * cc;
-    float4 kl = make_float4(0.f, 0.f, 0.f, 0.f), uu = kl, kzl = kl;
-    if (z >= 0 && z < a.nz && x >= 0 && x + 4 <= a.pitch) {
-      const long long o = (long long)z * a.pitch + x;
-      const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
-      const float4 l4 = *reinterpret_cast<const float4*>(l1 + o);
-      kl = make_float4(k4.x * l4.x, k4.y * l4.y, k4.z * l4.z, k4.w * l4.w);
-      if (VTI) {
-        const float4 q4 = __ldg(reinterpret_cast<const float4*>(a.kz + o));
-        kzl = make_float4(q4.x * l4.x, q4.y * l4.y, q4.z * l4.z, q4.w * l4.w);
-      }
-      uu = *reinterpret_cast<const float4*>(u1 + o);
-    }
-    *reinterpret_cast<float4*>(&s_kl[rr][4 * cc]) = kl;
-    if (VTI) *reinterpret_cast<float4*>(&s_kzl[rr][4 * cc]) = kzl;
-    *reinterpret_cast<float4*>(&s_u[rr][4 * cc]) = uu;
-  }
-  __syncthreads();
-  const int z = z0 + threadIdx.y, x = x0 + 4 * threadIdx.x;
-  if (!in_tiled(a, z, x)) return;
-  const int rr = R + threadIdx.y, cx = HT_H + 4 * threadIdx.x;
-  const long long o = (long long)z * a.pitch + x;
-  const float4 l2 = *reinterpret_cast<const float4*>(a.la2 + fb + o);
-  const float4 l1c = *reinterpret_cast<const float4*>(l1 + o);
-  const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
-  float v[4], L[4], Lz[4];  // VTI: L = Lx(U), Lz = Lz(U)
-  const float ch = 0.5f * a.w.c[0];
-#pragma unroll
-  for (int m = 0; m < 4; ++m) {
-    if (VTI) {  // the per-cell VTI interior path, term by term
-      float lx = ch * s_kl[rr][cx + m], lz = ch * s_kzl[rr][cx + m];
-      float ux = ch * s_u[rr][cx + m], uz = ch * s_u[rr][cx + m];
-#pragma unroll
-      for (int j = 1; j <= R; ++j) {
-        lx += a.w.c[j] * (s_kl[rr][cx + m - j] + s_kl[rr][cx + m + j]);
-        lz += a.w.c[j] * (s_kzl[rr - j][cx + m] + s_kzl[rr + j][cx + m]);
-        ux += a.w.c[j] * (s_u[rr][cx + m - j] + s_u[rr][cx + m + j]);
-        uz += a.w.c[j] * (s_u[rr - j][cx + m] + s_u[rr + j][cx + m]);
-      }
-      v[m] = 2.f * comp(l1c, m) + lx + lz - comp(l2, m);
-      L[m] = ux;
-      Lz[m] = uz;
-    } else {
-      float lap = a.w.c[0] * s_kl[rr][cx + m];
-      float lu = a.w.c[0] * s_u[rr][cx + m];
-#pragma unroll
-      for (int j = 1; j <= R; ++j) {
-        lap += a.w.c[j] * (s_kl[rr - j][cx + m] + s_kl[rr + j][cx + m] + s_kl[rr][cx + m - j] + s_kl[rr][cx + m + j]);
-        lu += a.w.c[j] * (s_u[rr - j][cx + m] + s_u[rr + j][cx + m] + s_u[rr][cx + m - j] + s_u[rr][cx + m + j]);
-      }
-      v[m] = 2.f * comp(l1c, m) + lap - comp(l2, m);
-      L[m] = lu;
-      Lz[m] = 0.f;
-    }
-  }
-  // residuals of the records of step j-1 in this row
-  if (a.resid != nullptr) {
-    const int* rp = a.rec_row_ptr + (long long)b * a.nz;
-    int lo = rp[z], hi = rp[z + 1];  // receivers of the row, sorted by column
-    const int end = hi;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (a.rec_x[mid] < x) lo = mid + 1; else hi = mid;
-    }
-    for (int q = lo; q < end && a.rec_x[q] < x + 4; ++q) {
-      const int dx = a.rec_x[q] - x;
-      const float rv = a.resid[(long long)a.rec_col[q] * a.nch];
-#pragma unroll
-      for (int m = 0; m < 4; ++m)
-        if (dx == m) v[m] += rv;
-    }
-  }
-  *reinterpret_cast<float4*>(a.lout + fb + o) = make_float4(v[0], v[1], v[2], v[3]);
-  float4* gp = reinterpret_cast<float4*>(a.grad + fb + o);
-  const float4 g0 = *gp;
-  float4 kz4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (VTI) {  // dJ/dkx += La Lx(U), dJ/dkz += La Lz(U)
-    *gp = make_float4(g0.x + v[0] * L[0], g0.y + v[1] * L[1], g0.z + v[2] * L[2], g0.w + v[3] * L[3]);
-    float4* gq = reinterpret_cast<float4*>(a.grad2 + fb + o);
-    const float4 h0 = *gq;
-    *gq = make_float4(h0.x + v[0] * Lz[0], h0.y + v[1] * Lz[1], h0.z + v[2] * Lz[2], h0.w + v[3] * Lz[3]);
-    kz4 = __ldg(reinterpret_cast<const float4*>(a.kz + o));
-  } else {
-    *gp = make_float4(g0.x + v[0] * k4.x * L[0], g0.y + v[1] * k4.y * L[1], g0.z + v[2] * k4.z * L[2],
-                      g0.w + v[3] * k4.w * L[3]);
-  }
-  if (a.uout != nullptr) {
-    const float4 uj = *reinterpret_cast<const float4*>(a.uj + fb + o);
-    float ujv[4] = {uj.x, uj.y, uj.z, uj.w};
-    if (a.src_ptr != nullptr) {
-      for (int q = a.src_ptr[b]; q < a.src_ptr[b + 1]; ++q) {
-        const int dx = a.src_x[q] - x;
-        if (a.src_z[q] == z && dx >= 0 && dx < 4) {
-          const float wv = a.wavelet[(long long)a.src_wrow[q] * a.nt + a.t_src];
-#pragma unroll
-          for (int m = 0; m < 4; ++m)
-            if (dx == m) ujv[m] -= wv;
-        }
-      }
-    }
-    float uo[4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m)
-      uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + (VTI ? comp(k4, m) * L[m] + comp(kz4, m) * Lz[m] : comp(k4, m) * L[m]);
-    *reinterpret_cast<float4*>(a.uout + fb + o) = make_float4(uo[0], uo[1], uo[2], uo[3]);
-  }
-}
+// Tiles of the reverse step: rows, columns, column halo (>= R).
+constexpr int HT_Z = 8, HT_X = 128, HT_H = 4;
 
 
 // ------------------------------------------------ single-step VJP ---
@@ -724,21 +373,25 @@ __global__ void __launch_bounds__(256) habc_step_vjp_kernel(const HabcVjpArgs a)
 
 
 // --------------------------------------------------- all-cell tiles ---
-// The plain / VTI / Born reverse step in one launch, tile 8 x 128 with block
-// (32, 8) (lane: four columns).  La_j = 2 wi La1 + L(k wi La1) - wi La2 (VTI:
-// x neighbours by kx, z neighbours by kz) from shared-memory tiles of
-// k wi La1 and U_{j-1}; tiles within reach of a strip also stage La1 and La2
+// The reverse step of every HABC equation, tile 8 x 128 with block (32, 8)
+// (lane: four columns).  EQ 0 (plain, Born): La_j = 2 wi La1 + L(k wi La1)
+// - wi La2; EQ 1 (VTI): x neighbours by kx, z neighbours by kz; EQ 2
+// (variable density, R = 1): the transpose of C D, i.e. each neighbour's
+// C wi La1 times the buoyancy of the half point between, from shared-memory
+// tiles of (k or C) wi La1 and U_{j-1}; tiles within reach of a strip also stage La1 and La2
 // (two-row halo) and add the one-way transposes of the four sides, with each
 // cell's interior and side shares read from the five planes that
 // habc_shares_kernel fills once per reverse loop; then the receiver
 // residuals, the gradient term and the reconstruction inside the box, the
 // saved ring (or 0) outside it.
-template <int R, bool VTI, bool NEAR>
+template <int R, int EQ, bool NEAR>
 __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a) {
+  constexpr bool VTI = EQ == 1, RHO = EQ == 2;
+  static_assert(!RHO || R == 1, "variable density is second order");
   // row halo: the stencil's R, and 2 for the one-way lines (q - d, q - 2d)
   constexpr int HR = R < 2 ? 2 : R;
   constexpr int ROWS = HT_Z + 2 * HR, W = HT_X + 2 * HT_H;
-  __shared__ __align__(16) float s_kl[ROWS][W];             // k wi La1 (VTI: kx wi La1)
+  __shared__ __align__(16) float s_kl[ROWS][W];             // k wi La1 (VTI: kx wi La1; density: C wi La1)
   __shared__ __align__(16) float s_kzl[VTI ? ROWS : 1][W];  // VTI: kz wi La1
   __shared__ __align__(16) float s_u[ROWS][W];
   __shared__ __align__(16) float s_l1[NEAR ? ROWS : 1][W];  // La1 and La2 (tiles near a strip only)
@@ -752,6 +405,7 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
   const int hw = a.hw;
   const bool mult = a.multiple != 0;
   const long long pl = (long long)a.nz * a.pitch;
+  const float* __restrict__ kp = RHO ? a.rho_c : a.k;  // the plane that weights La1
   // does any cell of the tile or its halo have an interior share below 1, or
   // lie within reach of a one-way line (depth <= hw)?
   const bool near = hw > 0 && ((!mult && z0 - HR <= hw) || z0 + HT_Z + HR >= a.nz - 1 - hw ||
@@ -773,7 +427,7 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
     float r1[4] = {0.f, 0.f, 0.f, 0.f}, r2[4] = {0.f, 0.f, 0.f, 0.f};
     if (z >= 0 && z < a.nz && x >= 0 && x < a.nx) {
       const long long o = (long long)z * a.pitch + x;
-      const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
+      const float4 k4 = __ldg(reinterpret_cast<const float4*>(kp + o));
       const float4 l4 = *reinterpret_cast<const float4*>(l1 + o);
       const float4 q4 = VTI ? __ldg(reinterpret_cast<const float4*>(a.kz + o)) : k4;
       const float4 v4 = *reinterpret_cast<const float4*>(u1 + o);
@@ -805,8 +459,24 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
   const long long o = (long long)z * a.pitch + x;
   const float4 l2v = *reinterpret_cast<const float4*>(a.la2 + fb + o);
   const float4 l1c = *reinterpret_cast<const float4*>(l1 + o);
-  const float4 k4 = __ldg(reinterpret_cast<const float4*>(a.k + o));
+  const float4 k4 = __ldg(reinterpret_cast<const float4*>(kp + o));
   const float4 kz4 = VTI ? __ldg(reinterpret_cast<const float4*>(a.kz + o)) : k4;
+  // variable density: the four half-point buoyancies of the cells (bx+, bx-,
+  // bz+, bz-), bz+ of the row above, bz- of the row below, bx+ of the
+  // column left of the group and bx- of the column right of it
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 bxp = z4, bxn = z4, bzp = z4, bzn = z4, bzpU = z4, bznD = z4;
+  float bxpL = 0.f, bxnR = 0.f;
+  if constexpr (RHO) {
+    bxp = __ldg(reinterpret_cast<const float4*>(a.rho_c + pl + o));
+    bxn = __ldg(reinterpret_cast<const float4*>(a.rho_c + 2 * pl + o));
+    bzp = __ldg(reinterpret_cast<const float4*>(a.rho_c + 3 * pl + o));
+    bzn = __ldg(reinterpret_cast<const float4*>(a.rho_c + 4 * pl + o));
+    if (z > 0) bzpU = __ldg(reinterpret_cast<const float4*>(a.rho_c + 3 * pl + o - a.pitch));
+    if (z + 1 < a.nz) bznD = __ldg(reinterpret_cast<const float4*>(a.rho_c + 4 * pl + o + a.pitch));
+    if (x > 0) bxpL = __ldg(a.rho_c + pl + o - 1);
+    if (x + 4 < a.nx) bxnR = __ldg(a.rho_c + 2 * pl + o + 4);
+  }
   // one-way transposes of side `sd` at cell (z, xm) of local column cxm:
   // strip cells p = q, q - d, q - 2d (staged La1 / La2) and the wrap of the
   // line's depth hw-1 cell into its edge cell (global)
@@ -882,7 +552,19 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
     const float wq = (xm < a.nx) ? wi_at(z, xm) : 0.f;
     const float ow = NEAR ? comp(ow4, m) : 0.f;
     float lap, lu, luz = 0.f;
-    if (VTI) {
+    if (RHO) {
+      const float bl = m == 0 ? bxpL : comp(bxp, m - 1);
+      const float br = m == 3 ? bxnR : comp(bxn, m + 1);
+      lap = -(comp(bxp, m) + comp(bxn, m) + comp(bzp, m) + comp(bzn, m)) * s_kl[rr][cx + m] +
+            bl * s_kl[rr][cx + m - 1] + br * s_kl[rr][cx + m + 1] + comp(bzpU, m) * s_kl[rr - 1][cx + m] +
+            comp(bznD, m) * s_kl[rr + 1][cx + m];
+      // D(U_{j-1}) of the cell's own half points
+      const float u0 = s_u[rr][cx + m];
+      const float dxp = s_u[rr][cx + m + 1] - u0, dxn = u0 - s_u[rr][cx + m - 1];
+      const float dzp = s_u[rr + 1][cx + m] - u0, dzn = u0 - s_u[rr - 1][cx + m];
+      lu = comp(bxp, m) * dxp - comp(bxn, m) * dxn + comp(bzp, m) * dzp - comp(bzn, m) * dzn;
+      luz = 0.f;
+    } else if (VTI) {
       float lx = ch * s_kl[rr][cx + m], lz = ch * s_kzl[rr][cx + m];
       float ux = ch * s_u[rr][cx + m], uz = ch * s_u[rr][cx + m];
 #pragma unroll
@@ -945,11 +627,32 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
       }
     }
   }
+  // variable density: the five gradient terms of cell m (dJ/dC and the
+  // four buoyancies) from La_j and the differences of U_{j-1}
+  const long long fs = (long long)a.nshots * a.sstride;  // one density gradient field
+  auto rho_terms = [&](int m, float t[5]) {
+    const float u0 = s_u[rr][cx + m], vC = v[m] * comp(k4, m);
+    t[0] = v[m] * L[m];
+    t[1] = vC * (s_u[rr][cx + m + 1] - u0);
+    t[2] = -vC * (u0 - s_u[rr][cx + m - 1]);
+    t[3] = vC * (s_u[rr + 1][cx + m] - u0);
+    t[4] = -vC * (u0 - s_u[rr - 1][cx + m]);
+  };
   if (row_in && x >= a.ring.ix0 && x + 3 < a.ring.ix1) {
     // all four columns inside the box: vector gradient update and reconstruction
-    float4* gp = reinterpret_cast<float4*>(a.grad + fb + o);
+    float4* gp = reinterpret_cast<float4*>((RHO ? a.grad_rho : a.grad) + fb + o);
     const float4 g0 = *gp;
-    if (VTI) {
+    if constexpr (RHO) {
+      float t[4][5];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) rho_terms(m, t[m]);
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        float4* gq = reinterpret_cast<float4*>(a.grad_rho + q * fs + fb + o);
+        const float4 h0 = q == 0 ? g0 : *gq;
+        *gq = make_float4(h0.x + t[0][q], h0.y + t[1][q], h0.z + t[2][q], h0.w + t[3][q]);
+      }
+    } else if (VTI) {
       *gp = make_float4(g0.x + v[0] * L[0], g0.y + v[1] * L[1], g0.z + v[2] * L[2], g0.w + v[3] * L[3]);
       float4* gq = reinterpret_cast<float4*>(a.grad2 + fb + o);
       const float4 h0 = *gq;
@@ -973,7 +676,13 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
     const long long om = o + m;
     if (row_in && xm >= a.ring.ix0 && xm < a.ring.ix1) {
       const float kk = comp(k4, m);
-      if (VTI) {
+      if (RHO) {
+        float t[5];
+        rho_terms(m, t);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) a.grad_rho[q * fs + fb + om] += t[q];
+        uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + kk * L[m];
+      } else if (VTI) {
         a.grad[fb + om] += v[m] * L[m];
         a.grad2[fb + om] += v[m] * Lz[m];
         uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + kk * L[m] + comp(kz4, m) * Lz[m];
@@ -981,9 +690,26 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
         a.grad[fb + om] += v[m] * kk * L[m];
         uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + kk * L[m];
       }
-    } else if (a.uout != nullptr) {
-      const int ri = a.ring.index(z, xm);
-      uo[m] = (ri >= 0 && a.ring_in != nullptr) ? a.ring_in[(long long)b * a.ring.size + ri] : 0.f;
+    } else {
+      if constexpr (RHO) {
+        // the box's one-cell rim: the half-point buoyancy terms that reach
+        // into the box (their U values are the box's and the saved ring's),
+        // so that dJ/drho is complete at the box's edge cells
+        const bool xr = a.ring.inside(z, xm + 1), xl = a.ring.inside(z, xm - 1);
+        const bool zd = a.ring.inside(z + 1, xm), zu = a.ring.inside(z - 1, xm);
+        if (xr || xl || zd || zu) {
+          float t[5];
+          rho_terms(m, t);
+          if (xr) a.grad_rho[fs + fb + om] += t[1];
+          if (xl) a.grad_rho[2 * fs + fb + om] += t[2];
+          if (zd) a.grad_rho[3 * fs + fb + om] += t[3];
+          if (zu) a.grad_rho[4 * fs + fb + om] += t[4];
+        }
+      }
+      if (a.uout != nullptr) {
+        const int ri = a.ring.index(z, xm);
+        uo[m] = (ri >= 0 && a.ring_in != nullptr) ? a.ring_in[(long long)b * a.ring.size + ri] : 0.f;
+      }
     }
   }
   if (a.uout != nullptr) *reinterpret_cast<float4*>(a.uout + fb + o) = make_float4(uo[0], uo[1], uo[2], uo[3]);
@@ -1061,73 +787,26 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
   a.rec_col = q.rec_col;
   a.nch = q.nch;
   a.resid = resid;
-  const int R = a.R, far = a.hw + R;
-  const bool vti = kz != nullptr;
-  if (rho_c == nullptr && R <= HT_H) {
-    // plain / VTI / Born: every cell in tiles
-    a.tz0 = a.tz1 = a.tx0 = a.tx1 = 0;
-    const dim3 grid((unsigned)((g.nx + HT_X - 1) / HT_X), (unsigned)((g.nz + HT_Z - 1) / HT_Z), (unsigned)g.nshots);
-    switch (R * 2 + (vti ? 1 : 0)) {
-#define SGB_TILE2(RR, V)                                                    \
-  habc_bwd_tile_kernel<RR, V, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); \
-  if (a.hw > 0) habc_bwd_tile_kernel<RR, V, true><<<grid, dim3(32, HT_Z), 0, s>>>(a);
-      case 2: SGB_TILE2(1, false) break;
-      case 3: SGB_TILE2(1, true) break;
-      case 4: SGB_TILE2(2, false) break;
-      case 5: SGB_TILE2(2, true) break;
-      case 6: SGB_TILE2(3, false) break;
-      case 7: SGB_TILE2(3, true) break;
-      case 8: SGB_TILE2(4, false) break;
-      case 9: SGB_TILE2(4, true) break;
-#undef SGB_TILE2
-      default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
-  }
-  // variable density: the tiled interior kernel does not apply (rho_c set),
-  // so the per-cell kernel takes every cell
-  a.tz0 = a.multiple ? R : far;
-  a.tz1 = g.nz - far;
-  a.tx0 = (far + 3) / 4 * 4;
-  a.tx1 = (g.nx - far) / 4 * 4;
-  const bool tiled = rho_c == nullptr && R <= HT_H && a.tz1 > a.tz0 && a.tx1 > a.tx0 && a.tz0 >= R &&
-                     a.tz1 + R <= g.nz;
-  if (!tiled) a.tz0 = a.tz1 = a.tx0 = a.tx1 = 0;
-  if (tiled) {
-    // the box must cover the region (the gradient and the reconstruction
-    // are written there unconditionally)
-    if (a.tz0 < ring.iz0 || a.tz1 > ring.iz1 || a.tx0 < ring.ix0 || a.tx1 > ring.ix1) {
-      a.tz0 = a.tz1 = a.tx0 = a.tx1 = 0;
-    } else {
-      const dim3 grid((unsigned)((a.tx1 - a.tx0 + HT_X - 1) / HT_X), (unsigned)((a.tz1 - a.tz0 + HT_Z - 1) / HT_Z),
-                      (unsigned)g.nshots);
-      switch (R * 2 + (vti ? 1 : 0)) {
-        case 2: habc_bwd_interior_kernel<1, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-        case 3: habc_bwd_interior_kernel<1, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-        case 4: habc_bwd_interior_kernel<2, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-        case 5: habc_bwd_interior_kernel<2, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-        case 6: habc_bwd_interior_kernel<3, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-        case 7: habc_bwd_interior_kernel<3, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-        case 8: habc_bwd_interior_kernel<4, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-        case 9: habc_bwd_interior_kernel<4, true><<<grid, dim3(32, HT_Z), 0, s>>>(a); break;
-      }
-    }
-  }
-  const long long total = FrameCells(a).plane * g.nshots;
-  long long blocks = (total + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  const int R = a.R;
+  if (R > HT_H) return cudaErrorInvalidValue;
   const int eq = rho_c != nullptr ? 2 : (kz != nullptr ? 1 : 0);
-  if (eq == 2 && a.R != 1) return cudaErrorInvalidValue;  // variable density: 2nd order only
-  switch (a.R * 3 + eq) {
-    case 3: habc_bwd_kernel<1, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 4: habc_bwd_kernel<1, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 5: habc_bwd_kernel<1, 2><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 6: habc_bwd_kernel<2, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 7: habc_bwd_kernel<2, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 9: habc_bwd_kernel<3, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 10: habc_bwd_kernel<3, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 12: habc_bwd_kernel<4, 0><<<(unsigned)blocks, 256, 0, s>>>(a); break;
-    case 13: habc_bwd_kernel<4, 1><<<(unsigned)blocks, 256, 0, s>>>(a); break;
+  if (eq == 2 && R != 1) return cudaErrorInvalidValue;  // variable density: 2nd order only
+  const dim3 grid((unsigned)((g.nx + HT_X - 1) / HT_X), (unsigned)((g.nz + HT_Z - 1) / HT_Z), (unsigned)g.nshots);
+  // one launch for the tiles out of reach of the strips, one for the rest
+  switch (R * 3 + eq) {
+#define SGB_TILE2(RR, EQ)                                                    \
+  habc_bwd_tile_kernel<RR, EQ, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); \
+  if (a.hw > 0) habc_bwd_tile_kernel<RR, EQ, true><<<grid, dim3(32, HT_Z), 0, s>>>(a);
+    case 3: SGB_TILE2(1, 0) break;
+    case 4: SGB_TILE2(1, 1) break;
+    case 5: SGB_TILE2(1, 2) break;
+    case 6: SGB_TILE2(2, 0) break;
+    case 7: SGB_TILE2(2, 1) break;
+    case 9: SGB_TILE2(3, 0) break;
+    case 10: SGB_TILE2(3, 1) break;
+    case 12: SGB_TILE2(4, 0) break;
+    case 13: SGB_TILE2(4, 1) break;
+#undef SGB_TILE2
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
