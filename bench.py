@@ -620,13 +620,14 @@ def bench_habc(args):
                        "grid": [nz, nx], "shots": shots, "nt": nt, "order": order, "ckpt_every": ck,
                        "l2": "inputs larger than L2 (141 MB per field)"},
             "shots_per_s": shots / (ms * 1e-3), "phases_ms": {"forward": fwd_ms, "adjoint": rev_ms},
-            "roofline": {"kernel": "habc_bwd_interior_kernel + habc_bwd_kernel", "bound": "hbm", "achieved": rev_gbs,
+            "roofline": {"kernel": "habc_bwd_tile_kernel (far + near tiles)", "bound": "hbm", "achieved": rev_gbs,
                          "peak": peak, "peak_kind": kind, "unit": "GB/s", "frac": rev_gbs / peak, "traffic": None,
                          "bytes_per_launch": rev_bytes, "launch_ms": rev_ms / (nt - 1)},
             "roofline_forward": {"kernel": "acoustic_fwd_tile_kernel<HABC>", "achieved": fwd_gbs,
                                  "frac": fwd_gbs / peak, "unit": "GB/s", "launch_ms": fwd_ms / nt},
-            # per step: NT forward, 2 (NT-1) reverse, coefficients, misfit, reduction
-            "gpu_launches": args.steps * (nt + 2 * (nt - 1) + 3), "clocks": clocks.summary()}
+            # per step: NT forward, 2 (NT-1) reverse (far and near tiles), share planes, coefficients,
+            # misfit, reduction
+            "gpu_launches": args.steps * (nt + 2 * (nt - 1) + 4), "clocks": clocks.summary()}
     print(json.dumps(line))
     return 0
 
@@ -853,14 +854,15 @@ def bench_born(args):
                        "grid": [nz, nx], "shots": shots, "nt": nt, "ckpt_every": ck,
                        "l2": "inputs larger than L2 (70 MB per field, 6 fields)"},
             "shots_per_s": shots / (ms * 1e-3), "phases_ms": {"forward": fwd_ms, "adjoint": rev_ms},
-            "roofline": {"kernel": "habc_bwd_kernel", "bound": "hbm", "achieved": rev_gbs, "peak": peak,
+            "roofline": {"kernel": "habc_bwd_tile_kernel (far + near tiles)", "bound": "hbm", "achieved": rev_gbs, "peak": peak,
                          "peak_kind": kind, "unit": "GB/s", "frac": rev_gbs / peak, "traffic": None,
                          "bytes_per_launch": rev_bytes, "launch_ms": rev_ms / (nt - 1)},
-            "roofline_forward": {"kernel": "acoustic_fwd_kernel<HABC> x2 (background, scattered)",
+            "roofline_forward": {"kernel": "acoustic_fwd_tile_kernel<HABC> x2 (background, scattered)",
                                  "achieved": fwd_gbs, "frac": fwd_gbs / peak, "unit": "GB/s",
                                  "launch_ms": fwd_ms / nt},
-            # per step: 2 NT forward + NT ring gathers, NT-1 reverse, coefficients, misfit, reduction
-            "gpu_launches": args.steps * (3 * nt + (nt - 1) + 3), "clocks": clocks.summary()}
+            # per step: 2 NT forward (background, scattered), 2 (NT-1) reverse (far and near tiles), share
+            # planes, coefficients, misfit, reduction
+            "gpu_launches": args.steps * (2 * nt + 2 * (nt - 1) + 4), "clocks": clocks.summary()}
     print(json.dumps(line))
     return 0
 
@@ -949,13 +951,14 @@ def bench_vti(args):
                        "grid": [nz, nx], "shots": shots, "nt": nt, "ckpt_every": ck,
                        "l2": "inputs larger than L2 (70 MB per field)"},
             "shots_per_s": shots / (ms_ * 1e-3), "phases_ms": {"forward": fwd_ms, "adjoint": rev_ms},
-            "roofline": {"kernel": "habc_bwd_kernel (VTI)", "bound": "hbm", "achieved": rev_gbs, "peak": peak,
+            "roofline": {"kernel": "habc_bwd_tile_kernel (VTI, far + near tiles)", "bound": "hbm", "achieved": rev_gbs, "peak": peak,
                          "peak_kind": kind, "unit": "GB/s", "frac": rev_gbs / peak, "traffic": None,
                          "bytes_per_launch": rev_bytes, "launch_ms": rev_ms / (nt - 1)},
-            "roofline_forward": {"kernel": "acoustic_fwd_kernel<HABC> (VTI)", "achieved": fwd_gbs,
+            "roofline_forward": {"kernel": "acoustic_fwd_tile_kernel<HABC> (VTI)", "achieved": fwd_gbs,
                                  "frac": fwd_gbs / peak, "unit": "GB/s", "launch_ms": fwd_ms / nt},
-            # per step: NT forward + NT ring gathers, NT-1 reverse, coefficients, misfit, 2 reductions
-            "gpu_launches": args.steps * (2 * nt + (nt - 1) + 3), "clocks": clocks.summary()}
+            # per step: NT forward, 2 (NT-1) reverse (far and near tiles), share planes, coefficients,
+            # misfit, 2 reductions
+            "gpu_launches": args.steps * (nt + 2 * (nt - 1) + 5), "clocks": clocks.summary()}
     print(json.dumps(line))
     return 0
 
@@ -1041,13 +1044,14 @@ def bench_rho(args):
                        "grid": [nz, nx], "shots": shots, "nt": nt, "ckpt_every": ck,
                        "l2": "inputs larger than L2 (70 MB per field)"},
             "shots_per_s": shots / (ms_ * 1e-3), "phases_ms": {"forward": fwd_ms, "adjoint": rev_ms},
-            "roofline": {"kernel": "habc_bwd_kernel (variable density)", "bound": "hbm", "achieved": rev_gbs,
+            "roofline": {"kernel": "habc_bwd_tile_kernel (variable density, far + near tiles)", "bound": "hbm", "achieved": rev_gbs,
                          "peak": peak, "peak_kind": kind, "unit": "GB/s", "frac": rev_gbs / peak, "traffic": None,
                          "bytes_per_launch": rev_bytes, "launch_ms": rev_ms / (nt - 1)},
-            "roofline_forward": {"kernel": "acoustic_fwd_kernel<HABC> (variable density)", "achieved": fwd_gbs,
+            "roofline_forward": {"kernel": "acoustic_fwd_tile_kernel<HABC> (variable density)", "achieved": fwd_gbs,
                                  "frac": fwd_gbs / peak, "unit": "GB/s", "launch_ms": fwd_ms / nt},
-            # per step: NT forward + NT ring gathers, NT-1 reverse, coefficients, misfit, 5 reductions
-            "gpu_launches": args.steps * (2 * nt + (nt - 1) + 7), "clocks": clocks.summary()}
+            # per step: NT forward, 2 (NT-1) reverse (far and near tiles), share planes, coefficients,
+            # misfit, 5 reductions
+            "gpu_launches": args.steps * (nt + 2 * (nt - 1) + 8), "clocks": clocks.summary()}
     print(json.dumps(line))
     return 0
 

@@ -371,25 +371,6 @@ __global__ void acoustic_grad_reduce_kernel(int nz, int nx, int pitch, int nshot
   }
 }
 
-// Copies the boundary ring between a field [nshots][nz][pitch] and its
-// slots [nshots][ring.size]: a gather (field -> slots) after each forward
-// step, a scatter (slots -> field) after each reverse reconstruction.
-__global__ void ring_copy_kernel(int nshots, Ring ring, int pitch, long long sstride, float* __restrict__ field,
-                                 float* __restrict__ slots, int scatter) {
-  const long long n = (long long)nshots * ring.size;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int b = (int)(i / ring.size);
-    int z, x;
-    ring.cell((int)(i - (long long)b * ring.size), z, x);
-    float* f = field + b * sstride + (long long)z * pitch + x;
-    if (scatter)
-      *f = slots[i];
-    else
-      slots[i] = *f;
-  }
-}
-
 // ------------------------------------------------------------- launch ---
 
 template <int R, int TZ, bool HABC>
@@ -483,16 +464,6 @@ cudaError_t launch_acoustic_coef(const sgb_grid& gr, const float* vp, const floa
   const long long n = (long long)gr.nz * gr.pitch;
   const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
   acoustic_coef_kernel<<<blocks, 256, 0, s>>>(gr.nz, gr.nx, gr.pitch, vp, damp, boundary, gr.dt, gr.h, g, k);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_ring_copy(const sgb_grid& gr, const Ring& ring, float* field, float* slots, bool scatter,
-                             cudaStream_t s) {
-  const long long n = (long long)gr.nshots * ring.size;
-  if (n == 0) return cudaSuccess;
-  const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
-  ring_copy_kernel<<<blocks, 256, 0, s>>>(gr.nshots, ring, gr.pitch, (long long)gr.nz * gr.pitch, field, slots,
-                                          scatter ? 1 : 0);
   return cudaGetLastError();
 }
 

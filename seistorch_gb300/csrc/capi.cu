@@ -56,8 +56,6 @@ cudaError_t launch_acoustic_fwd(int R, bool habc, int tz, const AcStepArgs& a, c
 cudaError_t launch_acoustic_vjp(int R, const AcVjpArgs& a, cudaStream_t s);
 cudaError_t launch_acoustic_coef(const sgb_grid& gr, const float* vp, const float* damp, int boundary,
                                  float* g, float* k, cudaStream_t s);
-cudaError_t launch_ring_copy(const sgb_grid& gr, const Ring& ring, float* field, float* slots, bool scatter,
-                             cudaStream_t s);
 int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model, const sgb_acquisition* acq,
                            const sgb_bs_store* bs, float* const ubuf[3], int32_t ucur, int32_t uprev,
                            float* const lbuf[3], float* grad_shot, float* grad_vp, bool born, cudaStream_t s,
@@ -805,7 +803,7 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
   const int K = bs->ckpt_every;
   const int nslots = K > 0 ? nt / K : 0;
   if (model->boundary == 1) {
-    // HABC: per-cell gather kernel (habc_bwd.cu), same buffer rotation
+    // HABC: tiled reverse-step kernel (habc_bwd.cu), same buffer rotation
     if ((acq->nsrc > 0 && acq->src_ptr == nullptr)) return SGB_ERR_ARG;
     int uj = ucur, ujm1 = uprev, ufree = 3 - ucur - uprev;
     int l1 = 0, l2 = 1, lfree = 2;
