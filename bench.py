@@ -203,7 +203,7 @@ def main():
                          "(L2-resident); habc_gradient: the headline grid and model with the hybrid absorbing "
                          "boundary (acoustic_habc), --order 2 (default) or 4")
     ap.add_argument("--order", type=int, default=0, help="habc_gradient: spatial order (2 or 4)")
-    ap.add_argument("--pairs", type=int, default=2000, help="learned_fwi: training pairs")
+    ap.add_argument("--pairs", type=int, default=800, help="learned_fwi: training pairs")
     ap.add_argument("--epochs", type=int, default=12, help="learned_fwi: training epochs")
     ap.add_argument("--iters", type=int, default=20, help="learned_fwi: FWI iterations")
     ap.add_argument("--save-net", default="", help="learned_fwi: write the trained parameters (.npz)")
@@ -347,8 +347,10 @@ def main():
     return 0
 
 
-def e2e_through_api(args, dev, vp_init, obs_host, wav, sources, receivers, world):
-    """Same metric through build_model / WaveRNN / autograd with host buffers."""
+def e2e_through_api(args, dev, vp_init, obs_host, wav, sources, receivers, world, equation="acoustic",
+                    boundary="pml", order=ORDER, nt=NT):
+    """Same metric through build_model / WaveRNN / autograd with host buffers
+    (`equation` acoustic with a PML, or acoustic_habc with the HABC)."""
     import torch
     import torch.distributed as dist
 
@@ -356,17 +358,17 @@ def e2e_through_api(args, dev, vp_init, obs_host, wav, sources, receivers, world
     from seistorch_gb300.distributed import allreduce_gradient
     from seistorch_gb300.postprocess import L2
 
-    cfg = {"equation": "acoustic", "dtype": "float32",
-           "geom": {"dt": DT, "h": H, "nt": NT, "boundary": {"type": "pml", "width": WIDTH},
+    cfg = {"equation": equation, "dtype": "float32",
+           "geom": {"dt": DT, "h": H, "nt": nt, "boundary": {"type": boundary, "width": WIDTH},
                     "multiple": False, "boundary_saving": True, "source_type": ["h1"], "receiver_type": ["h1"],
-                    "spatial_order": ORDER, "invlist": {"vp": True}}}
+                    "spatial_order": order, "invlist": {"vp": True}}}
     vp_int = vp_init[WIDTH:-WIDTH, WIDTH:-WIDTH]
     _, model = build_model(cfg, device=dev, mode="inversion", models={"vp": vp_int})
     srcs = [[x - WIDTH, z - WIDTH] for [(z, x)] in sources]
     recs = [[[x - WIDTH for x in xs], [z - WIDTH for z in zs]] for zs, xs in receivers]
     model.reset_geom(list(range(len(srcs))), srcs, recs, cfg)
     vp_host = torch.tensor(vp_init, dtype=torch.float32).pin_memory()
-    obs_pinned = obs_host.reshape(NT, len(sources), NREC).permute(1, 0, 2).contiguous().pin_memory()
+    obs_pinned = obs_host.reshape(nt, len(sources), NREC).permute(1, 0, 2).contiguous().pin_memory()
     wav_host = torch.tensor(wav)[None].pin_memory()
     grad_host = torch.empty_like(vp_host).pin_memory()
     loss_host = torch.empty(1).pin_memory()
@@ -397,7 +399,7 @@ def e2e_through_api(args, dev, vp_init, obs_host, wav, sources, receivers, world
     wall = (time.perf_counter() - t0) / args.steps
     nz, nx = vp_init.shape
     h2d = vp_host.numel() * 4 + obs_pinned.numel() * 4 + wav_host.numel() * 4
-    return {"value": len(sources) * nz * nx * NT * world / wall / 1e9, "unit": "Gpts/s",
+    return {"value": len(sources) * nz * nx * nt * world / wall / 1e9, "unit": "Gpts/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(grad_host.numel() * 4 + 4),
             "ms_per_step": wall * 1e3, "api": "build_model -> WaveRNN.forward -> loss.backward"}
 
@@ -628,6 +630,9 @@ def bench_habc(args):
             # per step: NT forward, 2 (NT-1) reverse (far and near tiles), share planes, coefficients,
             # misfit, reduction
             "gpu_launches": args.steps * (nt + 2 * (nt - 1) + 4), "clocks": clocks.summary()}
+    if not args.no_e2e:
+        line["e2e"] = e2e_through_api(args, dev, vp_init, obs.cpu(), wav, sources, receivers, 1,
+                                      equation="acoustic_habc", boundary="habc", order=order, nt=nt)
     print(json.dumps(line))
     return 0
 

@@ -146,7 +146,10 @@ struct FwdMany {
 
 // per group: map_u = U_n [nshots][nz][nx], box {W, TZ+2R, 1};
 //            map_um = U_{n-1}, box {128, TZ, 1} (used when PT)
-template <int R, int TZ, int NWP, int S, bool PT, int SB, class P, bool HB = false>
+// HB: 0 PML; HABC with 1 the plain update (plus the Born / viscoacoustic
+// additive field), 2 VTI (k Lx + kz Lz), 3 variable density (C D(u)) -- one
+// instantiation per equation, so each carries only its own branch
+template <int R, int TZ, int NWP, int S, bool PT, int SB, class P, int HB = 0>
 __device__ __forceinline__ void fwd_tiles(const P& prov) {
   static_assert(SB == 1 || PT, "several shots per tile need the previous field in the stage");
   using Lay = FwdTileLayout<R, TZ, S, PT, SB>;
@@ -244,7 +247,7 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
         const float* srow = su + (lr + R) * UW;
         const float4 c = win[R];
         float4 y;
-        if (HB && R == 1 && a.rho_c != nullptr) {  // variable density: g (u - u-) + u- + C D(u)
+        if constexpr (HB == 3 && R == 1) {  // variable density: g (u - u-) + u- + C D(u)
           const long long po = (long long)z * a.pitch + x, pl = (long long)a.nz * a.pitch;
           const bool in = xin && z < a.nz;
           const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -259,7 +262,7 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
                             comp(bzp, m) * (comp(win[R + 1], m) - cc) - comp(bzn, m) * (cc - comp(win[R - 1], m));
             set_comp(y, m, fmaf(comp(C4, m), D, fmaf(comp(vg[i], m), cc - comp(vm[i], m), comp(vm[i], m))));
           }
-        } else if (HB && a.kz != nullptr) {  // VTI: k Lx + kz Lz
+        } else if constexpr (HB == 2) {  // VTI: k Lx + kz Lz
           float4 Lx, Lz;
           lap_row_xz<R>(win, srow, lane, a.w, Lx, Lz);
           const float4 vz = (xin && z < a.nz) ? ldg4(a.kz + (long long)z * a.pitch + x) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -274,7 +277,7 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
           y.y = fmaf(vk[i].y, L.y, fmaf(vg[i].y, c.y - vm[i].y, vm[i].y));
           y.z = fmaf(vk[i].z, L.z, fmaf(vg[i].z, c.z - vm[i].z, vm[i].z));
           y.w = fmaf(vk[i].w, L.w, fmaf(vg[i].w, c.w - vm[i].w, vm[i].w));
-          if (HB && (a.born_out != nullptr || a.born_in != nullptr) && xin && z < a.nz) {
+          if (HB == 1 && (a.born_out != nullptr || a.born_in != nullptr) && xin && z < a.nz) {
             const long long po = (long long)z * a.pitch + x;
             if (a.born_out != nullptr) {  // m k L(u): the scattered field's source (Born)
               const float4 mm = ldg4(a.born_m + po);
@@ -288,7 +291,7 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
             }
           }
         }
-        if (HB && z < a.nz && xin && (z < a.hw || z >= a.nz - a.hw || x < a.hw || x + 3 >= a.nx - a.hw)) {
+        if (HB != 0 && z < a.nz && xin && (z < a.hw || z >= a.nz - a.hw || x < a.hw || x + 3 >= a.nx - a.hw)) {
           // the one-way blend on strip cells: four cells of one side at once,
           // else cell by cell (corners, diagonals, mixed groups; one copy of
           // its code, not unrolled)
@@ -365,8 +368,12 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
       if ((int)blockIdx.x + q * G < ntiles) mbar_wait(&bars[q % S], (q / S) & 1, nullptr);
 }
 
-template <int R, int TZ, int NWP, int S, bool PT, int SB, bool HB = false>
-__global__ void __launch_bounds__(32 * NWP) acoustic_fwd_tile_kernel(const __grid_constant__ CUtensorMap tm_u,
+// the second-order HABC instantiations with two rows per warp run 640
+// threads per SM (registers held to 102), the others 512 (128 registers,
+// no spills)
+template <int R, int TZ, int NWP, int S, bool PT, int SB, int HB = 0>
+__global__ void __launch_bounds__(32 * NWP, HB != 0 ? ((R == 1 && TZ / NWP <= 2) ? 20 : 16) / NWP : 1)
+    acoustic_fwd_tile_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                                      const __grid_constant__ CUtensorMap tm_um,
                                                                      const AcStreamArgs a) {
   fwd_tiles<R, TZ, NWP, S, PT, SB, FwdOne<SB>, HB>(FwdOne<SB>{&tm_u, &tm_um, a});
@@ -392,7 +399,7 @@ static const FwdCfg FWD_TILE_CFGS[] = {{16, 4, 3, 1}, {16, 4, 3, 1}, {8, 4, 4, 1
 // Launches the variant on batch b; with s == nullptr and prepare_only it
 // only sets the kernel's shared-memory attribute (done once per variant, and
 // before any stream capture).
-template <int R, int TZ, int NWP, int S, bool PT, int MAXG, int SB = 1, bool HB = false>
+template <int R, int TZ, int NWP, int S, bool PT, int MAXG, int SB = 1, int HB = 0>
 static cudaError_t fwd_tile_t(const AcFwdBatch<MAXG>& b, cudaStream_t s, bool prepare_only) {
   using Lay = FwdTileLayout<R, TZ, S, PT, MAXG == 1 ? SB : 1>;
   const size_t smem = Lay::BYTES + 128;  // + alignment slack
@@ -452,10 +459,20 @@ int fwd_tile_rows() { return FWD_TILE_CFGS[g_fwd_cfg].tz; }
 int fwd_tile_shots() { return FWD_TILE_CFGS[g_fwd_cfg].sb; }
 int stencil_box_width(int R) { return (R % 2 == 0) ? TX + 8 : TX + 16; }
 
-// The HABC family's forward: one variant (HT-row tiles, 4 warps, HS stages,
-// previous field by global loads, which the blend's strip neighbours share).
-constexpr int HT = 8, HS = 4;
-int habc_tile_rows() { return HT; }
+// The HABC family's forward: HT-row tiles, 4 warps, HS stages, previous
+// field through the TMA stage (the fastest of the variants timed on the
+// 64-shot 500 x 1100 second-order grid: 137 us a step against 153-166 us);
+// the second-order plain equation (also Born and the viscoacoustic additive
+// field) can take any of the HABC_FWD variants (rows per tile, warps,
+// stages, previous field via TMA).
+constexpr int HT = 8, HS = 3;
+struct HabcFwdCfg {
+  int tz, nw, s;
+  bool pt;
+};
+constexpr HabcFwdCfg HABC_FWD[6] = {{8, 4, 3, true},   {16, 4, 2, true}, {16, 4, 3, true},
+                                    {8, 4, 4, false}, {16, 4, 3, false}, {32, 8, 2, true}};
+int habc_tile_rows(int R, int hb) { return (R == 1 && hb == 1) ? HABC_FWD[g_habc_fwd_cfg].tz : HT; }
 
 cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s,
                                        bool habc) {
@@ -467,11 +484,23 @@ cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcS
   b.tile0[0] = 0;
   b.tile0[1] = a.nshots * a.ntx * a.nzc;
   if (!habc) return fwd_dispatch<1>(R, b, s, false);
+  // variable density and VTI are second order (the reference's kernels)
+  if (a.rho_c != nullptr) return R == 1 ? fwd_tile_t<1, HT, 4, HS, true, 1, 1, 3>(b, s, false) : cudaErrorInvalidValue;
+  if (a.kz != nullptr) return R == 1 ? fwd_tile_t<1, HT, 4, HS, true, 1, 1, 2>(b, s, false) : cudaErrorInvalidValue;
   switch (R) {
-    case 1: return fwd_tile_t<1, HT, 4, HS, false, 1, 1, true>(b, s, false);
-    case 2: return fwd_tile_t<2, HT, 4, HS, false, 1, 1, true>(b, s, false);
-    case 3: return fwd_tile_t<3, HT, 4, HS, false, 1, 1, true>(b, s, false);
-    case 4: return fwd_tile_t<4, HT, 4, HS, false, 1, 1, true>(b, s, false);
+    case 1:
+      switch (g_habc_fwd_cfg) {
+        case 0: return fwd_tile_t<1, 8, 4, 3, true, 1, 1, 1>(b, s, false);
+        case 1: return fwd_tile_t<1, 16, 4, 2, true, 1, 1, 1>(b, s, false);
+        case 2: return fwd_tile_t<1, 16, 4, 3, true, 1, 1, 1>(b, s, false);
+        case 3: return fwd_tile_t<1, 8, 4, 4, false, 1, 1, 1>(b, s, false);
+        case 4: return fwd_tile_t<1, 16, 4, 3, false, 1, 1, 1>(b, s, false);
+        case 5: return fwd_tile_t<1, 32, 8, 2, true, 1, 1, 1>(b, s, false);
+      }
+      return cudaErrorInvalidValue;
+    case 2: return fwd_tile_t<2, HT, 4, HS, true, 1, 1, 1>(b, s, false);
+    case 3: return fwd_tile_t<3, HT, 4, HS, true, 1, 1, 1>(b, s, false);
+    case 4: return fwd_tile_t<4, HT, 4, HS, true, 1, 1, 1>(b, s, false);
   }
   return cudaErrorInvalidValue;
 }

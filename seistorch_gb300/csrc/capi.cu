@@ -67,7 +67,7 @@ int pick_tz(int nz, int nx, int nshots, int tz_max);
 // streaming kernels in acoustic_stream.cu
 cudaError_t launch_acoustic_fwd_stream(int R, const CUtensorMap* maps, const AcStreamArgs& a, cudaStream_t s,
                                        bool habc = false);
-int habc_tile_rows();
+int habc_tile_rows(int R, int hb);
 int vacoustic_kterm(const sgb_grid& g, const float* pre, const float* u1, const float* u2, const float* post,
                     float* out, float* work, float* tw, cudaStream_t s);
 
@@ -90,7 +90,7 @@ int fwd_tile_rows();
 int fwd_tile_shots();
 int bwd_tile_rows();
 int stencil_box_width(int R);
-int set_stream_config(int fwd, int bwd, int zc);
+int set_stream_config(int fwd, int bwd, int habc);
 cudaError_t launch_habc_step_vjp(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_habc_vjp_io& io,
                                  cudaStream_t s);
 cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, const sgb_acquisition& q,
@@ -283,8 +283,8 @@ int sgb_device_status(int* out, int reset) {
   return SGB_OK;
 }
 
-int sgb_set_stream_config(int32_t fwd_cfg, int32_t bwd_cfg, int32_t zc) {
-  return set_stream_config(fwd_cfg, bwd_cfg, zc) == 0 ? SGB_OK : SGB_ERR_ARG;
+int sgb_set_stream_config(int32_t fwd_cfg, int32_t bwd_cfg, int32_t habc_cfg) {
+  return set_stream_config(fwd_cfg, bwd_cfg, habc_cfg) == 0 ? SGB_OK : SGB_ERR_ARG;
 }
 
 int sgb_ring_size(const sgb_grid* grid, int32_t iz0, int32_t iz1, int32_t ix0, int32_t ix1, int32_t ring,
@@ -495,7 +495,7 @@ int acoustic_forward_impl(const sgb_grid* grid, const sgb_acoustic_model* model,
   CUtensorMap mu[3], mum[3];
   AcStreamArgs sa;
   std::memset(&sa, 0, sizeof(sa));
-  const int tzr = habc ? habc_tile_rows() : fwd_tile_rows();
+  const int tzr = habc ? habc_tile_rows(R, a.rho_c != nullptr ? 3 : (a.kz != nullptr ? 2 : 1)) : fwd_tile_rows();
   const int tsb = habc ? 1 : fwd_tile_shots();
   const int bw = stencil_box_width(R);
   for (int i = 0; i < 3; ++i)
@@ -594,7 +594,7 @@ int sgb_born_forward(const sgb_grid* grid, const sgb_acoustic_model* model, cons
   }
   const int R = model->order / 2;
   ap.ring = ring;
-  const int tzr = habc_tile_rows();
+  const int tzr = habc_tile_rows(R, 1);
   const int bw = stencil_box_width(R);
   CUtensorMap pu[3], pum[3], su3[3], sum3[3];
   for (int i = 0; i < 3; ++i)

@@ -413,54 +413,117 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
   // two launches share the grid: the NEAR instantiation takes the tiles
   // within reach of a strip, the other the rest (with none of the strip code)
   if (near != NEAR) return;
-  auto wi_at = [&](int z, int x) -> float {
-    if (!near) return 1.f;
+  // interior shares of the four cells (z, x .. x+3), x a multiple of 4
+  auto wi4_at = [&](int z, int x) -> float4 {
+    if (!near) return make_float4(1.f, 1.f, 1.f, 1.f);
     const long long oo = (long long)z * a.pitch + x;
-    if (a.wpl != nullptr) return __ldg(a.wpl + oo);
-    const float bb = __ldg(a.hb + oo);  // b = 0: no side share, wi = 1
-    return bb == 0.f ? 1.f : habc_weights(z, x, a.nz, a.nx, hw, mult, bb).wi;
-  };
-  for (int c = tid; c < ROWS * (W / 4); c += 256) {
-    const int rr = c / (W / 4), cc = c - rr * (W / 4);
-    const int z = z0 - HR + rr, x = x0 - HT_H + 4 * cc;
-    float kl[4] = {0.f, 0.f, 0.f, 0.f}, kzl[4] = {0.f, 0.f, 0.f, 0.f}, uu[4] = {0.f, 0.f, 0.f, 0.f};
-    float r1[4] = {0.f, 0.f, 0.f, 0.f}, r2[4] = {0.f, 0.f, 0.f, 0.f};
-    if (z >= 0 && z < a.nz && x >= 0 && x < a.nx) {
-      const long long o = (long long)z * a.pitch + x;
-      const float4 k4 = __ldg(reinterpret_cast<const float4*>(kp + o));
-      const float4 l4 = *reinterpret_cast<const float4*>(l1 + o);
-      const float4 q4 = VTI ? __ldg(reinterpret_cast<const float4*>(a.kz + o)) : k4;
-      const float4 v4 = *reinterpret_cast<const float4*>(u1 + o);
-      const float4 m4 = NEAR ? *reinterpret_cast<const float4*>(a.la2 + fb + o) : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.wpl != nullptr) return __ldg(reinterpret_cast<const float4*>(a.wpl + oo));
+    float4 r;
 #pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        if (x + m < a.nx) {
-          const float w = wi_at(z, x + m);
-          kl[m] = comp(k4, m) * w * comp(l4, m);
-          if (VTI) kzl[m] = comp(q4, m) * w * comp(l4, m);
-          uu[m] = comp(v4, m);
-          r1[m] = comp(l4, m);
-          r2[m] = comp(m4, m);
-        }
+    for (int m = 0; m < 4; ++m) {
+      const float bb = x + m < a.nx ? __ldg(a.hb + oo + m) : 0.f;  // b = 0: no side share, wi = 1
+      set_comp(r, m, bb == 0.f ? 1.f : habc_weights(z, x + m, a.nz, a.nx, hw, mult, bb).wi);
+    }
+    return r;
+  };
+  // stage (k or C) wi La1, U_{j-1} and, near a strip, La1 and La2 with their
+  // halo.  Far tiles (and variable density) issue the loads of all of a
+  // thread's groups first, then the point loads of its own four cells, and
+  // only then write shared memory, so that one memory latency covers them
+  // all; near tiles, issue-bound and short of registers, stage group by group.
+  constexpr bool PRE = !NEAR || RHO;
+  constexpr int NST = ROWS * (W / 4), NIT = (NST + 255) / 256;
+  const float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f);
+  struct Grp {
+    float4 k, l, q, v, m, w;
+  };
+  auto stage_load = [&](int c, Grp& g) {
+    const int rr_ = c / (W / 4), cc = c - rr_ * (W / 4);
+    const int zs = z0 - HR + rr_, xs = x0 - HT_H + 4 * cc;
+    g.k = g.l = g.q = g.v = g.m = f0;
+    g.w = make_float4(1.f, 1.f, 1.f, 1.f);
+    if (c < NST && zs >= 0 && zs < a.nz && xs >= 0 && xs < a.nx) {
+      const long long os = (long long)zs * a.pitch + xs;
+      g.k = __ldg(reinterpret_cast<const float4*>(kp + os));
+      g.l = *reinterpret_cast<const float4*>(l1 + os);
+      if (VTI) g.q = __ldg(reinterpret_cast<const float4*>(a.kz + os));
+      g.v = *reinterpret_cast<const float4*>(u1 + os);
+      if (NEAR) g.m = *reinterpret_cast<const float4*>(a.la2 + fb + os);
+      if (NEAR) g.w = wi4_at(zs, xs);
+    }
+  };
+  auto stage_store = [&](int c, Grp& g) {
+    const int rr_ = c / (W / 4), cc = c - rr_ * (W / 4);
+    const int xs = x0 - HT_H + 4 * cc;
+    float kl[4] = {0.f, 0.f, 0.f, 0.f}, kzl[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      if (xs + m < a.nx) {  // columns beyond the grid stay 0
+        const float w = comp(g.w, m);
+        kl[m] = comp(g.k, m) * w * comp(g.l, m);
+        if (VTI) kzl[m] = comp(g.q, m) * w * comp(g.l, m);
+      } else {
+        set_comp(g.v, m, 0.f);
+        set_comp(g.l, m, 0.f);
+        set_comp(g.m, m, 0.f);
       }
     }
-    *reinterpret_cast<float4*>(&s_kl[rr][4 * cc]) = make_float4(kl[0], kl[1], kl[2], kl[3]);
-    if (VTI) *reinterpret_cast<float4*>(&s_kzl[rr][4 * cc]) = make_float4(kzl[0], kzl[1], kzl[2], kzl[3]);
-    *reinterpret_cast<float4*>(&s_u[rr][4 * cc]) = make_float4(uu[0], uu[1], uu[2], uu[3]);
+    *reinterpret_cast<float4*>(&s_kl[rr_][4 * cc]) = make_float4(kl[0], kl[1], kl[2], kl[3]);
+    if (VTI) *reinterpret_cast<float4*>(&s_kzl[rr_][4 * cc]) = make_float4(kzl[0], kzl[1], kzl[2], kzl[3]);
+    *reinterpret_cast<float4*>(&s_u[rr_][4 * cc]) = g.v;
     if constexpr (NEAR) {
-      *reinterpret_cast<float4*>(&s_l1[rr][4 * cc]) = make_float4(r1[0], r1[1], r1[2], r1[3]);
-      *reinterpret_cast<float4*>(&s_l2[rr][4 * cc]) = make_float4(r2[0], r2[1], r2[2], r2[3]);
+      *reinterpret_cast<float4*>(&s_l1[rr_][4 * cc]) = g.l;
+      *reinterpret_cast<float4*>(&s_l2[rr_][4 * cc]) = g.m;
+    }
+  };
+  const int z = z0 + threadIdx.y, x = x0 + 4 * threadIdx.x;
+  const bool cell_in = z < a.nz && x < a.nx;
+  const int rr = HR + threadIdx.y, cx = HT_H + 4 * threadIdx.x;
+  const long long o = (long long)z * a.pitch + x;
+  const bool row_in = z >= a.ring.iz0 && z < a.ring.iz1;
+  const bool box4 = row_in && x >= a.ring.ix0 && x + 3 < a.ring.ix1;  // all four cells inside the box
+  float4 k4 = f0, kz4 = f0, l2g = f0, l1g = f0, uj4 = f0, g04 = f0, g24 = f0;
+  auto point_loads = [&]() {
+    if (!cell_in) return;
+    k4 = __ldg(reinterpret_cast<const float4*>(kp + o));
+    if (VTI) kz4 = __ldg(reinterpret_cast<const float4*>(a.kz + o));
+    if (!NEAR) {
+      l2g = *reinterpret_cast<const float4*>(a.la2 + fb + o);
+      l1g = *reinterpret_cast<const float4*>(l1 + o);
+    }
+  };
+  // U_j and the gradient of the four cells (reconstruction, gradient term)
+  auto tail_loads = [&]() {
+    if (!cell_in) return;
+    if (a.uout != nullptr && row_in) uj4 = *reinterpret_cast<const float4*>(a.uj + fb + o);
+    if (box4) {
+      g04 = *reinterpret_cast<const float4*>((RHO ? a.grad_rho : a.grad) + fb + o);
+      if (VTI) g24 = *reinterpret_cast<const float4*>(a.grad2 + fb + o);
+    }
+  };
+  if constexpr (PRE) {
+    Grp g[NIT];
+#pragma unroll
+    for (int it = 0; it < NIT; ++it) stage_load(tid + 256 * it, g[it]);
+    point_loads();
+    tail_loads();
+#pragma unroll
+    for (int it = 0; it < NIT; ++it)
+      if (tid + 256 * it < NST) stage_store(tid + 256 * it, g[it]);
+  } else {
+    for (int c = tid; c < NST; c += 256) {
+      Grp g;
+      stage_load(c, g);
+      stage_store(c, g);
     }
   }
   __syncthreads();
-  const int z = z0 + threadIdx.y, x = x0 + 4 * threadIdx.x;
-  if (z >= a.nz || x >= a.nx) return;
-  const int rr = HR + threadIdx.y, cx = HT_H + 4 * threadIdx.x;
-  const long long o = (long long)z * a.pitch + x;
-  const float4 l2v = *reinterpret_cast<const float4*>(a.la2 + fb + o);
-  const float4 l1c = *reinterpret_cast<const float4*>(l1 + o);
-  const float4 k4 = __ldg(reinterpret_cast<const float4*>(kp + o));
-  const float4 kz4 = VTI ? __ldg(reinterpret_cast<const float4*>(a.kz + o)) : k4;
+  if (!cell_in) return;
+  if constexpr (!PRE) point_loads();
+  if (!VTI) kz4 = k4;
+  // La2 and La1 of the four cells (staged in near tiles)
+  const float4 l2v = NEAR ? *reinterpret_cast<const float4*>(&s_l2[rr][cx]) : l2g;
+  const float4 l1c = NEAR ? *reinterpret_cast<const float4*>(&s_l1[rr][cx]) : l1g;
   // variable density: the four half-point buoyancies of the cells (bx+, bx-,
   // bz+, bz-), bz+ of the row above, bz- of the row below, bx+ of the
   // column left of the group and bx- of the column right of it
@@ -529,27 +592,86 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
     }
     return acc;
   };
-  // the one-way sums of the four cells: one copy of the code for every
-  // (cell, side) pair (not unrolled, so the kernel stays small)
+  // top / bottom sides: the four cells share their depth dq, so the strip
+  // cells p = q, q - d, q - 2d (and the wrap) are rows of four
+  auto share4 = [&](int sd, int pz) -> float4 {
+    const long long oo = (long long)pz * a.pitch + x;
+    if (a.wpl != nullptr) return __ldg(reinterpret_cast<const float4*>(a.wpl + (1 + sd) * pl + oo));
+    float4 r;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) set_comp(r, m, x + m < a.nx ? share(sd, pz, x + m) : 0.f);
+    return r;
+  };
+  auto oneway_rows = [&](int sd, int dq, int sz, float4& acc) {
+    auto coefs = [&](int pz, float4& lam, float4& mu) {
+      const float4 c = __ldg(reinterpret_cast<const float4*>(a.vp + (long long)pz * a.pitch + x));
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        set_comp(lam, m, comp(c, m) * a.lamf);
+        set_comp(mu, m, comp(c, m) * comp(c, m) * a.muf);
+      }
+    };
+    float4 lam, mu;
+    if (dq < hw) {
+      const float4 ws = share4(sd, z);
+      coefs(z, lam, mu);
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+        set_comp(acc, m, comp(acc, m) + comp(ws, m) * ((2.f - comp(lam, m) - comp(mu, m)) * s_l1[rr][cx + m] +
+                                                       (comp(lam, m) - 1.f) * s_l2[rr][cx + m]));
+    }
+    if (dq >= 1) {
+      const float4 ws = share4(sd, z - sz);
+      coefs(z - sz, lam, mu);
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+        set_comp(acc, m, comp(acc, m) + comp(ws, m) * ((comp(lam, m) + 2.f * comp(mu, m)) * s_l1[rr - sz][cx + m] -
+                                                       comp(lam, m) * s_l2[rr - sz][cx + m]));
+    }
+    if (dq >= 2) {
+      const float4 ws = share4(sd, z - 2 * sz);
+      coefs(z - 2 * sz, lam, mu);
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+        set_comp(acc, m, comp(acc, m) - comp(ws, m) * comp(mu, m) * s_l1[rr - 2 * sz][cx + m]);
+    }
+    if (dq == 0) {
+      const int pz = z + (hw - 1) * sz;
+      if (pz >= 0 && pz < a.nz) {
+        const float4 ws = share4(sd, pz);
+        coefs(pz, lam, mu);
+        const float4 lw = *reinterpret_cast<const float4*>(l1 + (long long)pz * a.pitch + x);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) set_comp(acc, m, comp(acc, m) - comp(ws, m) * comp(mu, m) * comp(lw, m));
+      }
+    }
+  };
+  // the one-way sums of the four cells: rows of four for the top and bottom
+  // sides; cell by cell (one rolled copy of the code) for the left and right
+  // sides, in the lanes within their reach only
   float4 ow4 = make_float4(0.f, 0.f, 0.f, 0.f);
   if constexpr (NEAR) {
+    if (!mult && z <= hw) oneway_rows(0, z, 1, ow4);
+    if (a.nz - 1 - z <= hw) oneway_rows(1, a.nz - 1 - z, -1, ow4);
+    if (x <= hw || x + 3 >= a.nx - 1 - hw) {
 #pragma unroll 1
-    for (int t = 0; t < 16; ++t) {
-      const int m = t >> 2, sd = t & 3;
-      const int xm = x + m;
-      if (xm >= a.nx) continue;
-      const int dq = sd == 0 ? z : sd == 1 ? a.nz - 1 - z : sd == 2 ? xm : a.nx - 1 - xm;
-      if (dq > hw) continue;
-      const int sz = sd == 0 ? 1 : sd == 1 ? -1 : 0, sx = sd == 2 ? 1 : sd == 3 ? -1 : 0;
-      set_comp(ow4, m, comp(ow4, m) + oneway(sd, dq, sz, sx, xm, cx + m));
+      for (int t = 0; t < 8; ++t) {
+        const int m = t >> 1, sd = 2 + (t & 1);
+        const int xm = x + m;
+        if (xm >= a.nx) continue;
+        const int dq = sd == 2 ? xm : a.nx - 1 - xm;
+        if (dq > hw) continue;
+        set_comp(ow4, m, comp(ow4, m) + oneway(sd, dq, 0, sd == 2 ? 1 : -1, xm, cx + m));
+      }
     }
   }
+  const float4 wq4 = wi4_at(z, x);
   const float ch = 0.5f * a.w.c[0];
   float v[4], L[4], Lz[4];
 #pragma unroll
   for (int m = 0; m < 4; ++m) {
     const int xm = x + m;
-    const float wq = (xm < a.nx) ? wi_at(z, xm) : 0.f;
+    const float wq = (xm < a.nx) ? comp(wq4, m) : 0.f;
     const float ow = NEAR ? comp(ow4, m) : 0.f;
     float lap, lu, luz = 0.f;
     if (RHO) {
@@ -609,12 +731,11 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
   }
   *reinterpret_cast<float4*>(a.lout + fb + o) = make_float4(v[0], v[1], v[2], v[3]);
   // gradient and reconstruction inside the box; the saved ring (or 0) outside
-  const bool row_in = z >= a.ring.iz0 && z < a.ring.iz1;
+  if constexpr (!PRE) tail_loads();
   float uo[4] = {0.f, 0.f, 0.f, 0.f};
   float ujv[4] = {0.f, 0.f, 0.f, 0.f};
   if (a.uout != nullptr && row_in) {
-    const float4 uj = *reinterpret_cast<const float4*>(a.uj + fb + o);
-    ujv[0] = uj.x; ujv[1] = uj.y; ujv[2] = uj.z; ujv[3] = uj.w;
+    ujv[0] = uj4.x; ujv[1] = uj4.y; ujv[2] = uj4.z; ujv[3] = uj4.w;
     if (a.src_ptr != nullptr) {
       for (int q = a.src_ptr[b]; q < a.src_ptr[b + 1]; ++q) {
         const int dx = a.src_x[q] - x;
@@ -638,10 +759,10 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
     t[3] = vC * (s_u[rr + 1][cx + m] - u0);
     t[4] = -vC * (u0 - s_u[rr - 1][cx + m]);
   };
-  if (row_in && x >= a.ring.ix0 && x + 3 < a.ring.ix1) {
+  if (box4) {
     // all four columns inside the box: vector gradient update and reconstruction
     float4* gp = reinterpret_cast<float4*>((RHO ? a.grad_rho : a.grad) + fb + o);
-    const float4 g0 = *gp;
+    const float4 g0 = g04;
     if constexpr (RHO) {
       float t[4][5];
 #pragma unroll
@@ -655,7 +776,7 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
     } else if (VTI) {
       *gp = make_float4(g0.x + v[0] * L[0], g0.y + v[1] * L[1], g0.z + v[2] * L[2], g0.w + v[3] * L[3]);
       float4* gq = reinterpret_cast<float4*>(a.grad2 + fb + o);
-      const float4 h0 = *gq;
+      const float4 h0 = g24;
       *gq = make_float4(h0.x + v[0] * Lz[0], h0.y + v[1] * Lz[1], h0.z + v[2] * Lz[2], h0.w + v[3] * Lz[3]);
     } else {
       *gp = make_float4(g0.x + v[0] * k4.x * L[0], g0.y + v[1] * k4.y * L[1], g0.z + v[2] * k4.z * L[2],

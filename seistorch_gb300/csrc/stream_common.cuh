@@ -151,6 +151,6 @@ static int resident_blocks(Kern kern, int threads, size_t smem) {
 }
 
 // Variant selection shared with the host (acoustic_stream.cu).
-extern int g_fwd_cfg, g_bwd_cfg;
+extern int g_fwd_cfg, g_bwd_cfg, g_habc_fwd_cfg;
 
 }  // namespace sgb
