@@ -28,6 +28,9 @@ struct GemmArgs {
   float* out_f32;  // CONV: optional fp32 copy; WGRAD: dW [Cout][Cin][3][3] (accumulated)
   int out_cstride, out_coff;
   int* status;
+  // logical tile grid (x, y, z) of the persistent kernel: tile t is
+  // (t % gx, (t / gx) % gy, t / (gx * gy))
+  int gx, gy, gz;
 };
 
 }  // namespace nn
