@@ -419,9 +419,21 @@ cudaError_t launch_t(const CUtensorMap* maps, const GemmArgs& g0, dim3 grid, cud
     const int pad = sm_bytes / (tm + 1) + 1;  // tm + 1 CTAs of this size no longer fit
     if (pad > smem) smem = pad;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 192, smem) != cudaSuccess || nb < 1) nb = 1;
+    // residency from the kernel's own resources: registers (allocated per
+    // warp in units of 256), static + dynamic shared memory (plus the 1 KB
+    // the system reserves per CTA), TMEM columns
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, kern);
+    if (e != cudaSuccess) return e;
+    int regs_sm = 0;
+    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;
+    const int by_regs = warp_regs > 0 ? regs_sm / (warp_regs * 6) : 1;
+    const int by_smem = sm_bytes / ((int)fa.sharedSizeBytes + smem + 1024);
+    int nb = by_regs < by_smem ? by_regs : by_smem;
+    if (nb < 1) nb = 1;
     per_sm = nb < tm ? nb : tm;
   }
   GemmArgs g = g0;

@@ -83,8 +83,18 @@ __global__ void to_chw_kernel(int n, int h, int w, int c, int cstride, int coff,
 }
 
 // Input convolution: 2 fp32 channels [n][2][h][w] -> c bf16 channels (ReLU).
+template <bool SMEM_W>
 __global__ void conv_in_fwd_kernel(int n, int h, int w, int c, const float* in, const float* W, const float* b,
                                    bf16* out, int cstride, int coff) {
+  // the weights (18 per output channel) and biases: staged once per block
+  // where they fit, read by every thread of the block as broadcasts
+  extern __shared__ float cin_w[];
+  if (SMEM_W) {
+    for (int k = threadIdx.x; k < 19 * c; k += blockDim.x) cin_w[k] = k < 18 * c ? W[k] : b[k - 18 * c];
+    __syncthreads();
+  }
+  const float* Wp = SMEM_W ? cin_w : W;
+  const float* bp = SMEM_W ? cin_w + 18 * c : b;
   const long long total = (long long)n * h * w;
   GRID_STRIDE(i, total) {
     const int x = (int)(i % w);
@@ -103,8 +113,9 @@ __global__ void conv_in_fwd_kernel(int n, int h, int w, int c, const float* in, 
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const int co = c8 + j;
-        float a = b[co];
-        for (int k = 0; k < 18; ++k) a = fmaf(W[co * 18 + k], v[k], a);
+        float a = bp[co];
+#pragma unroll
+        for (int k = 0; k < 18; ++k) a = fmaf(Wp[co * 18 + k], v[k], a);
         o[j] = a > 0.f ? a : 0.f;
       }
       st8(out + i * cstride + coff + c8, pack8(o));
@@ -169,6 +180,69 @@ __global__ void conv_out_fwd_kernel(int n, int h, int w, int c, const bf16* in, 
       }
     out[i] = a;
   }
+}
+
+// The same convolution for c <= 64 from shared memory: a block of 256
+// threads takes 256 pixels of one image row, stages the three input rows
+// (258 pixels with the halo, c channels, 16-byte vectors) and the weights
+// (tap-major) once, and each thread sums its pixel's 9 taps from there.  A
+// thread walks its pixel's channel vectors starting at (lane mod c/8), so
+// that the 8 threads of a 16-byte access phase hit distinct banks.
+constexpr int COUT_TX = 256;
+template <int CV>  // channel vectors per pixel (c = 8 CV)
+__global__ void __launch_bounds__(COUT_TX) conv_out_tile_kernel(int n, int h, int w, const bf16* in, int cstride,
+                                                                 const float* W, const float* b, float* out) {
+  extern __shared__ __align__(16) unsigned char cout_smem[];
+  constexpr int cv = CV, c = 8 * CV, cols = COUT_TX + 2;
+  uint4* srow = reinterpret_cast<uint4*>(cout_smem);  // [3][cols][cv]
+  float* ws = reinterpret_cast<float*>(srow + 3 * cols * cv);  // [9][c]
+  const int ntx = (w + COUT_TX - 1) / COUT_TX;
+  const int xt = blockIdx.x % ntx;
+  const long long ry = blockIdx.x / ntx;
+  const int y = (int)(ry % h), bb = (int)(ry / h);
+  const int x0 = xt * COUT_TX;
+  for (int k = threadIdx.x; k < 9 * c; k += COUT_TX) {
+    const int tap = k / c, ci = k - tap * c;
+    ws[k] = W[ci * 9 + tap];
+  }
+  // eight vectors per thread in flight at a time: loads first, then stores
+  const int nvec = 3 * cols * cv;
+  for (int k0 = threadIdx.x; k0 < nvec; k0 += 8 * COUT_TX) {
+    uint4 q[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int k = k0 + u * COUT_TX;
+      q[u] = make_uint4(0u, 0u, 0u, 0u);
+      if (k < nvec) {
+        const int v = k % cv, rc = k / cv;
+        const int col = rc % cols, r = rc / cols;
+        const int yy = y - 1 + r, xx = x0 - 1 + col;
+        if (yy >= 0 && yy < h && xx >= 0 && xx < w) q[u] = ld8(in + (((long long)bb * h + yy) * w + xx) * cstride + 8 * v);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (k0 + u * COUT_TX < nvec) srow[k0 + u * COUT_TX] = q[u];
+  }
+  __syncthreads();
+  const int t = threadIdx.x, x = x0 + t;
+  if (x >= w) return;
+  float acc[4] = {b[0], 0.f, 0.f, 0.f};  // four partial sums: short FMA chains
+#pragma unroll
+  for (int tap = 0; tap < 9; ++tap) {
+    const int ky = tap / 3, kx = tap - 3 * ky;
+    const uint4* px = srow + (ky * cols + t + kx) * cv;
+    const float* wt = ws + tap * c;
+#pragma unroll
+    for (int vv = 0; vv < cv; ++vv) {
+      const int v = (vv + t) & (cv - 1);
+      float f[8];
+      unpack8(px[v], f);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[j & 3] = fmaf(wt[8 * v + j], f[j], acc[j & 3]);
+    }
+  }
+  out[((long long)bb * h + y) * w + x] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
 }
 
 // Data gradient of the output convolution, times [act > 0] (the ReLU of the
@@ -411,7 +485,12 @@ cudaError_t launch_to_chw(int n, int h, int w, int c, int cstride, int coff, con
 
 cudaError_t launch_conv_in_fwd(int n, int h, int w, int c, const float* in, const float* W, const float* b, bf16* out,
                                int cstride, int coff, cudaStream_t s) {
-  conv_in_fwd_kernel<<<blocks_for((long long)n * h * w), 256, 0, s>>>(n, h, w, c, in, W, b, out, cstride, coff);
+  if (c <= 256)
+    conv_in_fwd_kernel<true><<<blocks_for((long long)n * h * w), 256, (size_t)19 * c * 4, s>>>(n, h, w, c, in, W, b,
+                                                                                           out, cstride, coff);
+  else
+    conv_in_fwd_kernel<false><<<blocks_for((long long)n * h * w), 256, 0, s>>>(n, h, w, c, in, W, b, out, cstride,
+                                                                              coff);
   return cudaGetLastError();
 }
 
@@ -424,6 +503,19 @@ cudaError_t launch_conv_in_wgrad(int n, int h, int w, int c, const float* in, co
 
 cudaError_t launch_conv_out_fwd(int n, int h, int w, int c, const bf16* in, int cstride, const float* W,
                                 const float* b, float* out, cudaStream_t s) {
+  if (c == 32 || c == 64) {
+    const size_t smem = (size_t)3 * (COUT_TX + 2) * (c / 8) * 16 + (size_t)9 * c * 4;
+    auto kern = c == 32 ? conv_out_tile_kernel<4> : conv_out_tile_kernel<8>;
+    static bool set[2] = {false, false};
+    if (!set[c == 64]) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      set[c == 64] = true;
+    }
+    const long long blocks = (long long)n * h * ((w + COUT_TX - 1) / COUT_TX);
+    kern<<<(unsigned)blocks, COUT_TX, smem, s>>>(n, h, w, in, cstride, W, b, out);
+    return cudaGetLastError();
+  }
   conv_out_fwd_kernel<<<blocks_for((long long)n * h * w), 256, 0, s>>>(n, h, w, c, in, cstride, W, b, out);
   return cudaGetLastError();
 }

@@ -7,11 +7,14 @@
 * Orders 6 and 8 (no reference golden at these orders): records of the
   HABC loop vs the fp64 oracle (``fd2d.forward``, whose order-8 stencil is
   pinned by the PML goldens and whose HABC blend by the o2 / o4 goldens),
-  relative L2 <= 1e-5; and the boundary-saving gradient's directional
-  derivative <g, dv> for a smooth dv inside the undamped box vs the central
-  difference (J(vp + e dv) - J(vp - e dv)) / 2e of the oracle's fp64
-  misfit, relative error <= 1e-3 (the fp32 gradient against an fp64
-  difference quotient with O(e^2) truncation).
+  relative L2 <= 1e-5; and the boundary-saving gradient of J = sum syn^2
+  (zero observed data, as the reference's gradient goldens) at single cells
+  -- a source, a receiver-row cell, the undamped box's top edge, the
+  interior -- vs central differences (J(vp + e d_q) - J(vp - e d_q)) / 2e of
+  the oracle's fp64 J, relative error <= 1e-3 (observed: 1e-6 .. 3e-5).
+  With nonzero observed data the gradient near a source is the small
+  difference of large terms and fp32 residuals cannot resolve it, so the
+  zero-data misfit is the well-conditioned probe.
 """
 import numpy as np
 import pytest
@@ -69,11 +72,7 @@ def _case(order):
     wav = fd2d.ricker(15.0, dt, nt, delay=60)
     src = [[(w + 2, w + 12)], [(w + 2, w + 48)]]
     rec = [([w + 2] * nxi, list(range(w, w + nxi)))] * 2
-    # a smooth perturbation well inside the undamped box (rows and columns
-    # 50 .. 109; below 1e-8 at its edges)
-    dv = np.exp(-((zz - 80) ** 2 + (xx - 78) ** 2) / 40.0)
-    return dict(w=w, nt=nt, dt=dt, h=h, order=order, vp0=vp0, vp_true=vp_true, b=b, wav=wav, src=src, rec=rec,
-                dv=dv)
+    return dict(w=w, nt=nt, dt=dt, h=h, order=order, vp0=vp0, vp_true=vp_true, b=b, wav=wav, src=src, rec=rec)
 
 
 def _oracle_records(c, vp):
@@ -91,21 +90,21 @@ def test_habc_high_order_records_and_gradient_vs_oracle(dev, order):
     prop = engine.AcousticPropagator(nz, nx, c["dt"], c["h"], order, "habc", c["w"], False, dev)
     acq = engine.Acquisition(nz, nx, c["src"], c["rec"], c["wav"], dev)
     bt = torch.tensor(c["b"], dtype=torch.float32, device=dev)
-    obs_np = _oracle_records(c, c["vp_true"])
     # records vs the fp64 oracle
     with torch.no_grad():
         r, _ = engine.acoustic_loop(torch.tensor(c["vp_true"], dtype=torch.float32, device=dev), prop, bt, acq)
     got = r.reshape(nt, B, nrec, 1).permute(1, 0, 2, 3).cpu().numpy()
-    assert rel_l2(got, obs_np) < 1e-5
-    # the boundary-saving gradient of J = sum (syn - obs)^2
-    obs = torch.tensor(obs_np, dtype=torch.float32, device=dev).permute(1, 0, 2, 3).reshape(r.shape)
+    assert rel_l2(got, _oracle_records(c, c["vp_true"])) < 1e-5
+    # the boundary-saving gradient of J = sum syn^2
     vp = torch.tensor(c["vp0"], dtype=torch.float32, device=dev, requires_grad=True)
     syn, _ = engine.acoustic_loop(vp, prop, bt, acq, False, engine.default_ckpt_every(nt))
-    ((syn - obs) ** 2).sum().backward()
+    (syn.double() ** 2).sum().backward()
     g = vp.grad.double().cpu().numpy()
-    directional = float((g * c["dv"]).sum())
-    J = lambda v: float(((_oracle_records(c, v) - obs_np) ** 2).sum())
-    e = 2.0  # m/s at the centre of dv
-    fd = (J(c["vp0"] + e * c["dv"]) - J(c["vp0"] - e * c["dv"])) / (2.0 * e)
-    print(f"o{order}: <g, dv> = {directional:.6e}, central difference {fd:.6e}")
-    assert abs(directional - fd) < 1e-3 * abs(fd)
+    J = lambda v: float((_oracle_records(c, v) ** 2).sum())
+    e = 1e-2  # m/s
+    for (iz, ix) in [(52, 62), (52, 80), (50, 70), (60, 62)]:
+        dq = np.zeros_like(c["vp0"])
+        dq[iz, ix] = 1.0
+        fd = (J(c["vp0"] + e * dq) - J(c["vp0"] - e * dq)) / (2.0 * e)
+        print(f"o{order} cell ({iz}, {ix}): gradient {g[iz, ix]:.6e}, central difference {fd:.6e}")
+        assert abs(g[iz, ix] - fd) < 1e-3 * abs(fd)
