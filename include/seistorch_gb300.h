@@ -219,7 +219,7 @@ int sgb_acoustic_forward(const sgb_grid *grid, const sgb_acoustic_model *model,
 /* Adjoint of sgb_acoustic_forward (PML or HABC): boundary-saving
  * reconstruction of the forward wavefield in the interior box + adjoint time
  * stepping + vp gradient, in one fused kernel per step (PML: TMA tile
- * pipeline; HABC: a per-cell kernel that also applies the transposed
+ * pipeline; HABC: a tiled kernel that also applies the transposed
  * one-way boundary blend, acoustic_habc.py:79-204; model->vp and
  * model->damp = the HABC weights are required).  Replaces the autograd path
  * of checkpoint_new.py:146-217 with an exact discrete adjoint.
@@ -227,7 +227,10 @@ int sgb_acoustic_forward(const sgb_grid *grid, const sgb_acoustic_model *model,
  *               ubuf[uprev] = U_{nt-1} (as left by sgb_acoustic_forward);
  *   lbuf[0..2]: [nshots][nz][pitch] adjoint scratch (zeroed here);
  *   acq->records: dJ/d(records) [nt][nrec][nch] (the adjoint source);
- *   grad_shot: [nshots][nz][pitch] per-shot accumulation, zeroed here;
+ *   grad_shot: [nshots][nz][pitch] scratch: the adjoint adds every shot's
+ *              gradient term into its first [nz][pitch] plane (zeroed here)
+ *              with reduction atomics, so the order of the sum over shots
+ *              is not fixed;
  *   grad_vp: [nz][pitch] out, dJ/dvp inside the interior box, 0 outside. */
 int sgb_acoustic_backward(const sgb_grid *grid, const sgb_acoustic_model *model,
                           const sgb_acquisition *acq, const sgb_bs_store *bs,

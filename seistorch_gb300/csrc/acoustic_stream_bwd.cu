@@ -10,7 +10,10 @@
 //   nu_j = g (nu1 - nu2) + nu2 + k (L(nu1) + R^T r_{j-1}),
 // and dJ/dvp = (2/vp) sum_j nu_j L(U_{j-1}).  One kernel per reverse step:
 //   * nu_j from nu_{j+1} (haloed) and nu_{j+2};
-//   * the gradient term nu_j L(U_{j-1}) inside the undamped box;
+//   * the gradient term nu_j L(U_{j-1}) inside the undamped box, added to
+//     one gradient plane shared by all shots with 16-byte reduction atomics
+//     (the plane stays in L2; per-shot planes cost 8 B of DRAM traffic per
+//     shot-point and step);
 //   * the reconstruction U_{j-2} = 2 U_{j-1} - (U_j - S w_{j-1}) + k L(U_{j-1})
 //     inside the box (g = 2 there), the saved ring around it (each CTA
 //     copies a share after its tiles), 0 in the damped band.
@@ -24,16 +27,15 @@ struct BwdTileLayout {
   static constexpr int UROWS = TZ + 2 * R;
   static constexpr int UF = round32(UROWS * UW);
   static constexpr int PF = TZ * TX;
-  static constexpr int STAGE = 2 * UF + PF;  // U_{j-1}, nu_{j+1} (haloed) | grad
+  static constexpr int STAGE = 2 * UF;  // U_{j-1}, nu_{j+1} (haloed)
   static constexpr size_t BYTES = (size_t)(S * STAGE + PF) * 4 + S * 8;  // + adjoint-source tile
-  static constexpr uint32_t TX_BYTES = (2 * UROWS * UW + TZ * TX) * 4;
+  static constexpr uint32_t TX_BYTES = 2 * UROWS * UW * 4;
 };
 
 template <int R, int TZ, int NWP, int S>
 __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_tile_kernel(
     const __grid_constant__ CUtensorMap tm_u,     // U_{j-1}   box {W, TZ+2R, 1}
     const __grid_constant__ CUtensorMap tm_n,     // nu_{j+1}  box {W, TZ+2R, 1}
-    const __grid_constant__ CUtensorMap tm_grad,  // grad_shot box {128, TZ, 1}
     const AcBwdStreamArgs a) {
   using Lay = BwdTileLayout<R, TZ, S>;
   constexpr int RPW = TZ / NWP;
@@ -54,7 +56,6 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_
     mbar_arrive_expect_tx(&bars[stage], Lay::TX_BYTES);
     tma_load_3d(st, &tm_u, g.x0 - LO, g.z0 - R, g.b, &bars[stage]);
     tma_load_3d(st + Lay::UF, &tm_n, g.x0 - LO, g.z0 - R, g.b, &bars[stage]);
-    tma_load_3d(st + 2 * Lay::UF, &tm_grad, g.x0, g.z0, g.b, &bars[stage]);
   };
   if (tid == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
@@ -118,7 +119,6 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_
     if (!mbar_wait(&bars[stage], (k / S) & 1, a.status)) s_abort = 1;
     const float* st = smem + stage * Lay::STAGE;
     const float* sn = st + Lay::UF;
-    const float* sgr = st + 2 * Lay::UF;
     const bool cols_all = x >= a.ring.ix0 && x + 3 < a.ring.ix1;
     const bool cols_any = x + 3 >= a.ring.ix0 && x < a.ring.ix1;
     const int lr0 = wid * RPW;
@@ -137,7 +137,6 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_
       wn[2 * R] = lds4(sn + (lr + 2 * R) * UW + LO + 4 * lane);
       const float4 LU = lap_row<R>(wu, st + (lr + R) * UW, lane, a.w);
       const float4 LN = lap_row<R>(wn, sn + (lr + R) * UW, lane, a.w);
-      float4 gs = lds4(sgr + lr * TX + 4 * lane);
       float4 inj = make_float4(0.f, 0.f, 0.f, 0.f);
       if (has_rec) {
         inj = lds4(sinj + lr * TX + 4 * lane);
@@ -157,18 +156,13 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_
         *reinterpret_cast<float4*>(a.lout + goff) = nj;
         const bool zin = z >= a.ring.iz0 && z < a.ring.iz1;
         if (zin && cols_any) {
-          if (cols_all) {
-            gs.x = fmaf(nj.x, LU.x, gs.x);
-            gs.y = fmaf(nj.y, LU.y, gs.y);
-            gs.z = fmaf(nj.z, LU.z, gs.z);
-            gs.w = fmaf(nj.w, LU.w, gs.w);
-          } else {
+          float4 gs = make_float4(nj.x * LU.x, nj.y * LU.y, nj.z * LU.z, nj.w * LU.w);
+          if (!cols_all) {
 #pragma unroll
             for (int m = 0; m < 4; ++m)
-              if (x + m >= a.ring.ix0 && x + m < a.ring.ix1)
-                set_comp(gs, m, fmaf(comp(nj, m), comp(LU, m), comp(gs, m)));
+              if (x + m < a.ring.ix0 || x + m >= a.ring.ix1) set_comp(gs, m, 0.f);
           }
-          *reinterpret_cast<float4*>(a.grad_shot + goff) = gs;
+          red_add4(a.grad_shot + (goff - fbase), gs);
         }
         if (a.do_recon) {
           float4 uo;
@@ -231,7 +225,7 @@ static cudaError_t bwd_tile_t(const CUtensorMap* maps, const AcBwdStreamArgs& a,
     blocks = resident_blocks(kern, 32 * NWP, smem);
   }
   const int tiles = a.nshots * a.ntx * a.nzc;
-  kern<<<(unsigned)(tiles < blocks ? tiles : blocks), 32 * NWP, smem, s>>>(maps[0], maps[1], maps[2], a);
+  kern<<<(unsigned)(tiles < blocks ? tiles : blocks), 32 * NWP, smem, s>>>(maps[0], maps[1], a);
   return cudaGetLastError();
 }
 

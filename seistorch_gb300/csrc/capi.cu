@@ -796,8 +796,9 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
   const Ring ring = make_ring(*grid, bs->iz0, bs->iz1, bs->ix0, bs->ix1, bs->ring);
   if (ring.size != bs->ring_size) return SGB_ERR_SHAPE;
   for (int i = 0; i < 3; ++i) SGB_CUDA_CHECK(cudaMemsetAsync(lbuf[i], 0, field * sizeof(float), s));
-  SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot, 0, ngrad * field * sizeof(float), s));
-  if (grad_shot2 != nullptr) SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot2, 0, field * sizeof(float), s));
+  // the adjoints accumulate every shot into plane 0 of each gradient field
+  for (int q = 0; q < ngrad; ++q) SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot + q * field, 0, plane * sizeof(float), s));
+  if (grad_shot2 != nullptr) SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot2, 0, plane * sizeof(float), s));
   const int R = model->order / 2;
   const int nt = acq->nt;
   const int K = bs->ckpt_every;
@@ -846,23 +847,25 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
     rim.ix0 = ring.ix0 > 0 ? ring.ix0 - 1 : 0;
     rim.iz1 = ring.iz1 < grid->nz ? ring.iz1 + 1 : grid->nz;
     rim.ix1 = ring.ix1 < grid->nx ? ring.ix1 + 1 : grid->nx;
+    // every shot's terms went into plane 0 of each gradient field
+    sgb_grid one = *grid;
+    one.nshots = 1;
     for (int q = 0; q < ngrad; ++q)
-      SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot + q * field, gscale, q == 0 ? ring : rim,
+      SGB_CUDA_CHECK(launch_acoustic_grad_reduce(one, grad_shot + q * field, gscale, q == 0 ? ring : rim,
                                                  grad_vp + q * plane, s));
-    if (kz != nullptr) SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot2, nullptr, ring, grad_out2, s));
+    if (kz != nullptr) SGB_CUDA_CHECK(launch_acoustic_grad_reduce(one, grad_shot2, nullptr, ring, grad_out2, s));
     return SGB_OK;
   }
   // tensor maps: haloed stencil boxes (136 x (TZ+2R)) and point boxes
   // (128 x TZ) of every rotating buffer; lbuf carries nu = k * Lambda
   const int tzr = bwd_tile_rows();
   const int bw = stencil_box_width(R);
-  CUtensorMap uf[3], nf[3], mgrad;
+  CUtensorMap uf[3], nf[3];
   for (int i = 0; i < 3; ++i) {
     if (field_map(&uf[i], ubuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R) ||
         field_map(&nf[i], lbuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R))
       return SGB_ERR_CUDA;
   }
-  if (field_map(&mgrad, grad_shot, grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr)) return SGB_ERR_CUDA;
   if ((acq->nsrc > 0 && acq->src_zr == nullptr) || (acq->records != nullptr && acq->rec_zr == nullptr))
     return SGB_ERR_ARG;
   AcBwdStreamArgs sb;
@@ -903,7 +906,7 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
     sb.do_recon = j >= 3;
     sb.t_src = j - 1;
     sb.resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
-    const CUtensorMap maps[3] = {uf[ujm1], nf[l1], mgrad};
+    const CUtensorMap maps[2] = {uf[ujm1], nf[l1]};
     sb.ring_in = j >= 3 ? bs->ring_store + (long long)(j - 3) * grid->nshots * ring.size : nullptr;
     SGB_CUDA_CHECK(launch_acoustic_bwd_stream(R, maps, sb, s));
     if (ck && j >= 3) {
@@ -919,7 +922,10 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
     l1 = lfree;
     lfree = old_l2;
   }
-  SGB_CUDA_CHECK(launch_acoustic_grad_reduce(*grid, grad_shot, gscale, ring, grad_vp, s));
+  // every shot's gradient term went into plane 0 of grad_shot
+  sgb_grid one = *grid;
+  one.nshots = 1;
+  SGB_CUDA_CHECK(launch_acoustic_grad_reduce(one, grad_shot, gscale, ring, grad_vp, s));
   return SGB_OK;
 }
 

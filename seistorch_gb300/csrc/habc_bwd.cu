@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
   const long long o = (long long)z * a.pitch + x;
   const bool row_in = z >= a.ring.iz0 && z < a.ring.iz1;
   const bool box4 = row_in && x >= a.ring.ix0 && x + 3 < a.ring.ix1;  // all four cells inside the box
-  float4 k4 = f0, kz4 = f0, l2g = f0, l1g = f0, uj4 = f0, g04 = f0, g24 = f0;
+  float4 k4 = f0, kz4 = f0, l2g = f0, l1g = f0, uj4 = f0;
   auto point_loads = [&]() {
     if (!cell_in) return;
     k4 = __ldg(reinterpret_cast<const float4*>(kp + o));
@@ -492,14 +492,10 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
       l1g = *reinterpret_cast<const float4*>(l1 + o);
     }
   };
-  // U_j and the gradient of the four cells (reconstruction, gradient term)
+  // U_j of the four cells (reconstruction)
   auto tail_loads = [&]() {
     if (!cell_in) return;
     if (a.uout != nullptr && row_in) uj4 = *reinterpret_cast<const float4*>(a.uj + fb + o);
-    if (box4) {
-      g04 = *reinterpret_cast<const float4*>((RHO ? a.grad_rho : a.grad) + fb + o);
-      if (VTI) g24 = *reinterpret_cast<const float4*>(a.grad2 + fb + o);
-    }
   };
   if constexpr (PRE) {
     Grp g[NIT];
@@ -759,28 +755,21 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
     t[3] = vC * (s_u[rr + 1][cx + m] - u0);
     t[4] = -vC * (u0 - s_u[rr - 1][cx + m]);
   };
+  // gradient terms: every shot adds into plane 0 of its gradient field(s)
+  // (16-byte reductions in L2; the shot reduction reads that plane)
   if (box4) {
     // all four columns inside the box: vector gradient update and reconstruction
-    float4* gp = reinterpret_cast<float4*>((RHO ? a.grad_rho : a.grad) + fb + o);
-    const float4 g0 = g04;
     if constexpr (RHO) {
       float t[4][5];
 #pragma unroll
       for (int m = 0; m < 4; ++m) rho_terms(m, t[m]);
 #pragma unroll
-      for (int q = 0; q < 5; ++q) {
-        float4* gq = reinterpret_cast<float4*>(a.grad_rho + q * fs + fb + o);
-        const float4 h0 = q == 0 ? g0 : *gq;
-        *gq = make_float4(h0.x + t[0][q], h0.y + t[1][q], h0.z + t[2][q], h0.w + t[3][q]);
-      }
+      for (int q = 0; q < 5; ++q) red_add4(a.grad_rho + q * fs + o, make_float4(t[0][q], t[1][q], t[2][q], t[3][q]));
     } else if (VTI) {
-      *gp = make_float4(g0.x + v[0] * L[0], g0.y + v[1] * L[1], g0.z + v[2] * L[2], g0.w + v[3] * L[3]);
-      float4* gq = reinterpret_cast<float4*>(a.grad2 + fb + o);
-      const float4 h0 = g24;
-      *gq = make_float4(h0.x + v[0] * Lz[0], h0.y + v[1] * Lz[1], h0.z + v[2] * Lz[2], h0.w + v[3] * Lz[3]);
+      red_add4(a.grad + o, make_float4(v[0] * L[0], v[1] * L[1], v[2] * L[2], v[3] * L[3]));
+      red_add4(a.grad2 + o, make_float4(v[0] * Lz[0], v[1] * Lz[1], v[2] * Lz[2], v[3] * Lz[3]));
     } else {
-      *gp = make_float4(g0.x + v[0] * k4.x * L[0], g0.y + v[1] * k4.y * L[1], g0.z + v[2] * k4.z * L[2],
-                        g0.w + v[3] * k4.w * L[3]);
+      red_add4(a.grad + o, make_float4(v[0] * k4.x * L[0], v[1] * k4.y * L[1], v[2] * k4.z * L[2], v[3] * k4.w * L[3]));
     }
     if (a.uout != nullptr) {
 #pragma unroll
@@ -801,14 +790,14 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
         float t[5];
         rho_terms(m, t);
 #pragma unroll
-        for (int q = 0; q < 5; ++q) a.grad_rho[q * fs + fb + om] += t[q];
+        for (int q = 0; q < 5; ++q) atomicAdd(a.grad_rho + q * fs + om, t[q]);
         uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + kk * L[m];
       } else if (VTI) {
-        a.grad[fb + om] += v[m] * L[m];
-        a.grad2[fb + om] += v[m] * Lz[m];
+        atomicAdd(a.grad + om, v[m] * L[m]);
+        atomicAdd(a.grad2 + om, v[m] * Lz[m]);
         uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + kk * L[m] + comp(kz4, m) * Lz[m];
       } else {
-        a.grad[fb + om] += v[m] * kk * L[m];
+        atomicAdd(a.grad + om, v[m] * kk * L[m]);
         uo[m] = 2.f * s_u[rr][cx + m] - ujv[m] + kk * L[m];
       }
     } else {
@@ -821,10 +810,10 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
         if (xr || xl || zd || zu) {
           float t[5];
           rho_terms(m, t);
-          if (xr) a.grad_rho[fs + fb + om] += t[1];
-          if (xl) a.grad_rho[2 * fs + fb + om] += t[2];
-          if (zd) a.grad_rho[3 * fs + fb + om] += t[3];
-          if (zu) a.grad_rho[4 * fs + fb + om] += t[4];
+          if (xr) atomicAdd(a.grad_rho + fs + om, t[1]);
+          if (xl) atomicAdd(a.grad_rho + 2 * fs + om, t[2]);
+          if (zd) atomicAdd(a.grad_rho + 3 * fs + om, t[3]);
+          if (zu) atomicAdd(a.grad_rho + 4 * fs + om, t[4]);
         }
       }
       if (a.uout != nullptr) {

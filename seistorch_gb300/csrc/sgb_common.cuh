@@ -121,6 +121,13 @@ FdWeights fd_weights(int order);
 
 int set_cuda_error(cudaError_t e);
 
+// p[0..3] += v as one 16-byte reduction in L2 (p 16-byte aligned): the
+// adjoints add every shot's gradient term into one plane with it.
+__device__ __forceinline__ void red_add4(float* p, const float4& v) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};\n" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+               : "memory");
+}
+
 }  // namespace sgb
 
 #define SGB_CUDA_CHECK(expr)                              \
