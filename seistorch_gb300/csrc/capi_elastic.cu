@@ -248,8 +248,9 @@ int sgb_elastic_backward(const sgb_grid* grid, const sgb_elastic_model* model, c
   a.status = status_ptr();
   const long long field = (long long)grid->nz * grid->pitch * grid->nshots;
   for (int f = 0; f < 10; ++f) SGB_CUDA_CHECK(cudaMemsetAsync(abuf[f], 0, field * sizeof(float), s));
+  // the reverse loop adds every shot's gradient terms into plane 0 of each field
   for (int k = 0; k < 3; ++k) {
-    SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot[k], 0, field * sizeof(float), s));
+    SGB_CUDA_CHECK(cudaMemsetAsync(grad_shot[k], 0, (long long)grid->nz * grid->pitch * sizeof(float), s));
     a.grad[k] = grad_shot[k];
   }
   const int nt = acq->nt;
@@ -278,7 +279,9 @@ int sgb_elastic_backward(const sgb_grid* grid, const sgb_elastic_model* model, c
   }
   if (grad_out != nullptr && vp != nullptr && vs != nullptr && rho != nullptr) {
     const float* gs[3] = {grad_shot[0], grad_shot[1], grad_shot[2]};
-    SGB_CUDA_CHECK(launch_elastic_grad(*grid, model->coef, gs, vp, vs, rho, 1, bs->iz0, bs->iz1, bs->ix0, bs->ix1,
+    sgb_grid one = *grid;
+    one.nshots = 1;
+    SGB_CUDA_CHECK(launch_elastic_grad(one, model->coef, gs, vp, vs, rho, 1, bs->iz0, bs->iz1, bs->ix0, bs->ix1,
                                        grad_out, s));
   }
   return SGB_OK;

@@ -79,6 +79,7 @@ def test_born_single_step_matches_oracle(dev):
     the oracle's Born step on random fields."""
     from seistorch_gb300.equations2d import acoustic_lsrtm_habc as mod
     g = load("born_habc_o2")
+    mod.spatial_order = g["order"]
     rng = np.random.default_rng(1)
     nz, nx = g["models"]["vp"].shape
     f = [rng.standard_normal((2, nz, nx)).astype(np.float32) for _ in range(4)]

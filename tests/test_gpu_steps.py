@@ -53,6 +53,21 @@ def _case(name):
     return g
 
 
+@pytest.fixture(autouse=True)
+def _keep_spatial_orders():
+    """The equation modules keep their spatial order in a module global (as
+    the reference's do); restore every one after each test so that later
+    tests see the default."""
+    from seistorch_gb300.equations2d import (acoustic, acoustic_habc, acoustic_lsrtm_habc, acoustic_rho_habc,
+                                             vacoustic_habc, vti_habc2)
+    mods = [acoustic, acoustic_habc, acoustic_lsrtm_habc, acoustic_rho_habc, vacoustic_habc, vti_habc2]
+    saved = [getattr(m, "spatial_order", None) for m in mods]
+    yield
+    for m, v in zip(mods, saved):
+        if v is not None:
+            m.spatial_order = v
+
+
 def _module(g):
     from seistorch_gb300.equations2d import (acoustic, acoustic_habc, acoustic_lsrtm_habc, acoustic_rho_habc,
                                              elastic, vacoustic_habc, vti_habc2)
