@@ -662,7 +662,11 @@ __global__ void elastic_grad_kernel(int nz, int nx, int pitch, int nshots, long 
   }
 }
 
-constexpr int EL_TZ = 32;
+// Rows per band: each warp walks one (shot, 120-column strip, band).  Short
+// bands (many warps in flight) won on the 400 x 900, 32-shot grid: forward
+// 0.62 / 0.71 / 0.74 and reverse 0.57 / 0.62 / 0.60 of measured HBM at
+// 32 / 16 / 8 rows (longer bands that fill whole waves lost further).
+constexpr int EL_TZ = 16, EL_TZ_FWD = 8, EL_TZ_REV = 16;
 
 template <class K>
 void grid_for(K, long long n, int* blocks) {
@@ -677,29 +681,33 @@ void elastic_strip_geometry(int nz, int nx, int* nstrip, int* nband) {
   *nband = (nz + EL_TZ - 1) / EL_TZ;
 }
 
-cudaError_t launch_elastic_fwd(const ElFwdArgs& a, cudaStream_t s) {
+cudaError_t launch_elastic_fwd(const ElFwdArgs& a0, cudaStream_t s) {
+  ElFwdArgs a = a0;
+  a.nband = (a.nz + EL_TZ_FWD - 1) / EL_TZ_FWD;
   const long long warps = (long long)a.nshots * a.nstrip * a.nband;
-  elastic_fwd_kernel<EL_TZ><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(a);
+  elastic_fwd_kernel<EL_TZ_FWD><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_elastic_bwd(const ElBwdArgs& a, int mode, cudaStream_t s) {
+cudaError_t launch_elastic_bwd(const ElBwdArgs& a0, int mode, cudaStream_t s) {
+  ElBwdArgs a = a0;
+  a.nband = (a.nz + EL_TZ_REV - 1) / EL_TZ_REV;
   const long long warps = (long long)a.nshots * a.nstrip * a.nband;
   constexpr size_t smem0 = 4 * 2 * bwd_pre_rows<0>() * 128 * sizeof(float);
   constexpr size_t smem1 = 4 * 2 * bwd_pre_rows<1>() * 128 * sizeof(float);
   static bool set = false;
   if (!set) {
-    cudaError_t e = cudaFuncSetAttribute(elastic_bwd_kernel<EL_TZ, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(elastic_bwd_kernel<EL_TZ_REV, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem0);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(elastic_bwd_kernel<EL_TZ, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+      e = cudaFuncSetAttribute(elastic_bwd_kernel<EL_TZ_REV, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
     if (e != cudaSuccess) return e;
     set = true;
   }
   if (mode == 0)
-    elastic_bwd_kernel<EL_TZ, 0><<<(unsigned)((warps + 3) / 4), 128, smem0, s>>>(a);
+    elastic_bwd_kernel<EL_TZ_REV, 0><<<(unsigned)((warps + 3) / 4), 128, smem0, s>>>(a);
   else
-    elastic_bwd_kernel<EL_TZ, 1><<<(unsigned)((warps + 3) / 4), 128, smem1, s>>>(a);
+    elastic_bwd_kernel<EL_TZ_REV, 1><<<(unsigned)((warps + 3) / 4), 128, smem1, s>>>(a);
   return cudaGetLastError();
 }
 
