@@ -157,6 +157,21 @@ class Acquisition:
         self.rec_z = torch.as_tensor(zz, device=device)
         self.rec_xs = torch.as_tensor(xx, device=device)
 
+    def with_wavelet(self, wavelet):
+        """A copy with another wavelet (same number of rows) that shares this
+        batch's source and receiver tables (a loop already in flight keeps
+        its own wavelet)."""
+        import copy
+        wav = torch.as_tensor(wavelet, dtype=torch.float32, device=self.wavelet.device)
+        if wav.ndim == 1:
+            wav = wav[None]
+        if wav.shape[0] != self.wavelet.shape[0]:
+            raise ValueError("the new wavelet has a different number of rows")
+        other = copy.copy(self)
+        other.wavelet = wav.contiguous()
+        other.nt = int(wav.shape[-1])
+        return other
+
     def struct(self, records=None, nch=1):
         return N.Acquisition(
             N.ptr(self.src_ptr), N.ptr(self.src_z), N.ptr(self.src_x), N.ptr(self.src_wrow),

@@ -48,6 +48,19 @@ class WaveRNN(torch.nn.Module):
         self.reset_probes(receivers)
 
     def _acquisition(self, x, super_source, super_probes, nz, nx, device):
+        # The device tables of the batch's sources and receivers are rebuilt
+        # only when the geometry changes: the key holds every source / probe
+        # module's buffers (storage, in-place version, shape), so reset_geom
+        # or an in-place edit of a coordinate invalidates it; a hit is a
+        # copy with this call's wavelet.
+        key = None
+        if super_source is None and super_probes is None:
+            key = (nz, nx, int(x.shape[0]), bool(self.source_encoding), str(device)) + tuple(
+                (id(m), name, buf.data_ptr(), buf._version, tuple(buf.shape))
+                for m in list(self.sources) + list(self.probes) for name, buf in m.named_buffers())
+            hit = getattr(self, "_acq_cache", None)
+            if hit is not None and hit[0] == key:
+                return hit[1].with_wavelet(x), list(hit[2])
         if super_source is None:
             bidx_source, keys = merge_sources_with_same_keys(self.sources)
             super_source = WaveSource(bidx_source, self.second_order_equation, **keys)
@@ -76,6 +89,8 @@ class WaveRNN(torch.nn.Module):
         if sum(len(r[0]) for r in receivers) != sum(reccounts):
             raise ValueError("receivers refer to shots outside the batch")
         acq = engine.Acquisition(nz, nx, sources, receivers, x, device, src_wrow=wrows)
+        if key is not None:
+            self._acq_cache = (key, acq, reccounts)
         return acq, reccounts
 
     def forward(self, x, omega=10.0, super_source=None, super_probes=None, vp=None):
