@@ -136,7 +136,7 @@ int sgb_cfl_check(int32_t scheme, int32_t order, float vmax, float dt, float h, 
 int sgb_debug_wait_probe(uint32_t polls, int32_t arrive, sgb_stream_t stream);
 
 /* Select the tile-pipeline variants used by later calls (host-only,
- * process-wide): fwd_cfg in [0, 7) and bwd_cfg in [0, 4) index the compiled
+ * process-wide): fwd_cfg in [0, 6) and bwd_cfg in [0, 4) index the compiled
  * (rows per tile, warps per CTA, pipeline stages) variants of the PML
  * forward and adjoint; habc_cfg in [0, 6) those of the second-order HABC
  * forward (plain, Born, viscoacoustic), 0 = the default.  The autotuner

@@ -371,9 +371,8 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
 // the second-order HABC instantiations with two rows per warp run 640
 // threads per SM (registers held to 102), the others 512 (128 registers,
 // no spills)
-// MB > 0: at least MB CTAs per SM (registers capped accordingly)
-template <int R, int TZ, int NWP, int S, bool PT, int SB, int HB = 0, int MB = 0>
-__global__ void __launch_bounds__(32 * NWP, MB > 0 ? MB : (HB != 0 ? ((R == 1 && TZ / NWP <= 2) ? 20 : 16) / NWP : 1))
+template <int R, int TZ, int NWP, int S, bool PT, int SB, int HB = 0>
+__global__ void __launch_bounds__(32 * NWP, HB != 0 ? ((R == 1 && TZ / NWP <= 2) ? 20 : 16) / NWP : 1)
     acoustic_fwd_tile_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                                      const __grid_constant__ CUtensorMap tm_um,
                                                                      const AcStreamArgs a) {
@@ -394,19 +393,19 @@ __global__ void __launch_bounds__(32 * NWP) acoustic_fwd_batch_kernel(const __gr
 struct FwdCfg {
   int tz, nwp, s, sb;
 };
-static const FwdCfg FWD_TILE_CFGS[] = {{16, 4, 3, 1}, {16, 4, 3, 1}, {8, 4, 4, 1}, {32, 8, 2, 1},
-                                       {16, 4, 2, 1}, {8, 4, 3, 1}, {16, 4, 2, 1}};
+static const FwdCfg FWD_TILE_CFGS[] = {{16, 4, 3, 1}, {16, 4, 3, 1}, {8, 4, 4, 1},
+                                       {32, 8, 2, 1}, {16, 4, 2, 1}, {8, 4, 3, 1}};
 
 // Launches the variant on batch b; with s == nullptr and prepare_only it
 // only sets the kernel's shared-memory attribute (done once per variant, and
 // before any stream capture).
-template <int R, int TZ, int NWP, int S, bool PT, int MAXG, int SB = 1, int HB = 0, int MB = 0>
+template <int R, int TZ, int NWP, int S, bool PT, int MAXG, int SB = 1, int HB = 0>
 static cudaError_t fwd_tile_t(const AcFwdBatch<MAXG>& b, cudaStream_t s, bool prepare_only) {
   using Lay = FwdTileLayout<R, TZ, S, PT, MAXG == 1 ? SB : 1>;
   const size_t smem = Lay::BYTES + 128;  // + alignment slack
   static int blocks = 0;
   if constexpr (MAXG == 1) {
-    auto kern = acoustic_fwd_tile_kernel<R, TZ, NWP, S, PT, SB, HB, MB>;
+    auto kern = acoustic_fwd_tile_kernel<R, TZ, NWP, S, PT, SB, HB>;
     if (blocks == 0) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
@@ -441,8 +440,6 @@ static cudaError_t fwd_tile_r(const AcFwdBatch<MAXG>& b, cudaStream_t s, bool pr
     case 3: return fwd_tile_t<R, 32, 8, 2, true>(b, s, prep);
     case 4: return fwd_tile_t<R, 16, 4, 2, true>(b, s, prep);
     case 5: return fwd_tile_t<R, 8, 4, 3, true>(b, s, prep);
-    // variant 4 held to five CTAs per SM (102 registers)
-    case 6: return fwd_tile_t<R, 16, 4, 2, true, MAXG, 1, 0, 5>(b, s, prep);
   }
   return cudaErrorInvalidValue;
 }

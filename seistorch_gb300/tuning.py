@@ -19,9 +19,8 @@ import torch
 
 from . import _native as N
 
-FWD_VARIANTS = [  # (rows per tile, warps, stages, previous field via TMA); the last: the fifth held to 5 CTAs/SM
-    (16, 4, 3, False), (16, 4, 3, True), (8, 4, 4, True), (32, 8, 2, True), (16, 4, 2, True), (8, 4, 3, True),
-    (16, 4, 2, True)]
+FWD_VARIANTS = [  # (rows per tile, warps, stages, previous field via TMA)
+    (16, 4, 3, False), (16, 4, 3, True), (8, 4, 4, True), (32, 8, 2, True), (16, 4, 2, True), (8, 4, 3, True)]
 BWD_VARIANTS = [(8, 4, 2), (8, 2, 2), (16, 4, 2), (8, 4, 3)]
 DEFAULT = (4, 0)
 
