@@ -79,6 +79,41 @@ def test_forward_through_wavernn(dev):
     assert rel_l2(got, g["records"]) < 1e-5
 
 
+def test_wavernn_acquisition_cache_follows_the_geometry(dev):
+    """WaveRNN keeps the batch's source / receiver tables between calls: a
+    second call with a doubled wavelet doubles the records (the cached tables
+    with the new wavelet), reset_geom with the shots in reverse order gives
+    the reference's records in reverse order, and an in-place shift of the
+    receiver coordinates changes them (the cache key follows the buffers)."""
+    from seistorch_gb300 import build_model
+    g = load("acoustic_pml_o4")
+    w = g["width"]
+    vp_int = g["models"]["vp"][w:-w, w:-w]
+    cfg = {"equation": "acoustic", "dtype": "float32",
+           "geom": {"dt": g["dt"], "h": g["h"], "nt": g["nt"], "boundary": {"type": "pml", "width": w},
+                    "multiple": False, "boundary_saving": True, "source_type": ["h1"],
+                    "receiver_type": ["h1"], "spatial_order": 4, "invlist": {"vp": False}}}
+    _, model = build_model(cfg, device=dev, mode="forward", models={"vp": vp_int})
+    srcs = [[int(x) - w, int(z) - w] for z, x in g["src"]]
+    recs = [[[int(x) - w for x in xs], [int(z) - w for z in zs]] for zs, xs in g["receivers"]]
+    wav = torch.tensor(g["wavelet"])[None]
+    records = lambda y: np.stack([t.detach().cpu().numpy() for t in y])
+    model.reset_geom([0, 1], srcs, recs, cfg)
+    first = records(model(wav))
+    twice = records(model(2.0 * wav))
+    assert rel_l2(first, g["records"]) < 1e-5
+    assert rel_l2(twice, 2.0 * first) < 1e-6
+    model.reset_geom([0, 1], srcs[::-1], recs[::-1], cfg)
+    assert rel_l2(records(model(wav)), g["records"][::-1]) < 1e-5
+    with torch.no_grad():
+        for probe in model.probes:
+            for name, buf in probe.named_buffers():
+                if name == "y":
+                    buf.add_(1)  # every receiver one row deeper
+    moved = records(model(wav))
+    assert rel_l2(moved, g["records"][::-1]) > 1e-3
+
+
 @pytest.mark.parametrize("name", ["acoustic_pml_o2", "acoustic_pml_o4", "acoustic_habc_o2"])
 def test_single_step_matches_oracle(dev, name):
     from seistorch_gb300.equations2d import acoustic, acoustic_habc
