@@ -753,8 +753,72 @@ def bench_elastic(args):
             "roofline_forward": {"kernel": "elastic_fwd_kernel", "achieved": fwd_gbs, "frac": fwd_gbs / peak,
                                  "unit": "GB/s", "launch_ms": fwd_ms / nt},
             "gpu_launches": args.steps * (2 * nt + 2), "clocks": clocks.summary()}
+    if not args.no_e2e:
+        line["e2e"] = e2e_models(args, dev, "elastic", "pml", EL_W, EL_DT, EL_H, 2, dict(init_m),
+                                 ("vp", "vs", "rho"), obs.cpu(), 2, wav, src, rec, nt, ["txx", "tzz"], ["vx", "vz"])
     print(json.dumps(line))
     return 0
+
+
+def e2e_models(args, dev, equation, boundary, w, dt, h, order, models, inverted, obs_host, nch, wav, src, rec, nt,
+               src_type, rec_type):
+    """A gradient workload through build_model / WaveRNN / autograd: every
+    step copies the padded models and the observed data from pinned host
+    memory, runs WaveRNN.forward and loss.backward, and copies the inverted
+    models' gradients and the loss back.  models: name -> padded array;
+    inverted: the names whose gradient is taken; obs_host: (nt, shots x nrec,
+    nch) records of the true model."""
+    import torch
+
+    from seistorch_gb300 import build_model
+    from seistorch_gb300.postprocess import L2
+
+    names = list(models)
+    cfg = {"equation": equation, "dtype": "float32",
+           "geom": {"dt": dt, "h": h, "nt": nt, "boundary": {"type": boundary, "width": w},
+                    "multiple": False, "boundary_saving": True, "source_type": list(src_type),
+                    "receiver_type": list(rec_type), "spatial_order": order,
+                    "invlist": {k: k in inverted for k in names}}}
+    _, model = build_model(cfg, device=dev, mode="inversion",
+                           models={k: np.asarray(models[k])[w:-w, w:-w] for k in names})
+    srcs = [[x - w, z - w] for [(z, x)] in src]
+    recs = [[[x - w for x in xs], [z - w for z in zs]] for zs, xs in rec]
+    model.reset_geom(list(range(len(srcs))), srcs, recs, cfg)
+    shots, nrec = len(src), len(rec[0][0])
+    hosts = {k: torch.tensor(np.asarray(models[k]), dtype=torch.float32).pin_memory() for k in names}
+    obs_pinned = obs_host.reshape(nt, shots, nrec, nch).permute(1, 0, 2, 3).contiguous().pin_memory()
+    wav_host = torch.tensor(wav)[None].pin_memory()
+    grads_host = {k: torch.empty_like(hosts[k]).pin_memory() for k in inverted}
+    loss_host = torch.empty(1).pin_memory()
+    params = {k: getattr(model.cell.geom, k) for k in names}
+
+    def step():
+        with torch.no_grad():
+            for k in names:
+                params[k].copy_(hosts[k].to(dev, non_blocking=True))
+        for k in inverted:
+            params[k].grad = None
+        obs = obs_pinned.to(dev, non_blocking=True)
+        y = model(wav_host.to(dev, non_blocking=True))
+        loss = L2()(torch.stack(list(y.data)), obs)
+        loss.backward()
+        for k in inverted:
+            grads_host[k].copy_(params[k].grad, non_blocking=True)
+        loss_host.copy_(loss.detach().reshape(1), non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / args.steps
+    nz, nx = hosts[names[0]].shape
+    h2d = sum(t_.numel() for t_ in hosts.values()) * 4 + obs_pinned.numel() * 4 + wav_host.numel() * 4
+    return {"value": shots * nz * nx * nt / wall / 1e9, "unit": "Gpts/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(sum(t_.numel() for t_ in grads_host.values()) * 4 + 4),
+            "ms_per_step": wall * 1e3, "api": "build_model -> WaveRNN.forward -> loss.backward"}
 
 
 # --------------------------------------------------------------- Born ---
@@ -868,6 +932,10 @@ def bench_born(args):
             # per step: 2 NT forward (background, scattered), 2 (NT-1) reverse (far and near tiles), share
             # planes, coefficients, misfit, reduction
             "gpu_launches": args.steps * (2 * nt + 2 * (nt - 1) + 4), "clocks": clocks.summary()}
+    if not args.no_e2e:
+        line["e2e"] = e2e_models(args, dev, "acoustic_lsrtm_habc", "habc", BN_W, BN_DT, BN_H, 2,
+                                 {"vp": v0, "m": 0.5 * m_true}, ("m",), obs.cpu(), 1, wav, src, rec, nt,
+                                 ["h1"], ["sh1"])
     print(json.dumps(line))
     return 0
 
@@ -964,6 +1032,10 @@ def bench_vti(args):
             # per step: NT forward, 2 (NT-1) reverse (far and near tiles), share planes, coefficients,
             # misfit, 2 reductions
             "gpu_launches": args.steps * (nt + 2 * (nt - 1) + 5), "clocks": clocks.summary()}
+    if not args.no_e2e:
+        line["e2e"] = e2e_models(args, dev, "vti_habc2", "habc", BN_W, BN_DT, BN_H, 2,
+                                 dict(zip(("vp", "epsilon", "delta"), init)), ("vp", "epsilon", "delta"),
+                                 obs.cpu(), 1, wav, src, rec, nt, ["p1"], ["p1"])
     print(json.dumps(line))
     return 0
 
@@ -1057,6 +1129,10 @@ def bench_rho(args):
             # per step: NT forward, 2 (NT-1) reverse (far and near tiles), share planes, coefficients,
             # misfit, 5 reductions
             "gpu_launches": args.steps * (nt + 2 * (nt - 1) + 8), "clocks": clocks.summary()}
+    if not args.no_e2e:
+        line["e2e"] = e2e_models(args, dev, "acoustic_rho_habc", "habc", BN_W, BN_DT, BN_H, 2,
+                                 dict(zip(("vp", "rho"), init)), ("vp", "rho"), obs.cpu(), 1, wav, src, rec, nt,
+                                 ["h1"], ["h1"])
     print(json.dumps(line))
     return 0
 

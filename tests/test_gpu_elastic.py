@@ -42,6 +42,28 @@ def _run(g, dev, requires_grad=False, ckpt=0):
     return (vp, vs, rho), per_shot, prop
 
 
+def test_forward_through_wavernn(dev):
+    """The user path for the elastic equation: build_model(dict config) ->
+    WaveRNN -> per-shot records (nt, nrec, vx / vz), against the reference."""
+    from seistorch_gb300 import build_model
+    g = load("elastic")
+    w = g["width"]
+    models = {k: g["models"][k][w:-w, w:-w] for k in ("vp", "vs", "rho")}
+    cfg = {"equation": "elastic", "dtype": "float32",
+           "geom": {"dt": g["dt"], "h": g["h"], "nt": g["nt"], "boundary": {"type": "pml", "width": w},
+                    "multiple": False, "boundary_saving": True, "source_type": list(g["source_type"]),
+                    "receiver_type": list(g["receiver_type"]), "spatial_order": 2,
+                    "invlist": {"vp": False, "vs": False, "rho": False}}}
+    _, model = build_model(cfg, device=dev, mode="forward", models=models)
+    srcs = [[int(x) - w, int(z) - w] for z, x in g["src"]]
+    recs = [[[int(x) - w for x in xs], [int(z) - w for z in zs]] for zs, xs in g["receivers"]]
+    model.reset_geom(list(range(len(srcs))), srcs, recs, cfg)
+    y = model(torch.tensor(g["wavelet"])[None])
+    got = np.stack([t.detach().cpu().numpy() for t in y])
+    assert got.shape == g["records"].shape
+    assert rel_l2(got, g["records"]) < 1e-5
+
+
 @pytest.mark.parametrize("name", ["elastic", "elastic_multiple"])
 def test_forward_matches_reference(dev, name):
     from seistorch_gb300 import elastic_engine, engine
