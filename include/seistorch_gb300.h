@@ -136,9 +136,9 @@ int sgb_cfl_check(int32_t scheme, int32_t order, float vmax, float dt, float h, 
 int sgb_debug_wait_probe(uint32_t polls, int32_t arrive, sgb_stream_t stream);
 
 /* Select the tile-pipeline variants used by later calls (host-only,
- * process-wide): fwd_cfg in [0, 6) and bwd_cfg in [0, 4) index the compiled
- * (rows per tile, warps per CTA, pipeline stages) variants of the PML
- * forward and adjoint; habc_cfg in [0, 6) those of the second-order HABC
+ * process-wide): fwd_cfg in [0, 6) and bwd_cfg in [0, 6) index the compiled
+ * (rows per tile, warps per CTA, pipeline stages, which point operands
+ * travel through the TMA stage) variants of the PML forward and adjoint; habc_cfg in [0, 6) those of the second-order HABC
  * forward (plain, Born, viscoacoustic), 0 = the default.  The autotuner
  * (seistorch_gb300.tuning) times the PML variants per grid. */
 int sgb_set_stream_config(int32_t fwd_cfg, int32_t bwd_cfg, int32_t habc_cfg);

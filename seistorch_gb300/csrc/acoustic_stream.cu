@@ -60,8 +60,8 @@ int plane_map(CUtensorMap* m, const float* p, int nz, int nx, int pitch, int box
 // Variant selection: fwd_cfg / bwd_cfg index the (rows per tile, warps per
 // CTA) tables of acoustic_stream_fwd.cu / acoustic_stream_bwd.cu, habc_cfg
 // the variants of the second-order HABC forward.
-int g_fwd_cfg = 4, g_bwd_cfg = 0, g_habc_fwd_cfg = 0;
-constexpr int N_FWD = 6, N_BWD = 4, N_HABC_FWD = 6;
+int g_fwd_cfg = 4, g_bwd_cfg = 4, g_habc_fwd_cfg = 0;
+constexpr int N_FWD = 6, N_BWD = 6, N_HABC_FWD = 6;
 
 int set_stream_config(int fwd, int bwd, int habc) {
   if (fwd < 0 || fwd >= N_FWD || bwd < 0 || bwd >= N_BWD || habc < 0 || habc >= N_HABC_FWD) return -1;

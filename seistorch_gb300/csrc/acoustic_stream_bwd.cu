@@ -21,23 +21,31 @@
 
 namespace sgb {
 
-template <int R, int TZ, int S>
+// PTM: how the point operands of a tile arrive -- 0: 16-byte global loads
+// issued before the stage wait; 1: U_j and nu_{j+2} in the TMA stage (they
+// land with the stage, S tiles ahead); 2: also the g and k rows.
+template <int R, int TZ, int S, int PTM = 0>
 struct BwdTileLayout {
   static constexpr int UW = Row<R>::W;
   static constexpr int UROWS = TZ + 2 * R;
   static constexpr int UF = round32(UROWS * UW);
   static constexpr int PF = TZ * TX;
-  static constexpr int STAGE = 2 * UF;  // U_{j-1}, nu_{j+1} (haloed)
+  static constexpr int PTB = PTM >= 1 ? 2 * PF : 0;  // U_j, nu_{j+2} rows
+  static constexpr int CTB = PTM >= 2 ? 2 * PF : 0;  // g, k rows
+  static constexpr int STAGE = 2 * UF + PTB + CTB;  // U_{j-1}, nu_{j+1} (haloed), then the point rows
   static constexpr size_t BYTES = (size_t)(S * STAGE + PF) * 4 + S * 8;  // + adjoint-source tile
-  static constexpr uint32_t TX_BYTES = 2 * UROWS * UW * 4;
+  static constexpr uint32_t TX_BYTES = (2 * UROWS * UW + PTB + CTB) * 4;
 };
 
-template <int R, int TZ, int NWP, int S>
-__global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_tile_kernel(
+template <int R, int TZ, int NWP, int S, int PTM>
+__global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? (PTM >= 2 ? 3 : 4) : 1) acoustic_bwd_tile_kernel(
     const __grid_constant__ CUtensorMap tm_u,     // U_{j-1}   box {W, TZ+2R, 1}
     const __grid_constant__ CUtensorMap tm_n,     // nu_{j+1}  box {W, TZ+2R, 1}
+    const __grid_constant__ CUtensorMap tm_up,    // U_j       box {128, TZ, 1} (PTM >= 1)
+    const __grid_constant__ CUtensorMap tm_np,    // nu_{j+2}  box {128, TZ, 1} (PTM >= 1)
+    const __grid_constant__ CUtensorMap tm_c,     // g, k      box {128, TZ, 2} (PTM == 2)
     const AcBwdStreamArgs a) {
-  using Lay = BwdTileLayout<R, TZ, S>;
+  using Lay = BwdTileLayout<R, TZ, S, PTM>;
   constexpr int RPW = TZ / NWP;
   constexpr int UW = Lay::UW, LO = Row<R>::LO;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -56,6 +64,11 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_
     mbar_arrive_expect_tx(&bars[stage], Lay::TX_BYTES);
     tma_load_3d(st, &tm_u, g.x0 - LO, g.z0 - R, g.b, &bars[stage]);
     tma_load_3d(st + Lay::UF, &tm_n, g.x0 - LO, g.z0 - R, g.b, &bars[stage]);
+    if constexpr (PTM >= 1) {
+      tma_load_3d(st + 2 * Lay::UF, &tm_up, g.x0, g.z0, g.b, &bars[stage]);
+      tma_load_3d(st + 2 * Lay::UF + Lay::PF, &tm_np, g.x0, g.z0, g.b, &bars[stage]);
+    }
+    if constexpr (PTM >= 2) tma_load_3d(st + 2 * Lay::UF + Lay::PTB, &tm_c, g.x0, g.z0, 0, &bars[stage]);
   };
   if (tid == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
@@ -79,14 +92,17 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_
 #pragma unroll
     for (int i = 0; i < RPW; ++i) {
       const int z = zw + i;
+      vun[i] = vn2[i] = vg[i] = vk[i] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (xin && z < a.nz) {
         const long long mo = (long long)z * a.pitch + x;
-        vun[i] = ldg4(a.unext + fbase + mo);
-        vn2[i] = ldg4(a.n2 + fbase + mo);
-        vg[i] = ldg4(a.g + mo);
-        vk[i] = ldg4(a.k + mo);
-      } else {
-        vun[i] = vn2[i] = vg[i] = vk[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (PTM == 0) {
+          vun[i] = ldg4(a.unext + fbase + mo);
+          vn2[i] = ldg4(a.n2 + fbase + mo);
+        }
+        if constexpr (PTM <= 1) {
+          vg[i] = ldg4(a.g + mo);
+          vk[i] = ldg4(a.k + mo);
+        }
       }
     }
     // forward sources of time j-1 in this warp's rows, removed from U_j
@@ -142,8 +158,11 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_
         inj = lds4(sinj + lr * TX + 4 * lane);
         sts4(sinj + lr * TX + 4 * lane, make_float4(0.f, 0.f, 0.f, 0.f));
       }
-      float4 un = vun[i];
-      const float4 n2 = vn2[i], g4 = vg[i], k4 = vk[i];
+      const float* sp = st + 2 * Lay::UF + lr * TX + 4 * lane;  // point rows of the stage
+      float4 un = PTM >= 1 ? lds4(sp) : vun[i];
+      const float4 n2 = PTM >= 1 ? lds4(sp + Lay::PF) : vn2[i];
+      const float4 g4 = PTM >= 2 ? lds4(sp + Lay::PTB) : vg[i];
+      const float4 k4 = PTM >= 2 ? lds4(sp + Lay::PTB + Lay::PF) : vk[i];
       const float4 n1 = wn[R], u1 = wu[R];
       float4 nj;
       nj.x = fmaf(k4.x, LN.x + inj.x, fmaf(g4.x, n1.x - n2.x, n2.x));
@@ -209,15 +228,18 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? 4 : 1) acoustic_bwd_
 // ------------------------------------------------------------- launch ---
 
 struct BwdCfg {
-  int tz, nwp, s;
+  int tz, nwp, s, ptm;
 };
-static const BwdCfg BWD_TILE_CFGS[] = {{8, 4, 2}, {8, 2, 2}, {16, 4, 2}, {8, 4, 3}};
+static const BwdCfg BWD_TILE_CFGS[] = {{8, 4, 2, 0}, {8, 2, 2, 0}, {16, 4, 2, 0}, {8, 4, 3, 0},
+                                       {8, 4, 2, 1}, {8, 4, 2, 2}};
 
-template <int R, int TZ, int NWP, int S>
+// maps: U_{j-1} and nu_{j+1} stencil boxes, U_j and nu_{j+2} point boxes,
+// the coefficient rows (the last three read only by the PTM variants)
+template <int R, int TZ, int NWP, int S, int PTM = 0>
 static cudaError_t bwd_tile_t(const CUtensorMap* maps, const AcBwdStreamArgs& a, cudaStream_t s) {
-  using Lay = BwdTileLayout<R, TZ, S>;
+  using Lay = BwdTileLayout<R, TZ, S, PTM>;
   const size_t smem = Lay::BYTES + 128;
-  auto kern = acoustic_bwd_tile_kernel<R, TZ, NWP, S>;
+  auto kern = acoustic_bwd_tile_kernel<R, TZ, NWP, S, PTM>;
   static int blocks = 0;
   if (blocks == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -225,7 +247,8 @@ static cudaError_t bwd_tile_t(const CUtensorMap* maps, const AcBwdStreamArgs& a,
     blocks = resident_blocks(kern, 32 * NWP, smem);
   }
   const int tiles = a.nshots * a.ntx * a.nzc;
-  kern<<<(unsigned)(tiles < blocks ? tiles : blocks), 32 * NWP, smem, s>>>(maps[0], maps[1], a);
+  kern<<<(unsigned)(tiles < blocks ? tiles : blocks), 32 * NWP, smem, s>>>(maps[0], maps[1], maps[2], maps[3],
+                                                                             maps[4], a);
   return cudaGetLastError();
 }
 
@@ -236,6 +259,8 @@ static cudaError_t bwd_tile_r(const CUtensorMap* maps, const AcBwdStreamArgs& a,
     case 1: return bwd_tile_t<R, 8, 2, 2>(maps, a, s);
     case 2: return bwd_tile_t<R, 16, 4, 2>(maps, a, s);
     case 3: return bwd_tile_t<R, 8, 4, 3>(maps, a, s);
+    case 4: return bwd_tile_t<R, 8, 4, 2, 1>(maps, a, s);
+    case 5: return bwd_tile_t<R, 8, 4, 2, 2>(maps, a, s);
   }
   return cudaErrorInvalidValue;
 }

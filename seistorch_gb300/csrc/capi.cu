@@ -860,12 +860,15 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
   // (128 x TZ) of every rotating buffer; lbuf carries nu = k * Lambda
   const int tzr = bwd_tile_rows();
   const int bw = stencil_box_width(R);
-  CUtensorMap uf[3], nf[3];
+  CUtensorMap uf[3], nf[3], up[3], np[3], cm;
   for (int i = 0; i < 3; ++i) {
     if (field_map(&uf[i], ubuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R) ||
-        field_map(&nf[i], lbuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R))
+        field_map(&nf[i], lbuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, bw, tzr + 2 * R) ||
+        field_map(&up[i], ubuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr) ||
+        field_map(&np[i], lbuf[i], grid->nz, grid->nx, grid->pitch, grid->nshots, TX, tzr))
       return SGB_ERR_CUDA;
   }
+  if (coef_map(&cm, model->coef, grid->nz, grid->nx, grid->pitch, tzr)) return SGB_ERR_CUDA;
   if ((acq->nsrc > 0 && acq->src_zr == nullptr) || (acq->records != nullptr && acq->rec_zr == nullptr))
     return SGB_ERR_ARG;
   AcBwdStreamArgs sb;
@@ -906,7 +909,7 @@ int acoustic_backward_impl(const sgb_grid* grid, const sgb_acoustic_model* model
     sb.do_recon = j >= 3;
     sb.t_src = j - 1;
     sb.resid = acq->records ? acq->records + (long long)(j - 1) * acq->nrec * acq->nch : nullptr;
-    const CUtensorMap maps[2] = {uf[ujm1], nf[l1]};
+    const CUtensorMap maps[5] = {uf[ujm1], nf[l1], up[uj], np[l2], cm};
     sb.ring_in = j >= 3 ? bs->ring_store + (long long)(j - 3) * grid->nshots * ring.size : nullptr;
     SGB_CUDA_CHECK(launch_acoustic_bwd_stream(R, maps, sb, s));
     if (ck && j >= 3) {

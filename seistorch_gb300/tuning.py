@@ -21,8 +21,9 @@ from . import _native as N
 
 FWD_VARIANTS = [  # (rows per tile, warps, stages, previous field via TMA)
     (16, 4, 3, False), (16, 4, 3, True), (8, 4, 4, True), (32, 8, 2, True), (16, 4, 2, True), (8, 4, 3, True)]
-BWD_VARIANTS = [(8, 4, 2), (8, 2, 2), (16, 4, 2), (8, 4, 3)]
-DEFAULT = (4, 0)
+BWD_VARIANTS = [  # (rows per tile, warps, stages, point rows via TMA: 0 none, 1 U_j and nu_{j+2}, 2 also g, k)
+    (8, 4, 2, 0), (8, 2, 2, 0), (16, 4, 2, 0), (8, 4, 3, 0), (8, 4, 2, 1), (8, 4, 2, 2)]
+DEFAULT = (4, 4)
 
 _CACHE = {}
 
