@@ -77,6 +77,10 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? (PTM >= 2 ? 3 : 4) :
     for (int s = 0; s < S; ++s)
       if ((int)blockIdx.x + s * G < ntiles) issue(blockIdx.x + s * G, s);
   }
+  // the saved ring of U_{j-2}, each CTA a share while its first boxes load:
+  // the tiles never write ring cells, and nothing in this launch reads U_{j-2}
+  if (a.do_recon && a.ring_in != nullptr)
+    ring_copy_share(a.ring, a.nshots, a.pitch, a.sstride, a.uout, const_cast<float*>(a.ring_in), true);
   for (int i = tid; i < Lay::PF / 4; i += 32 * NWP) sts4(sinj + 4 * i, make_float4(0.f, 0.f, 0.f, 0.f));
   __syncthreads();
   int k = 0;
@@ -213,16 +217,9 @@ __global__ void __launch_bounds__(32 * NWP, TZ / NWP <= 2 ? (PTM >= 2 ? 3 : 4) :
     if (__syncthreads_or(s_abort)) break;  // stage free
     if (tid == 0 && t + S * G < ntiles) issue(t + S * G, stage);
   }
-  if (s_abort) {
-    if (tid == 0)
-      for (int q = k; q < k + S; ++q)
-        if ((int)blockIdx.x + q * G < ntiles) mbar_wait(&bars[q % S], (q / S) & 1, nullptr);
-    return;
-  }
-  // the saved ring of U_{j-2}; the tiles above never write ring cells, and
-  // nothing in this launch reads U_{j-2}
-  if (a.do_recon && a.ring_in != nullptr)
-    ring_copy_share(a.ring, a.nshots, a.pitch, a.sstride, a.uout, const_cast<float*>(a.ring_in), true);
+  if (s_abort && tid == 0)
+    for (int q = k; q < k + S; ++q)
+      if ((int)blockIdx.x + q * G < ntiles) mbar_wait(&bars[q % S], (q / S) & 1, nullptr);
 }
 
 // ------------------------------------------------------------- launch ---

@@ -149,8 +149,13 @@ struct FwdMany {
 // HB: 0 PML; HABC with 1 the plain update (plus the Born / viscoacoustic
 // additive field), 2 VTI (k Lx + kz Lz), 3 variable density (C D(u)) -- one
 // instantiation per equation, so each carries only its own branch
-template <int R, int TZ, int NWP, int S, bool PT, int SB, class P, int HB = 0>
-__device__ __forceinline__ void fwd_tiles(const P& prov) {
+// pre(): work of every thread between the first boxes' issue and the first
+// stage wait (their load latency covers it)
+struct NoPre {
+  __device__ __forceinline__ void operator()() const {}
+};
+template <int R, int TZ, int NWP, int S, bool PT, int SB, class P, int HB = 0, class Pre = NoPre>
+__device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{}) {
   static_assert(SB == 1 || PT, "several shots per tile need the previous field in the stage");
   using Lay = FwdTileLayout<R, TZ, S, PT, SB>;
   constexpr int RPW = TZ / NWP;
@@ -180,6 +185,7 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
     for (int s = 0; s < S; ++s)
       if ((int)blockIdx.x + s * G < ntiles) issue(blockIdx.x + s * G, s);
   }
+  pre();
   __syncthreads();
   int k = 0;
   for (int t = blockIdx.x; t < ntiles; t += G, ++k) {
@@ -369,18 +375,20 @@ __device__ __forceinline__ void fwd_tiles(const P& prov) {
 }
 
 // the second-order HABC instantiations with two rows per warp run 640
-// threads per SM (registers held to 102), the others 512 (128 registers,
-// no spills)
+// threads per SM (registers held to 102), the others, and the PML ones, 512
+// (128 registers)
 template <int R, int TZ, int NWP, int S, bool PT, int SB, int HB = 0>
-__global__ void __launch_bounds__(32 * NWP, HB != 0 ? ((R == 1 && TZ / NWP <= 2) ? 20 : 16) / NWP : 1)
+__global__ void __launch_bounds__(32 * NWP, HB != 0 ? ((R == 1 && TZ / NWP <= 2) ? 20 : 16) / NWP : 16 / NWP)
     acoustic_fwd_tile_kernel(const __grid_constant__ CUtensorMap tm_u,
                                                                      const __grid_constant__ CUtensorMap tm_um,
                                                                      const AcStreamArgs a) {
-  fwd_tiles<R, TZ, NWP, S, PT, SB, FwdOne<SB>, HB>(FwdOne<SB>{&tm_u, &tm_um, a});
-  // the input field's boundary ring for the adjoint, spread over the CTAs'
-  // tails (the input is read-only in this launch)
-  if (a.ring_dst != nullptr)
-    ring_copy_share(a.ring, a.nshots, a.pitch, a.sstride, const_cast<float*>(a.ring_src), a.ring_dst, false);
+  // the input field's boundary ring for the adjoint, each CTA a share while
+  // its first boxes load (the input is read-only in this launch)
+  auto ring = [&]() {
+    if (a.ring_dst != nullptr)
+      ring_copy_share(a.ring, a.nshots, a.pitch, a.sstride, const_cast<float*>(a.ring_src), a.ring_dst, false);
+  };
+  fwd_tiles<R, TZ, NWP, S, PT, SB, FwdOne<SB>, HB>(FwdOne<SB>{&tm_u, &tm_um, a}, ring);
 }
 
 template <int R, int TZ, int NWP, int S, bool PT, int MAXG>

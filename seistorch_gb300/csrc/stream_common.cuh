@@ -123,16 +123,36 @@ __device__ __forceinline__ void apply_sources(const WarpSrc& s, int i, int lane,
 
 // This CTA's share of a boundary-ring copy between a field
 // [nshots][nz][pitch] and its slots [nshots][ring.size] (slot order of
-// Ring::index): scatter = slots -> field, else field -> slots.
+// Ring::index): scatter = slots -> field, else field -> slots.  Four
+// elements per thread and round: their loads are issued together.
 __device__ __forceinline__ void ring_copy_share(const Ring& ring, int nshots, int pitch, long long sstride,
                                                 float* field, float* slots, bool scatter) {
   const long long n = (long long)nshots * ring.size;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  auto cell_ptr = [&](long long i) -> float* {
     const int b = (int)(i / ring.size);
     int z, x;
     ring.cell((int)(i - (long long)b * ring.size), z, x);
-    float* f = field + b * sstride + (long long)z * pitch + x;
+    return field + b * sstride + (long long)z * pitch + x;
+  };
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    float* f[4];
+    float v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) f[q] = cell_ptr(i + q * stride);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = scatter ? slots[i + q * stride] : *f[q];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (scatter)
+        *f[q] = v[q];
+      else
+        slots[i + q * stride] = v[q];
+    }
+  }
+  for (; i < n; i += stride) {
+    float* f = cell_ptr(i);
     if (scatter)
       *f = slots[i];
     else
