@@ -212,6 +212,13 @@ __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{})
         vm[i] = vg[i] = vk[i] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
+    // source rows of the tile's shots, read before the stage wait as well
+    int2 szr[SB];
+#pragma unroll
+    for (int sb = 0; sb < SB; ++sb) {
+      szr[sb] = make_int2(0, 0);
+      if (a.src_ptr != nullptr && b0 + sb < a.nshots) szr[sb] = __ldg(reinterpret_cast<const int2*>(a.src_zr) + b0 + sb);
+    }
     unsigned rec_shots = 0;  // bit sb: shot b0 + sb has receivers in this band
     if (a.records != nullptr) {
 #pragma unroll
@@ -235,12 +242,9 @@ __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{})
         for (int i = 0; i < RPW; ++i) vm[i] = lds4(st + Lay::UF + sb * Lay::PSHOT + (lr0 + i) * TX + 4 * lane);
       }
       WarpSrc src{0u, -1, 0, 0.f};
-      if (a.src_ptr != nullptr) {
-        const int2 zr = __ldg(reinterpret_cast<const int2*>(a.src_zr) + b);
-        if (zr.x < zw + RPW && zr.y > zw)
-          src = warp_sources(lane, b, zw, RPW, g.x0, a.src_ptr, a.src_z, a.src_x, a.src_wrow, a.wavelet, a.nt,
-                             a.t, a.status);
-      }
+      if (a.src_ptr != nullptr && szr[sb].x < zw + RPW && szr[sb].y > zw)
+        src = warp_sources(lane, b, zw, RPW, g.x0, a.src_ptr, a.src_z, a.src_x, a.src_wrow, a.wavelet, a.nt, a.t,
+                           a.status);
       float4 win[2 * R + 1];
 #pragma unroll
       for (int j = 0; j < 2 * R; ++j) win[j] = lds4(su + (lr0 + j) * UW + LO + 4 * lane);
