@@ -332,6 +332,12 @@ def main():
         "roofline_forward": {"kernel": "acoustic_fwd_tile_kernel", "achieved": fwd_bytes / (fwd_launch_ms * 1e-3) / 1e9,
                              "frac": fwd_bytes / (fwd_launch_ms * 1e-3) / 1e9 / peak, "unit": "GB/s",
                              "launch_ms": fwd_launch_ms},
+        # the whole forward+adjoint step: 44 B per shot-point and time step
+        # (forward 12 + reconstruction 12 + adjoint 12 + gradient 8) plus the
+        # shared coefficient planes, over the step's wall time on the device
+        "roofline_step": {"achieved": (fwd_bytes * NT + bwd_bytes * (NT - 1)) / (ms_step * 1e-3) / 1e9,
+                          "frac": (fwd_bytes * NT + bwd_bytes * (NT - 1)) / (ms_step * 1e-3) / 1e9 / peak,
+                          "unit": "GB/s", "bytes_per_step": fwd_bytes * NT + bwd_bytes * (NT - 1)},
         # per step: NT forward, NT-1 reverse, coefficients, misfit, gradient reduction
         "gpu_launches": args.steps * (NT + (NT - 1) + 3),
         "clocks": clocks.summary(),
