@@ -74,6 +74,10 @@ __device__ __forceinline__ HabcW habc_weights(int z, int x, int nz, int nx, int 
 
 struct HabcBwdArgs {
   int nz, nx, pitch, nshots, hw, multiple, R;
+  // tile grid (ntx strips of HT_X columns, nzb bands of HT_Z rows) and the
+  // block of far tiles, strips [fx0, fx1) x bands [fz0, fz1): the far
+  // launch covers that block, the near launch the frame around it
+  int ntx, nzb, fx0, fx1, fz0, fz1;
   long long sstride;
   const float* __restrict__ la1;   // La_{j+1}
   const float* __restrict__ la2;   // La_{j+2}
@@ -397,7 +401,28 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
   __shared__ __align__(16) float s_l1[NEAR ? ROWS : 1][W];  // La1 and La2 (tiles near a strip only)
   __shared__ __align__(16) float s_l2[NEAR ? ROWS : 1][W];
   const int b = blockIdx.z;
-  const int z0 = blockIdx.y * HT_Z, x0 = blockIdx.x * HT_X;
+  int strip, band;
+  if constexpr (!NEAR) {
+    strip = a.fx0 + (int)blockIdx.x;
+    band = a.fz0 + (int)blockIdx.y;
+  } else {  // the frame: the bands above the far block, the strips beside it, the bands below
+    int i = blockIdx.x;
+    const int top = a.fz0 * a.ntx, nside = a.ntx - (a.fx1 - a.fx0), mid = (a.fz1 - a.fz0) * nside;
+    if (i < top) {
+      band = i / a.ntx;
+      strip = i - band * a.ntx;
+    } else if (i - top < mid) {
+      i -= top;
+      band = a.fz0 + i / nside;
+      const int j = i - (i / nside) * nside;
+      strip = j < a.fx0 ? j : a.fx1 + (j - a.fx0);
+    } else {
+      i -= top + mid;
+      band = a.fz1 + i / a.ntx;
+      strip = i - (i / a.ntx) * a.ntx;
+    }
+  }
+  const int z0 = band * HT_Z, x0 = strip * HT_X;
   const long long fb = (long long)b * a.sstride;
   const float* l1 = a.la1 + fb;
   const float* u1 = a.ujm1 + fb;
@@ -901,12 +926,40 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
   if (R > HT_H) return cudaErrorInvalidValue;
   const int eq = rho_c != nullptr ? 2 : (kz != nullptr ? 1 : 0);
   if (eq == 2 && R != 1) return cudaErrorInvalidValue;  // variable density: 2nd order only
-  const dim3 grid((unsigned)((g.nx + HT_X - 1) / HT_X), (unsigned)((g.nz + HT_Z - 1) / HT_Z), (unsigned)g.nshots);
+  // the far tiles (out of reach of every strip: the kernel's own test, per
+  // band and per strip) form one block of bands x strips; the rest is the
+  // frame around it
+  const int HR = R < 2 ? 2 : R;
+  a.ntx = (g.nx + HT_X - 1) / HT_X;
+  a.nzb = (g.nz + HT_Z - 1) / HT_Z;
+  auto near_band = [&](int bz) {
+    const int z0 = bz * HT_Z;
+    return a.hw > 0 && ((!a.multiple && z0 - HR <= a.hw) || z0 + HT_Z + HR >= a.nz - 1 - a.hw);
+  };
+  auto near_strip = [&](int sx) {
+    const int x0 = sx * HT_X;
+    return a.hw > 0 && (x0 - HT_H <= a.hw || x0 + HT_X + HT_H >= a.nx - 1 - a.hw);
+  };
+  a.fz0 = 0;
+  while (a.fz0 < a.nzb && near_band(a.fz0)) ++a.fz0;
+  a.fz1 = a.fz0;
+  while (a.fz1 < a.nzb && !near_band(a.fz1)) ++a.fz1;
+  a.fx0 = 0;
+  while (a.fx0 < a.ntx && near_strip(a.fx0)) ++a.fx0;
+  a.fx1 = a.fx0;
+  while (a.fx1 < a.ntx && !near_strip(a.fx1)) ++a.fx1;
+  if (a.fz1 == a.fz0 || a.fx1 == a.fx0) {  // no far tiles
+    a.fz0 = a.fz1 = a.nzb;
+    a.fx0 = a.fx1 = 0;
+  }
+  const int nfar = (a.fx1 - a.fx0) * (a.fz1 - a.fz0), nnear = a.ntx * a.nzb - nfar;
+  const dim3 gfar((unsigned)(a.fx1 - a.fx0), (unsigned)(a.fz1 - a.fz0), (unsigned)g.nshots);
+  const dim3 gnear((unsigned)nnear, 1u, (unsigned)g.nshots);
   // one launch for the tiles out of reach of the strips, one for the rest
   switch (R * 3 + eq) {
-#define SGB_TILE2(RR, EQ)                                                    \
-  habc_bwd_tile_kernel<RR, EQ, false><<<grid, dim3(32, HT_Z), 0, s>>>(a); \
-  if (a.hw > 0) habc_bwd_tile_kernel<RR, EQ, true><<<grid, dim3(32, HT_Z), 0, s>>>(a);
+#define SGB_TILE2(RR, EQ)                                                                    \
+  if (nfar > 0) habc_bwd_tile_kernel<RR, EQ, false><<<gfar, dim3(32, HT_Z), 0, s>>>(a);    \
+  if (nnear > 0) habc_bwd_tile_kernel<RR, EQ, true><<<gnear, dim3(32, HT_Z), 0, s>>>(a);
     case 3: SGB_TILE2(1, 0) break;
     case 4: SGB_TILE2(1, 1) break;
     case 5: SGB_TILE2(1, 2) break;
