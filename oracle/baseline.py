@@ -1,6 +1,6 @@
 """Timed CPU baseline of the acoustic L2-gradient step (oracle port).
 
-TEST / BASELINE INFRASTRUCTURE ONLY (see ``oracle/__init__.py``): used by
+TEST AND CPU-BASELINE INFRASTRUCTURE ONLY (see ``oracle/__init__.py``): used by
 ``bench.py`` as the CPU baseline and as its ``--impl reference`` arm.
 
 The reference's own implementation is Python on PyTorch and is not shipped
