@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(256) habc_step_vjp_kernel(const HabcVjpArgs a)
 // residuals, the gradient term and the reconstruction inside the box, the
 // saved ring (or 0) outside it.
 template <int R, int EQ, bool NEAR>
-__global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a) {
+__device__ __forceinline__ void habc_bwd_tile(const HabcBwdArgs& a) {
   constexpr bool VTI = EQ == 1, RHO = EQ == 2;
   static_assert(!RHO || R == 1, "variable density is second order");
   // row halo: the stencil's R, and 2 for the one-way lines (q - d, q - 2d)
@@ -850,6 +850,27 @@ __global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a)
   if (a.uout != nullptr) *reinterpret_cast<float4*>(a.uout + fb + o) = make_float4(uo[0], uo[1], uo[2], uo[3]);
 }
 
+// The plain / Born equation's kernel is left to the compiler's register
+// choice; the VTI and variable-density ones are held to the CTAs per SM
+// (eight warps each) that their registers allowed before the tile index
+// came from the far block or the frame: near tiles four (variable density
+// two), far tiles three (VTI of order 6 and 8 two).
+template <int R, int EQ, bool NEAR>
+constexpr int habc_bwd_min_blocks() {
+  if (NEAR) return EQ == 2 ? 2 : 4;
+  if (EQ == 2) return 3;
+  return R <= 2 ? 3 : 2;
+}
+template <int R, int EQ, bool NEAR>
+__global__ void __launch_bounds__(256) habc_bwd_tile_kernel(const HabcBwdArgs a) {
+  habc_bwd_tile<R, EQ, NEAR>(a);
+}
+template <int R, int EQ, bool NEAR>
+__global__ void __launch_bounds__(256, habc_bwd_min_blocks<R, EQ, NEAR>()) habc_bwd_tile_kernel_held(
+    const HabcBwdArgs a) {
+  habc_bwd_tile<R, EQ, NEAR>(a);
+}
+
 
 // The static shares of every cell: wi and the four sides' b * share.
 __global__ void habc_shares_kernel(int nz, int nx, int pitch, int hw, int mult, const float* __restrict__ hb,
@@ -957,9 +978,14 @@ cudaError_t launch_habc_bwd(const sgb_grid& g, const sgb_acoustic_model& m, cons
   const dim3 gnear((unsigned)nnear, 1u, (unsigned)g.nshots);
   // one launch for the tiles out of reach of the strips, one for the rest
   switch (R * 3 + eq) {
-#define SGB_TILE2(RR, EQ)                                                                    \
-  if (nfar > 0) habc_bwd_tile_kernel<RR, EQ, false><<<gfar, dim3(32, HT_Z), 0, s>>>(a);    \
-  if (nnear > 0) habc_bwd_tile_kernel<RR, EQ, true><<<gnear, dim3(32, HT_Z), 0, s>>>(a);
+#define SGB_TILE2(RR, EQ)                                                                           \
+  if constexpr (EQ == 0) {                                                                        \
+    if (nfar > 0) habc_bwd_tile_kernel<RR, EQ, false><<<gfar, dim3(32, HT_Z), 0, s>>>(a);         \
+    if (nnear > 0) habc_bwd_tile_kernel<RR, EQ, true><<<gnear, dim3(32, HT_Z), 0, s>>>(a);        \
+  } else {                                                                                        \
+    if (nfar > 0) habc_bwd_tile_kernel_held<RR, EQ, false><<<gfar, dim3(32, HT_Z), 0, s>>>(a);    \
+    if (nnear > 0) habc_bwd_tile_kernel_held<RR, EQ, true><<<gnear, dim3(32, HT_Z), 0, s>>>(a);   \
+  }
     case 3: SGB_TILE2(1, 0) break;
     case 4: SGB_TILE2(1, 1) break;
     case 5: SGB_TILE2(1, 2) break;
