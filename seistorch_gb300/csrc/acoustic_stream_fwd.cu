@@ -200,6 +200,8 @@ __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{})
     // point operands of this warp's rows, issued before the stage wait (the
     // coefficient rows serve every shot of the tile)
     float4 vm[RPW], vg[RPW], vk[RPW];
+    float4 vkz[HB == 2 ? RPW : 1];  // VTI: the kz rows as well
+    float4 vrc[HB == 3 ? RPW : 1][5];  // variable density: the C, bx+, bx-, bz+, bz- rows
 #pragma unroll
     for (int i = 0; i < RPW; ++i) {
       const int z = zw + i;
@@ -208,8 +210,18 @@ __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{})
         if (!PT) vm[i] = ldg4(a.um + (long long)b0 * a.sstride + mo);
         vg[i] = ldg4(a.g + mo);
         vk[i] = ldg4(a.k + mo);
+        if constexpr (HB == 2) vkz[i] = ldg4(a.kz + mo);
+        if constexpr (HB == 3) {
+#pragma unroll
+          for (int q = 0; q < 5; ++q) vrc[i][q] = ldg4(a.rho_c + q * (long long)a.nz * a.pitch + mo);
+        }
       } else {
         vm[i] = vg[i] = vk[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (HB == 2) vkz[i] = vm[i];
+        if constexpr (HB == 3) {
+#pragma unroll
+          for (int q = 0; q < 5; ++q) vrc[i][q] = vm[i];
+        }
       }
     }
     // source rows of the tile's shots, read before the stage wait as well
@@ -258,12 +270,8 @@ __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{})
         const float4 c = win[R];
         float4 y;
         if constexpr (HB == 3 && R == 1) {  // variable density: g (u - u-) + u- + C D(u)
-          const long long po = (long long)z * a.pitch + x, pl = (long long)a.nz * a.pitch;
-          const bool in = xin && z < a.nz;
-          const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-          const float4 C4 = in ? ldg4(a.rho_c + po) : z4, bxp = in ? ldg4(a.rho_c + pl + po) : z4;
-          const float4 bxn = in ? ldg4(a.rho_c + 2 * pl + po) : z4, bzp = in ? ldg4(a.rho_c + 3 * pl + po) : z4;
-          const float4 bzn = in ? ldg4(a.rho_c + 4 * pl + po) : z4;
+          const int ii = HB == 3 ? i : 0;
+          const float4 C4 = vrc[ii][0], bxp = vrc[ii][1], bxn = vrc[ii][2], bzp = vrc[ii][3], bzn = vrc[ii][4];
           const float xs[6] = {srow[LO - 1 + 4 * lane], c.x, c.y, c.z, c.w, srow[LO + 4 + 4 * lane]};
 #pragma unroll
           for (int m = 0; m < 4; ++m) {
@@ -275,7 +283,7 @@ __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{})
         } else if constexpr (HB == 2) {  // VTI: k Lx + kz Lz
           float4 Lx, Lz;
           lap_row_xz<R>(win, srow, lane, a.w, Lx, Lz);
-          const float4 vz = (xin && z < a.nz) ? ldg4(a.kz + (long long)z * a.pitch + x) : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 vz = vkz[HB == 2 ? i : 0];
 #pragma unroll
           for (int m = 0; m < 4; ++m)
             set_comp(y, m, fmaf(comp(vk[i], m), comp(Lx, m), fmaf(comp(vz, m), comp(Lz, m),
