@@ -202,6 +202,11 @@ __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{})
     float4 vm[RPW], vg[RPW], vk[RPW];
     float4 vkz[HB == 2 ? RPW : 1];  // VTI: the kz rows as well
     float4 vrc[HB == 3 ? RPW : 1][5];  // variable density: the C, bx+, bx-, bz+, bz- rows
+    // plain HABC equation with an additive field (the Born scattered step,
+    // the viscoacoustic term): its rows; else the Born background's m rows
+    float4 vbn[HB == 1 ? RPW : 1];
+    const float* bnp = nullptr;
+    if constexpr (HB == 1) bnp = a.born_in != nullptr ? a.born_in + (long long)b0 * a.sstride : a.born_m;
 #pragma unroll
     for (int i = 0; i < RPW; ++i) {
       const int z = zw + i;
@@ -211,6 +216,8 @@ __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{})
         vg[i] = ldg4(a.g + mo);
         vk[i] = ldg4(a.k + mo);
         if constexpr (HB == 2) vkz[i] = ldg4(a.kz + mo);
+        if constexpr (HB == 1) vbn[i] = (bnp != nullptr && (a.born_in != nullptr || a.born_out != nullptr))
+                                            ? ldg4(bnp + mo) : make_float4(0.f, 0.f, 0.f, 0.f);
         if constexpr (HB == 3) {
 #pragma unroll
           for (int q = 0; q < 5; ++q) vrc[i][q] = ldg4(a.rho_c + q * (long long)a.nz * a.pitch + mo);
@@ -218,6 +225,7 @@ __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{})
       } else {
         vm[i] = vg[i] = vk[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         if constexpr (HB == 2) vkz[i] = vm[i];
+        if constexpr (HB == 1) vbn[i] = vm[i];
         if constexpr (HB == 3) {
 #pragma unroll
           for (int q = 0; q < 5; ++q) vrc[i][q] = vm[i];
@@ -297,14 +305,15 @@ __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{})
           y.w = fmaf(vk[i].w, L.w, fmaf(vg[i].w, c.w - vm[i].w, vm[i].w));
           if (HB == 1 && (a.born_out != nullptr || a.born_in != nullptr) && xin && z < a.nz) {
             const long long po = (long long)z * a.pitch + x;
+            const float4 pre = vbn[HB == 1 ? i : 0];
             if (a.born_out != nullptr) {  // m k L(u): the scattered field's source (Born)
-              const float4 mm = ldg4(a.born_m + po);
+              const float4 mm = a.born_in == nullptr ? pre : ldg4(a.born_m + po);
               *reinterpret_cast<float4*>(a.born_out + fbase + po) =
                   make_float4(mm.x * (vk[i].x * L.x), mm.y * (vk[i].y * L.y), mm.z * (vk[i].z * L.z),
                               mm.w * (vk[i].w * L.w));
             }
             if (a.born_in != nullptr) {
-              const float4 sb4 = ldg4(a.born_in + fbase + po);
+              const float4 sb4 = pre;
               y = make_float4(y.x + sb4.x, y.y + sb4.y, y.z + sb4.z, y.w + sb4.w);
             }
           }
