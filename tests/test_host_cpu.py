@@ -56,6 +56,28 @@ def test_host_only_entry_points(lib):
     assert lib.sgb_ring_size(ctypes.byref(g), 50, 70, 50, 90, 0, ctypes.byref(out)) == 1
 
 
+def test_variant_tables_match_the_abi(lib):
+    """Every variant the autotuner names is one sgb_set_stream_config
+    accepts, the next index is refused, and the tuner's default is a valid
+    pair (host-only: nothing is launched)."""
+    from seistorch_gb300 import tuning
+    nf, nb = len(tuning.FWD_VARIANTS), len(tuning.BWD_VARIANTS)
+    try:
+        for f in range(nf):
+            assert lib.sgb_set_stream_config(f, 0, 0) == 0, f
+        for b in range(nb):
+            assert lib.sgb_set_stream_config(0, b, 0) == 0, b
+        for h in range(6):
+            assert lib.sgb_set_stream_config(0, 0, h) == 0, h
+        assert lib.sgb_set_stream_config(nf, 0, 0) != 0
+        assert lib.sgb_set_stream_config(0, nb, 0) != 0
+        assert lib.sgb_set_stream_config(0, 0, 6) != 0
+        assert lib.sgb_set_stream_config(-1, 0, 0) != 0
+        assert 0 <= tuning.DEFAULT[0] < nf and 0 <= tuning.DEFAULT[1] < nb
+    finally:
+        lib.sgb_set_stream_config(tuning.DEFAULT[0], tuning.DEFAULT[1], 0)
+
+
 def test_calls_validate_before_touching_the_gpu(lib):
     from seistorch_gb300 import _native as N
     g = N.Grid(64, 64, 64, 1, 0.001, 10.0)
