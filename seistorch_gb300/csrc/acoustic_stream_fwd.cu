@@ -157,6 +157,7 @@ struct NoPre {
 template <int R, int TZ, int NWP, int S, bool PT, int SB, class P, int HB = 0, class Pre = NoPre>
 __device__ __forceinline__ void fwd_tiles(const P& prov, const Pre& pre = Pre{}) {
   static_assert(SB == 1 || PT, "several shots per tile need the previous field in the stage");
+  static_assert(HB == 0 || SB == 1, "the HABC family runs one shot per tile (its rows are read for shot b0)");
   using Lay = FwdTileLayout<R, TZ, S, PT, SB>;
   constexpr int RPW = TZ / NWP;
   constexpr int UW = Lay::UW, LO = Row<R>::LO;
